@@ -1,0 +1,251 @@
+"""Pins the oracle (``oracle/numpy_ref.py``, ``oracle/torch_ref.py``) against
+
+* golden vectors produced by the reference's own source
+  (``tests/golden/make_golden.py``), and
+* the reference's own property tests on this path, ported onto the oracle:
+  ``tests/test_weno.py:34-166,288-338``, ``tests/test_timestepping.py:26-99``,
+  ``tests/test_convergence.py:395-460``.
+"""
+
+from __future__ import annotations
+
+import pathlib
+from itertools import product
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import numpy_ref as R
+from oracle import torch_ref as T
+
+GOLDEN = pathlib.Path(__file__).parent / "golden"
+
+
+def _load(name):
+    return dict(np.load(GOLDEN / f"{name}.npz"))
+
+
+# {{{ golden vectors from the reference
+
+
+@pytest.mark.parametrize("name", ["sine", "step"])
+@pytest.mark.parametrize("rec", ["wenojs53", "wenojs32", "esweno32"])
+def test_recon_golden(name, rec):
+    g = _load(f"recon_{name}")
+    u = g["u"]
+    s = R.weno_js_53_coefficients() if rec == "wenojs53" else R.weno_js_32_coefficients()
+    eps = 1.0e-6
+    np.testing.assert_array_equal(R.weno_smoothness(s, u), g[f"{rec}_beta"])
+    np.testing.assert_array_equal(R.weno_interp(s, u), g[f"{rec}_uhat"])
+    if rec == "esweno32":
+        omega = R.es_weno_weights(s, u, eps)
+        ul, ur = R.reconstruct_esweno32(s, eps, u)
+    else:
+        omega = R.weno_js_weights(s, u, eps)
+        ul, ur = R.reconstruct_wenojs(s, eps, u)
+    np.testing.assert_array_equal(omega, g[f"{rec}_omega"])
+    np.testing.assert_array_equal(ul, g[f"{rec}_ul"])
+    np.testing.assert_array_equal(ur, g[f"{rec}_ur"])
+
+
+RUNS = [
+    ("config1_rusanov_n256", "rusanov", "burgers", {"tfinal": 1.0}),
+    ("config1_lf_n256", "lf", "burgers", {"tfinal": 1.0}),
+    ("config1_esweno_n256", "esweno", "burgers", {"tfinal": 1.0}),
+    ("fourier_rusanov_n64_s11", "rusanov", "burgers", {"maxit": 40}),
+    ("fourier_rusanov_n96_s12", "rusanov", "burgers", {"maxit": 40}),
+    ("fourier_rusanov_n128_s13", "rusanov", "burgers", {"maxit": 40}),
+    ("fourier_rusanov_n50_s14", "rusanov", "burgers", {"maxit": 40}),
+    ("fourier_lf_n64_s21", "lf", "burgers", {"maxit": 40}),
+    ("fourier_esweno_n64_s22", "esweno", "burgers", {"maxit": 40}),
+    ("lwr_rusanov_n128_s31", "rusanov", "lwr", {"maxit": 60}),
+]
+
+
+def _spec(g, flux_kind, equation):
+    if flux_kind == "esweno":
+        return R.SchemeSpec(flux_kind="esweno", rec="esweno32", eps=float(g["eps"]),
+                            delta=float(g["delta"]), equation=equation)
+    return R.SchemeSpec(flux_kind=flux_kind, rec="wenojs53", eps=1.0e-6, equation=equation)
+
+
+@pytest.mark.parametrize(("name", "flux_kind", "equation", "kw"), RUNS)
+def test_numpy_oracle_runs_golden(name, flux_kind, equation, kw):
+    g = _load(name)
+    n = int(g["n"])
+    grid = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+    spec = _spec(g, flux_kind, equation)
+    if flux_kind == "esweno":
+        eps, delta = R.es_weno_parameters(grid, np.ones_like(grid.x))
+        assert eps == float(g["eps"]) and delta == float(g["delta"])
+    rhs0 = R.apply_operator(spec, grid, g["u0"])
+    np.testing.assert_array_equal(rhs0[3:-3], g["rhs0"][3:-3])
+    assert R.predict_timestep(spec, grid, g["u0"]) == float(g["dt0"])
+    u, dts = R.evolve(spec, grid, g["u0"], theta=1.0, **kw)
+    np.testing.assert_array_equal(np.array(dts), g["dts"])
+    np.testing.assert_array_equal(u[3:-3], g["u"][3:-3])
+
+
+@pytest.mark.parametrize(("name", "flux_kind", "equation", "kw"), RUNS)
+def test_torch_oracle_runs_golden(name, flux_kind, equation, kw):
+    """The torch restatement (used for derivatives) follows the reference to
+    round-off: same final state within 1e-11 with the reference's dt sequence."""
+    g = _load(name)
+    n = int(g["n"])
+    spec = _spec(g, flux_kind, equation)
+    u0 = torch.tensor(g["u0"][3:-3])[None]
+    dts = torch.tensor(g["dts"]).reshape(-1, 1)
+    u, _ = T.forward(u0, 2.0 / n, len(g["dts"]), dts=dts, flux_kind=flux_kind,
+                     rec=spec.rec, eps=spec.eps, delta=spec.delta, equation=equation)
+    err = np.max(np.abs(u[0].numpy() - g["u"][3:-3]))
+    assert err < 1.0e-11, err
+
+
+# }}}
+
+
+# {{{ ports of the reference's property tests
+
+
+@pytest.mark.parametrize("rec_name", ["wenojs32", "wenojs53"])
+def test_weno_smoothness_indicator_vectorization(rec_name):
+    """``tests/test_weno.py:34-108``: loop vs convolution, rtol 2e-15."""
+    rtol = 2.0e-15
+    s = R.weno_js_53_coefficients() if rec_name == "wenojs53" else R.weno_js_32_coefficients()
+    nghosts = s.b.shape[-1] // 2
+    nstencils = s.b.shape[0]
+    stencil = np.arange(-nghosts, nghosts + 1)
+    n = 64 + 2 * nghosts
+    m = np.s_[nghosts:-nghosts]
+    u = np.sin(np.linspace(0.0, 2.0 * np.pi, n))
+
+    beta0 = np.zeros((nstencils, n))
+    for j in range(*m.indices(n)):
+        for i, k in product(range(nstencils), range(s.a.size)):
+            beta0[i, j] += s.a[k] * np.sum(u[j + stencil] * s.b[i, k, ::-1]) ** 2
+    beta1 = R.weno_smoothness(s, u)
+    uhat0 = np.zeros((nstencils, n))
+    for j in range(*m.indices(n)):
+        for i in range(nstencils):
+            uhat0[i, j] = np.sum(u[j + stencil] * s.c[i, ::-1])
+    uhat1 = R.weno_interp(s, u)
+    err = np.linalg.norm(beta0[:, m] - beta1[:, m]) / np.linalg.norm(beta0[:, m])
+    assert err < rtol
+    err = np.linalg.norm(uhat0[:, m] - uhat1[:, m]) / np.linalg.norm(uhat0[:, m])
+    assert err < rtol
+
+
+@pytest.mark.parametrize(("rec_name", "n"), [("wenojs32", 512), ("wenojs53", 128)])
+@pytest.mark.parametrize("is_smooth", [True, False])
+def test_weno_smoothness_indicator(rec_name, n, is_smooth):
+    """``tests/test_weno.py:117-166``."""
+    s = R.weno_js_53_coefficients() if rec_name == "wenojs53" else R.weno_js_32_coefficients()
+    eps = 1.0e-12 if rec_name == "wenojs53" else 1.0e-6
+    nghosts = s.b.shape[-1] // 2
+    n = n + 2 * nghosts
+    m = np.s_[nghosts:-nghosts]
+    theta = np.linspace(0.0, 2.0 * np.pi, n)
+    u = np.sin(theta) if is_smooth else (theta < np.pi).astype(np.float64)
+    omega = R.weno_js_weights(s, u, eps)
+    error = np.max(np.abs(omega[:, m] - s.d))
+    if is_smooth:
+        assert error < 0.1
+    else:
+        assert error > 0.1
+
+
+def test_weno53_smooth_reconstruction_order():
+    """``tests/test_weno.py:288-338`` for WENOJS53 (order 5, EOC >= 4.5)."""
+    hs, el, er = [], [], []
+    s = R.weno_js_53_coefficients()
+
+    def func(x):
+        return np.sin(2.0 * np.pi * x)
+
+    for n in range(32, 256 + 1, 32):
+        grid = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+        u0 = R.cell_average_leggauss(grid, func, order=6)
+        ref = func(grid.f)
+        ul, ur = R.reconstruct_wenojs(s, 1.0e-12, u0)
+        i = grid.i_
+        el.append(np.max(np.abs(ul - ref[:-1])[i]) / np.max(np.abs(ref[:-1][i])))
+        er.append(np.max(np.abs(ur - ref[1:])[i]) / np.max(np.abs(ref[1:][i])))
+        hs.append(grid.dx_min)
+    assert R.estimate_order_of_convergence(np.array(hs), np.array(el)) >= 4.5
+    assert R.estimate_order_of_convergence(np.array(hs), np.array(er)) >= 4.5
+
+
+def test_ssprk33_time_convergence():
+    """``tests/test_timestepping.py:26-99`` for SSPRK33: u' = e^{-t}."""
+    tfinal = 4.0
+    hs, errs = [], []
+    for n in range(2, 7):
+        dt = 1.0 / 2.0**n
+        maxit = int(tfinal / dt)
+        dt = tfinal / maxit + 1.0e-15
+        u = np.array([-1.0])
+        t = 0.0
+        for _ in range(maxit):
+            u = R.ssprk33(lambda t_, u_: np.array([np.exp(-t_)]), dt, t, u)
+            t += dt
+        u_ex = -np.exp(-tfinal)
+        errs.append(abs(u[0] - u_ex) / abs(u_ex))
+        hs.append(dt)
+    assert R.estimate_order_of_convergence(np.array(hs), np.array(errs)) >= 3 - 0.1
+
+
+def test_advection_convergence_wenojs53():
+    """``tests/test_convergence.py:395-460``: periodic linear advection (a = 1)
+    with WENOJS53 (eps 1e-12) and an upwind flux, SSPRK33, dt = 8 h^{5/3},
+    EOC >= 4.5 in the weighted relative L1 norm. For a = 1 > 0 the Rusanov
+    flux with a constant speed is the upwind flux."""
+    hs, errs = [], []
+    for n in range(32, 256 + 1, 32):
+        grid = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+        spec = R.SchemeSpec(flux_kind="rusanov", rec="wenojs53", eps=1.0e-12,
+                            equation="advection")
+        u0 = R.cell_average_leggauss(grid, lambda x: R.ic_sine_sine(grid, x), order=5)
+        tfinal = 1.0
+        dt = 8.0 * (2.0 / n) ** (5.0 / 3.0)
+        maxit = int(tfinal / dt)
+        dt = tfinal / maxit + 1.0e-15
+        ev = None
+        for ev in R.step(lambda t, u: dt, lambda t, u: R.apply_operator(spec, grid, u),
+                         u0, maxit=maxit):
+            pass
+        uhat = R.cell_average_leggauss(grid, lambda x: R.ic_sine_sine(grid, x - tfinal),
+                                       order=5)
+        err = R.norm(grid, ev.u - uhat, p=1, weighted=True) / R.norm(grid, uhat, p=1,
+                                                                     weighted=True)
+        hs.append(grid.dx_min)
+        errs.append(err)
+    assert R.estimate_order_of_convergence(np.array(hs), np.array(errs)) >= 4.5
+
+
+# }}}
+
+
+# {{{ torch oracle derivative checks
+
+
+def test_torch_step_vjp_vs_finite_differences():
+    """The stand-in for ``jax.jacfwd`` (``src/pyshocks/timestepping.py:174``):
+    <p, J v> from autograd matches a central difference along v."""
+    torch.manual_seed(0)
+    n = 64
+    rng = np.random.default_rng(3)
+    grid = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+    u = torch.tensor(R.random_fourier_ic(rng, grid.f)[3:-3])[None]
+    p = torch.randn(1, n, dtype=torch.float64)
+    v = torch.randn(1, n, dtype=torch.float64)
+    dt = float(T.predict_dt(u, 2.0 / n)[0])
+    g = T.step_vjp(u, p, dt, 2.0 / n)
+    h = 1.0e-6
+    fp = T.ssprk33(u + h * v, dt, 2.0 / n)
+    fm = T.ssprk33(u - h * v, dt, 2.0 / n)
+    fd = torch.sum(p * (fp - fm)) / (2 * h)
+    assert abs(float(torch.sum(g * v) - fd)) < 1.0e-7 * max(1.0, abs(float(fd)))
+
+
+# }}}
