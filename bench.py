@@ -1,0 +1,427 @@
+"""Benchmark of the batched WENO5 forward path (one JSON line on rank 0).
+
+Workload (the batched plain-method configuration): B = 4096 inviscid Burgers
+instances on periodic [-1, 1], N drawn uniformly from {1024, 2048, 4096, 8192,
+16384} per instance from the seed, u0 = mean U(-0.5, 0.5) + 8-mode Fourier
+series (amplitudes N(0,1)/k^2, uniform phases) + 0-3 jumps of height U(-1, 1)
+(exact cell averages), WENO-JS5 (eps 1e-6) + Rusanov + SSPRK33, CFL 0.5
+(theta = 1 with the Rusanov estimate), float64, fixed step count.
+
+A "step" is one SSPRK33 step of the whole batch (one persistent kernel launch,
+per-instance dt computed on the device). ``value`` = interior cells x steps /
+second with the state resident in HBM (two 208 MB ping-pong buffers, larger
+than the 129 MB L2, so no flush is needed). ``e2e`` runs the same steps through
+the public API with host buffers: each step copies the batch from pinned host
+memory, resets the plan, steps once and copies the state back.
+
+``--impl reference`` times the CPU restatement of the reference's path
+(``oracle/shocks_ref.c``, OpenMP over instances, all host threads) on a
+bounded sample of the same workload: JAX, the reference's runtime, is not
+installable here, so the reference itself cannot run.
+
+Multi-GPU (torchrun): every rank runs its own full batch (rank-specific seed),
+no data-path collective; the time is the max over ranks (weak scaling).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+SIZES = (1024, 2048, 4096, 8192, 16384)
+BATCH = 4096
+SEED = 20261203
+EPS = 1.0e-6
+THETA = 1.0
+METRIC = "WENO5 cell-steps/s"
+BYTES_PER_CELL_STEP_F64 = 16  # one read + one write of u per fused step
+
+
+def workload_params(seed: int, batch: int = BATCH):
+    """Per-instance sizes and initial-condition parameters from the seed."""
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice(np.array(SIZES), size=batch)
+    params = []
+    for _ in range(batch):
+        m = rng.uniform(-0.5, 0.5)
+        k = np.arange(1, 9)
+        amp = rng.normal(0.0, 1.0, size=8) / k**2
+        phi = rng.uniform(0.0, 2.0 * np.pi, size=8)
+        nj = int(rng.integers(0, 4))
+        h = rng.uniform(-1.0, 1.0, size=nj)
+        xj = rng.uniform(-1.0, 1.0, size=nj)
+        params.append((m, amp, phi, h, xj))
+    return sizes.astype(np.int64), params
+
+
+def initial_state(sizes, params, device):
+    """Exact cell averages of the workload's initial conditions, packed (float64)."""
+    import torch
+
+    chunks = []
+    for n, (m, amp, phi, h, xj) in zip(sizes, params):
+        f = torch.linspace(-1.0, 1.0, int(n) + 1, dtype=torch.float64, device=device)
+        fl, fr = f[:-1], f[1:]
+        hh = fr - fl
+        u = torch.full_like(fl, m)
+        for kk in range(8):
+            k = kk + 1
+            u += amp[kk] * (torch.cos(k * np.pi * fl + phi[kk]) - torch.cos(k * np.pi * fr + phi[kk])) / (
+                k * np.pi * hh)
+        for hj, x in zip(h, xj):
+            u += hj * torch.clamp((fr - x) / hh, 0.0, 1.0)
+        chunks.append(u)
+    return torch.cat(chunks)
+
+
+# {{{ clocks
+
+
+class ClockSampler:
+    """``nvidia-smi`` samples of SM clock and throttle reasons during a region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if self.proc is None or not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    rows.append((float(parts[1]), float(parts[2]), parts[4:9]))
+                except ValueError:
+                    continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for _, _, flags in rows:
+            for nm, fl in zip(names, flags[1:]):
+                if fl.lower() == "active":
+                    reasons.add(nm)
+        load = [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(load), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# }}}
+
+
+def _profile_constants() -> dict:
+    p = ROOT / "profiles" / "roofline_constants.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
+
+
+def _measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
+
+
+def run_cpu_sample(sizes, params, *, n_inst: int, nsteps: int, threads: int = 0):
+    """Time the C restatement of the reference path on the first *n_inst*
+    instances for *nsteps* steps (best of 3); returns (cell-steps/s, threads)."""
+    import torch
+
+    from oracle import c_ref
+
+    sub_sizes = sizes[:n_inst]
+    u0 = initial_state(sub_sizes, params[:n_inst], "cpu").numpy()
+    off = np.zeros(n_inst + 1, dtype=np.int64)
+    off[1:] = np.cumsum(sub_sizes)
+    dx = 2.0 / sub_sizes.astype(np.float64)
+    c_ref.run_batch(u0, off, dx, theta=THETA, eps=EPS, nsteps=1, nthreads=threads)  # warm-up
+    best = None
+    used = 1
+    for _ in range(3):
+        t0 = time.perf_counter()
+        _, _, used = c_ref.run_batch(u0, off, dx, theta=THETA, eps=EPS, nsteps=nsteps,
+                                     nthreads=threads)
+        el = time.perf_counter() - t0
+        best = el if best is None else min(best, el)
+    del torch
+    return float(off[-1]) * nsteps / best, used
+
+
+def bench_reference(args, rank: int) -> None:
+    if rank != 0:
+        return
+    sizes, params = workload_params(SEED)
+    n_inst = args.cpu_instances
+    vals = []
+    used = 1
+    for i in range(args.warmup + args.steps):
+        rate, used = run_cpu_sample(sizes, params, n_inst=n_inst, nsteps=1)
+        if i >= args.warmup:
+            vals.append(rate)
+    value = float(np.median(vals))
+    cells = int(np.sum(sizes[:n_inst]))
+    sample = (f"first {n_inst} of the {BATCH} seeded instances ({cells} cells), one SSPRK33 "
+              f"step per timed step, best of 3")
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "cell-steps/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * cells / value,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": _config(args),
+        "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": used, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": ("the reference runs on JAX, which is not installable in this image; the "
+                 "timed CPU code is the C restatement of its path (oracle/shocks_ref.c)"),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def _config(args) -> dict:
+    return {
+        "workload": "batched plain WENO-JS5+Rusanov+SSPRK33 Burgers, B=4096, "
+                    "N~U{1024..16384}, CFL 0.5, periodic",
+        "batch": BATCH,
+        "sizes": list(SIZES),
+        "seed": SEED,
+        "eps": EPS,
+        "theta": THETA,
+        "precision": "float64",
+        "l2": "state (2 x 208 MB ping-pong) larger than the 129 MB L2; no flush",
+        "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
+    }
+
+
+def bench_gpu(args, rank: int, world: int) -> None:
+    import torch
+
+    import pyshocks_gb300 as gb
+    from pyshocks_gb300 import _lib as L
+    from pyshocks_gb300.batched import BatchedSolver
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sizes, params = workload_params(SEED + rank)
+    cells = int(np.sum(sizes))
+    rec = gb.reconstruction.make_reconstruction_from_name("wenojs53", eps=EPS)
+    scheme = gb.burgers.make_scheme_from_name("rusanov", rec=rec)
+    u0 = initial_state(sizes, params, dev)
+    solver = BatchedSolver(scheme, sizes, 2.0 / sizes.astype(np.float64), theta=THETA)
+    stream = torch.cuda.Stream(device=dev)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    with torch.cuda.stream(stream):
+        solver.reset(u0)
+        # warm-up (also captures the two-step graph)
+        solver.step(2 * max(1, (args.warmup + 1) // 2), graph=True)
+        stream.synchronize()
+        k = args.steps + (args.steps % 2)
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            e0.record(stream)
+            solver.step(k, graph=True)
+            e1.record(stream)
+            e1.synchronize()
+        torch.cuda.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        status = solver.status()
+    if status:
+        raise RuntimeError(f"step kernel reported status {status}")
+    t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    total_cells = cells * world
+    value = total_cells * k / (ms_max * 1e-3)
+    per_launch_s = ms * 1e-3 / k
+
+    # e2e through the public API with pinned host buffers
+    host_in = u0.cpu().pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    ke = max(2, min(args.steps, 6))
+    with torch.cuda.stream(stream):
+        for _ in range(1):
+            solver.reset(host_in.to(dev, non_blocking=True))
+            solver.step(1)
+            host_out.copy_(solver.u, non_blocking=True)
+        stream.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(ke):
+            dev_in = host_in.to(dev, non_blocking=True)
+            solver.reset(dev_in)
+            solver.step(1)
+            host_out.copy_(solver.u, non_blocking=True)
+        f1.record(stream)
+        f1.synchronize()
+        wall = time.perf_counter() - t0
+        e2e_ms = f0.elapsed_time(f1)
+    # wall clock: host staging, copies and kernels of every e2e step
+    e2e_value = total_cells * ke / max(wall, e2e_ms * 1e-3)
+
+    peaks = _measured_peaks()
+    consts = _profile_constants()
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    if hbm_peak is None:
+        hbm_peak, peak_src = 6800.0, "profiling-recipe fallback 6.8 TB/s (of fallback)"
+    algo_bytes = BYTES_PER_CELL_STEP_F64 * cells
+    achieved = algo_bytes / per_launch_s / 1e9
+    traffic = None
+    if "dram_bytes_per_cell_step" in consts:
+        traffic = consts["dram_bytes_per_cell_step"] * cells
+    fp64_peak = ctypes_fp_peak(L)
+    fp64 = None
+    if "fp64_flop_per_cell_step" in consts and fp64_peak:
+        fl = consts["fp64_flop_per_cell_step"] * cells / per_launch_s
+        fp64 = {"achieved": fl / 1e12, "peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                "frac": fl / fp64_peak, "flop_per_cell_step": consts["fp64_flop_per_cell_step"],
+                "peak_source": "shk_measure_fp_peak FMA chains on this GPU (of measured)"}
+    elif fp64_peak:
+        fp64 = {"peak": fp64_peak / 1e12, "unit": "TFLOP/s",
+                "peak_source": "shk_measure_fp_peak FMA chains on this GPU (of measured)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, used = run_cpu_sample(sizes, params, n_inst=args.cpu_instances, nsteps=1)
+        cpu = {"value": rate, "unit": "cell-steps/s", "cores": used, "kind": "port",
+               "sample": f"first {args.cpu_instances} instances of the batch, one step, "
+                         f"C restatement (oracle/shocks_ref.c), best of 3"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "cell-steps/s",
+            "n_gpus": world,
+            "steps": k,
+            "warmup": args.warmup,
+            "ms_per_step": ms_max / k,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64",
+            "data": "synthetic",
+            "config": _config(args),
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e_value, "unit": "cell-steps/s",
+                    "h2d_bytes_per_step": int(host_in.numel() * 8),
+                    "d2h_bytes_per_step": int(host_out.numel() * 8)},
+            "gpu_launches": k,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic,
+                         "kernel": "batched_step_kernel<double,Burgers,WENOJS53,Rusanov>",
+                         "algo_bytes_per_launch": algo_bytes, "peak_source": peak_src},
+            "fp64_pipe": fp64,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def ctypes_fp_peak(L):
+    import ctypes
+
+    v = ctypes.c_double()
+    st = L.lib().shk_measure_fp_peak(L.SHK_F64, 4096, ctypes.byref(v))
+    return float(v.value) if st == 0 else None
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--cpu-instances", type=int, default=256)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        bench_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    bench_gpu(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

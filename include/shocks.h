@@ -1,0 +1,167 @@
+/*
+ * libshocks -- GB300 (sm_103a) kernels for the 1D scalar conservation-law hot
+ * path of pyshocks: WENO-JS5 / ES-WENO3 reconstruction, Rusanov / global
+ * Lax-Friedrichs / ES-WENO fluxes, SSPRK33 stepping with the CFL time step,
+ * and the discrete adjoint of that step.
+ *
+ * C ABI: plain pointers and sizes, no C++ or torch types. All array pointers
+ * are DEVICE pointers unless the name starts with `h_`. Every call is
+ * asynchronous on `stream` (a cudaStream_t passed as void*; NULL = legacy
+ * default stream) and returns a shk_status; a device-side status word is
+ * read back with shk_plan_status().
+ *
+ * Reference interfaces (alexfikl/pyshocks) each entry point replaces are
+ * cited beside it as src/pyshocks/<file>:<line>.
+ */
+#ifndef SHOCKS_H
+#define SHOCKS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+typedef enum {
+    SHK_OK = 0,
+    SHK_EINVAL = 1,       /* bad argument (the reference raises ValueError)          */
+    SHK_ENONFINITE = 2,   /* "Time step is not finite" (timestepping.py:144-145)     */
+    SHK_ETIMEOUT = 3,     /* a bounded device-side wait expired                     */
+    SHK_ECUDA = 4,        /* a CUDA runtime call failed                              */
+    SHK_ENOMEM = 5,       /* allocation failed (plan creation only)                  */
+    SHK_EUNSUPPORTED = 6  /* combination not implemented                             */
+} shk_status;
+
+/* numerical flux (burgers/schemes.py:98-153,205-256) */
+enum { SHK_FLUX_RUSANOV = 0, SHK_FLUX_LF = 1, SHK_FLUX_ESWENO = 2 };
+/* reconstruction (reconstruction.py:335-348,386-439) */
+enum { SHK_REC_WENOJS53 = 0, SHK_REC_ESWENO32 = 1 };
+/* physical flux f(u) and wave speed f'(u) */
+enum { SHK_EQ_BURGERS = 0, SHK_EQ_ADVECTION = 1, SHK_EQ_LWR = 2 };
+/* state precision */
+enum { SHK_F64 = 0, SHK_F32 = 1 };
+
+/* A scheme on the hot path: the fields of the reference's frozen dataclasses
+ * Rusanov(rec, alpha) / LaxFriedrichs / ESWENO32 and WENOJS53(eps) /
+ * ESWENO32(eps, delta) (reconstruction.py:335-348,386-411). */
+typedef struct {
+    int32_t flux;      /* SHK_FLUX_*                                         */
+    int32_t rec;       /* SHK_REC_*                                          */
+    int32_t equation;  /* SHK_EQ_*                                           */
+    int32_t reserved;
+    double eps;        /* WENO epsilon (WENOJS53 default 1e-12; configs 1e-6) */
+    double delta;      /* ES-WENO delta (bound to dx^2 by burgers bind)       */
+    double nu;         /* Rusanov artificial viscosity dx^(alpha-1); 1 if alpha=1 */
+    double speed;      /* linear advection velocity (SHK_EQ_ADVECTION)        */
+} shk_scheme;
+
+const char* shk_strerror(int status);
+int shk_version(void);
+
+/* ---- single-instance drop-ins (reference ghosted layout, n + 2g cells) -- */
+
+/* max over the n interior cells of |f'(u)| into *amax (device double).
+ * Needed by SHK_FLUX_LF (scalar.py:258-278) and by predict_timestep. */
+int shk_max_wavespeed_f64(const shk_scheme* scheme, const double* u, int64_t n,
+                          int32_t nghosts, double* amax, void* stream);
+
+/* apply_operator (schemes.py:339-346 after scalar.py:529-540 periodic ghost
+ * fill): out[g:n+g] = -(F[i+1/2]-F[i-1/2])/dx. Output ghost cells receive the
+ * periodic image of the interior output. `amax` (device) is read for
+ * SHK_FLUX_LF only (from shk_max_wavespeed_f64 on the same u); may be NULL
+ * otherwise. u and out must not overlap. */
+int shk_apply_operator_f64(const shk_scheme* scheme, const double* u, double* out,
+                           int64_t n, int32_t nghosts, double dx, const double* amax,
+                           void* stream);
+
+/* predict_timestep with the driver's theta (burgers/schemes.py:121-127,
+ * examples/burgers.py:161-162): *dt = theta * (cfl / max|f'(u_interior)|),
+ * cfl = 0.5 * dx^(2 - alpha) computed by the caller. *dt is device memory. */
+int shk_predict_timestep_f64(const shk_scheme* scheme, const double* u, int64_t n,
+                             int32_t nghosts, double cfl, double theta, double* dt,
+                             void* stream);
+
+/* one SSPRK33 step (timestepping.py:312-320, advance() of timestepping.py:218-233)
+ * of a ghosted single instance: u_out = advance(u) with the three stages fused
+ * in one kernel; output ghosts receive the periodic image. */
+int shk_ssprk33_step_f64(const shk_scheme* scheme, const double* u, double* u_out,
+                         int64_t n, int32_t nghosts, double dx, double dt,
+                         void* stream);
+
+/* ---- batched plans ----------------------------------------------------- */
+
+/* A plan owns the device scratch of a batch: per-instance wave-speed maxima,
+ * time, dt history, status word, the (instance, tile) work list, the step
+ * counter and (optionally) a captured CUDA graph. Created once; every
+ * per-step call allocates nothing. Layout of the state buffers it steps:
+ * instance b occupies cells [h_offsets[b], h_offsets[b+1]) of a packed
+ * buffer (interior cells only; periodic wrap is done by the kernels).
+ * Instances whose start and length are multiples of 16 bytes are staged by
+ * TMA bulk copies, others by plain loads. */
+typedef struct shk_plan shk_plan;
+
+typedef struct {
+    int32_t dtype;        /* SHK_F64 / SHK_F32                                  */
+    int32_t tile;         /* cells per work item (0 = default)                  */
+    int32_t max_steps;    /* capacity of the dt history (0 = no history)        */
+    int32_t ctas_per_sm;  /* persistent grid size per SM (0 = occupancy)         */
+} shk_plan_opts;
+
+int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_offsets,
+                    const double* h_dx, const double* h_cfl, double theta,
+                    const shk_plan_opts* opts, shk_plan** out);
+int shk_plan_destroy(shk_plan* plan);
+
+/* reset the batch at time t0 (device, B doubles) with final times tfinal
+ * (device, B doubles; DBL_MAX = no final time, as step() with tfinal=None,
+ * timestepping.py:114-116) and prime the wave-speed maxima from u. */
+int shk_plan_reset(shk_plan* plan, const void* u, const double* t0, const double* tfinal,
+                   void* stream);
+
+/* advance every active instance by `nsteps` SSPRK33 steps (the step() loop of
+ * timestepping.py:128-152 with the CFL dt of burgers/schemes.py:121-127 and the
+ * final-time clip + 1e-15 of timestepping.py:139-142), ping-ponging between
+ * u_a and u_b (caller-owned, same layout). Step k reads the buffer holding
+ * the current state; after an even number of total steps since reset the
+ * state is in u_a, after an odd number in u_b. An instance with t >= tfinal is
+ * copied through unchanged; a non-finite dt sets SHK_ENONFINITE in the status
+ * word and freezes that instance. */
+int shk_plan_step(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps, void* stream);
+
+/* capture two steps (u_a -> u_b -> u_a) into a CUDA graph and replay it
+ * nsteps/2 times (nsteps must be even). */
+int shk_plan_step_graph(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps,
+                        void* stream);
+
+/* device pointers to the plan's per-instance time [B] and dt history
+ * [max_steps][B] (double), and the number of steps taken since reset. */
+int shk_plan_state(shk_plan* plan, double** t, double** dt_hist, int64_t** step_counter);
+
+/* device-to-device copies of the per-instance time [B] and of the whole dt
+ * history [max_steps][B] into caller buffers. */
+int shk_plan_copy_time(shk_plan* plan, double* t_out, void* stream);
+int shk_plan_copy_dt_history(shk_plan* plan, double* out, void* stream);
+
+/* copy the device status word to *h_status (synchronises `stream`). */
+int shk_plan_status(shk_plan* plan, int32_t* h_status, void* stream);
+
+/* FP64 reductions over the batch (grid.py:444-506, conservation checks):
+ * out[b] = sum_i u_b[i] (p = 0), sum |u_b[i]| (p = 1) or max |u_b[i]| (p = -1),
+ * accumulated in double for either state precision. */
+int shk_plan_reduce(shk_plan* plan, const void* u, int32_t p, double* out, void* stream);
+
+/* ---- measurement ------------------------------------------------------- */
+
+/* peak FMA throughput of the FP64 (dtype SHK_F64) or FP32 (SHK_F32) pipe of
+ * the current device in flop/s (2 per FMA), from independent FMA chains on
+ * every SM timed with CUDA events (synchronous; allocates a small buffer).
+ * No reference counterpart: it is the roofline denominator of the FP64-bound
+ * kernels. */
+int shk_measure_fp_peak(int32_t dtype, int32_t iters, double* flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SHOCKS_H */

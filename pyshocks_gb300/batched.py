@@ -1,0 +1,187 @@
+"""Batched stepping of thousands of independent instances of uneven size.
+
+A :class:`BatchedSolver` wraps one ``shk_plan`` of ``libshocks.so``: a packed
+device buffer of all instances' interior cells (``offsets[B+1]``), per-instance
+``dx``, CFL constant, time, final time and dt history, stepped by a persistent
+kernel that fuses the three SSPRK33 stages, computes the next step's CFL dt on
+the device and never returns to the host between steps. It is the batched form
+of ``step()`` (``src/pyshocks/timestepping.py:89-152``) with the Rusanov CFL
+estimate (``src/pyshocks/burgers/schemes.py:121-127``).
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import Sequence
+
+import numpy as np
+import torch
+
+from pyshocks_gb300 import _lib as L
+
+_DTYPES = {torch.float64: L.SHK_F64, torch.float32: L.SHK_F32}
+
+
+def pack_offsets(sizes: Sequence[int]) -> np.ndarray:
+    """``offsets[B+1]`` of a contiguous packing of instances of *sizes* cells."""
+    off = np.zeros(len(sizes) + 1, dtype=np.int64)
+    off[1:] = np.cumsum(np.asarray(sizes, dtype=np.int64))
+    return off
+
+
+class BatchedSolver:
+    """Persistent batched SSPRK33 solver for one scheme on periodic domains.
+
+    :arg scheme: a scheme of :mod:`pyshocks_gb300.burgers` (not the global
+        Lax-Friedrichs flux, whose per-stage global maximum forbids fusing).
+    :arg sizes: number of interior cells of every instance.
+    :arg dx: cell size per instance (or a scalar).
+    :arg theta: Courant factor of the driver closure ``theta * predict_timestep``.
+    :arg dtype: ``torch.float64`` or ``torch.float32`` state.
+    :arg max_steps: capacity of the per-step dt history (for the adjoint).
+    """
+
+    def __init__(
+        self,
+        scheme,
+        sizes: Sequence[int],
+        dx: float | Sequence[float],
+        *,
+        theta: float = 1.0,
+        dtype: torch.dtype = torch.float64,
+        tile: int = 0,
+        max_steps: int = 0,
+        ctas_per_sm: int = 0,
+        device: str | torch.device = "cuda",
+    ):
+        if dtype not in _DTYPES:
+            raise TypeError(f"unsupported dtype {dtype}")
+        self.lib = L.lib()
+        self.scheme = scheme
+        self.sizes = np.asarray(sizes, dtype=np.int64)
+        self.B = int(self.sizes.size)
+        self.offsets = pack_offsets(self.sizes)
+        self.total = int(self.offsets[-1])
+        dxs = np.broadcast_to(np.asarray(dx, dtype=np.float64), (self.B,)).copy()
+        self.dx = dxs
+        self.cfl = np.array([scheme.cfl_constant(float(h)) for h in dxs], dtype=np.float64)
+        self.theta = float(theta)
+        self.dtype = dtype
+        self.device = torch.device(device)
+        self.max_steps = int(max_steps)
+        self._cs = scheme.c_scheme(float(dxs[0]))
+        opts = L.ShkPlanOpts(dtype=_DTYPES[dtype], tile=int(tile), max_steps=self.max_steps,
+                             ctas_per_sm=int(ctas_per_sm))
+        plan = ctypes.c_void_p()
+        L.check(
+            self.lib.shk_plan_create(
+                self._cs, self.B, self.offsets.ctypes.data, dxs.ctypes.data,
+                self.cfl.ctypes.data, self.theta, ctypes.byref(opts), ctypes.byref(plan)),
+            "plan_create",
+        )
+        self._plan = plan
+        self.buf_a = torch.zeros(self.total, dtype=dtype, device=self.device)
+        self.buf_b = torch.zeros(self.total, dtype=dtype, device=self.device)
+        self._steps = 0
+
+    def __del__(self):
+        plan = getattr(self, "_plan", None)
+        if plan is not None and plan.value:
+            try:
+                torch.cuda.synchronize()
+                self.lib.shk_plan_destroy(plan)
+            except Exception:
+                pass
+            self._plan = None
+
+    # {{{ state
+
+    @property
+    def u(self) -> torch.Tensor:
+        """Packed current state (a view of the solver's buffer)."""
+        return self.buf_a if self._steps % 2 == 0 else self.buf_b
+
+    @property
+    def steps(self) -> int:
+        return self._steps
+
+    def instance(self, b: int, u: torch.Tensor | None = None) -> torch.Tensor:
+        u = self.u if u is None else u
+        return u[int(self.offsets[b]) : int(self.offsets[b + 1])]
+
+    def time(self) -> torch.Tensor:
+        """Per-instance time (a copy, float64)."""
+        out = torch.empty(self.B, dtype=torch.float64, device=self.device)
+        L.check(self.lib.shk_plan_copy_time(self._plan, out.data_ptr(), L.stream_handle()))
+        return out
+
+    def dt_history(self) -> torch.Tensor:
+        """``(steps, B)`` time steps taken (0 for inactive instances)."""
+        if not self.max_steps:
+            raise RuntimeError("solver created with max_steps=0")
+        n = min(self._steps, self.max_steps)
+        out = torch.empty((self.max_steps, self.B), dtype=torch.float64, device=self.device)
+        L.check(self.lib.shk_plan_copy_dt_history(self._plan, out.data_ptr(), L.stream_handle()))
+        return out[:n]
+
+    def status(self) -> int:
+        st = ctypes.c_int32()
+        L.check(self.lib.shk_plan_status(self._plan, ctypes.byref(st), L.stream_handle()))
+        return int(st.value)
+
+    def check_status(self) -> None:
+        st = self.status()
+        if st & L.ERR_NONFINITE:
+            raise ValueError("Time step is not finite (an instance was frozen)")
+        if st & L.ERR_TIMEOUT:
+            raise RuntimeError("bounded device wait expired in the step kernel")
+
+    # }}}
+
+    def reset(self, u0: torch.Tensor, *, t0=None, tfinal=None) -> None:
+        """Load the packed initial state (any device/dtype) and reset time.
+        *tfinal* ``None`` means no final time (the reference's ``finfo.max``)."""
+        self.buf_a.copy_(u0.reshape(-1).to(self.buf_a))
+        t0d = _per_instance(t0, self.B, self.device, 0.0)
+        tfd = _per_instance(tfinal, self.B, self.device, float(np.finfo(np.float64).max))
+        self._steps = 0
+        L.check(
+            self.lib.shk_plan_reset(self._plan, self.buf_a.data_ptr(), t0d.data_ptr(),
+                                    tfd.data_ptr(), L.stream_handle()),
+            "plan_reset",
+        )
+        self._keep = (t0d, tfd)
+
+    def step(self, nsteps: int = 1, *, graph: bool = False) -> torch.Tensor:
+        """Advance all active instances by *nsteps* SSPRK33 steps."""
+        stream = L.stream_handle()
+        if graph and nsteps >= 2 and self._steps % 2 == 0 and stream != 0:
+            n2 = nsteps - nsteps % 2
+            L.check(self.lib.shk_plan_step_graph(self._plan, self.buf_a.data_ptr(),
+                                                 self.buf_b.data_ptr(), n2, stream), "plan_step_graph")
+            self._steps += n2
+            nsteps -= n2
+        if nsteps:
+            L.check(self.lib.shk_plan_step(self._plan, self.buf_a.data_ptr(),
+                                           self.buf_b.data_ptr(), nsteps, stream), "plan_step")
+            self._steps += nsteps
+        return self.u
+
+    def reduce(self, p: int = 0, u: torch.Tensor | None = None) -> torch.Tensor:
+        """Per-instance FP64 ``sum u`` (p=0), ``sum |u|`` (p=1) or ``max |u|``
+        (p=-1), deterministic order."""
+        u = self.u if u is None else u
+        out = torch.empty(self.B, dtype=torch.float64, device=self.device)
+        L.check(self.lib.shk_plan_reduce(self._plan, u.data_ptr(), int(p), out.data_ptr(),
+                                         L.stream_handle()), "plan_reduce")
+        return out
+
+
+def _per_instance(v, B, device, default) -> torch.Tensor:
+    if v is None:
+        return torch.full((B,), default, dtype=torch.float64, device=device)
+    t = torch.as_tensor(v, dtype=torch.float64, device=device)
+    if t.dim() == 0:
+        t = t.expand(B)
+    return t.contiguous().clone()
+

@@ -1,0 +1,267 @@
+"""Schemes on the GB300 path (mirrors ``src/pyshocks/burgers/schemes.py`` plus
+the flux plug-ins used by the batched workloads).
+
+Each scheme class is the reference's frozen dataclass; ``apply_operator``,
+``predict_timestep`` and ``numerical_flux`` are registered with CUDA
+implementations from ``libshocks.so``. The physical flux is selected by the
+class: Burgers ``u^2/2`` (``burgers/schemes.py:37-39``), linear advection
+``c u`` and LWR traffic ``u (1 - u)`` (the plug-in pattern of
+``examples/traffic-flow-model.py:14-39``).
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, fields, replace
+from typing import Any, ClassVar
+
+import torch
+
+from pyshocks_gb300 import _lib as L
+from pyshocks_gb300 import reconstruction as rec_mod
+from pyshocks_gb300.grid import Grid
+from pyshocks_gb300.scalar import PeriodicBoundary
+from pyshocks_gb300.schemes import (
+    Boundary,
+    ConservationLawScheme,
+    SchemeBase,
+    apply_operator,
+    bind,
+    flux,
+    predict_timestep,
+)
+
+
+@dataclass(frozen=True)
+class GpuConservationLawScheme(ConservationLawScheme):
+    """Base of the schemes whose operator runs in ``libshocks.so``."""
+
+    equation_code: ClassVar[int] = L.SHK_EQ_BURGERS
+    flux_code: ClassVar[int] = L.SHK_FLUX_RUSANOV
+
+    @property
+    def speed(self) -> float:
+        return 1.0
+
+    def nu_for(self, dx: float) -> float:
+        """Artificial viscosity factor of the Rusanov flux (1 by default)."""
+        return 1.0
+
+    def cfl_constant(self, dx: float) -> float:
+        """``0.5 dx^(2 - alpha)`` of the CFL estimate."""
+        return 0.5 * dx
+
+    def c_scheme(self, dx: float = 1.0) -> L.ShkScheme:
+        rec = self.rec
+        s = L.ShkScheme()
+        s.flux = self.flux_code
+        s.rec = getattr(rec, "code", -1)
+        s.equation = self.equation_code
+        s.eps = float(getattr(rec, "eps", 1.0e-6))
+        s.delta = float(getattr(rec, "delta", 0.0))
+        s.nu = float(self.nu_for(dx))
+        s.speed = float(self.speed)
+        if s.rec < 0:
+            raise NotImplementedError(f"reconstruction {rec.name!r} is not on the GB300 path")
+        return s
+
+
+# {{{ Burgers
+
+
+@dataclass(frozen=True)
+class BurgersScheme(GpuConservationLawScheme):
+    """``src/pyshocks/burgers/schemes.py:29-34``."""
+
+
+@flux.register(BurgersScheme)
+def _flux_burgers(scheme, t, x, u):
+    return u**2 / 2
+
+
+@dataclass(frozen=True)
+class Rusanov(BurgersScheme):
+    """``src/pyshocks/burgers/schemes.py:98-107``."""
+
+    alpha: float = 1.0
+
+    def nu_for(self, dx: float) -> float:
+        # scalar.py:231-234 on a uniform grid (df = dx)
+        return 1.0 if abs(self.alpha - 1.0) <= 1.0e-8 else dx ** (self.alpha - 1)
+
+    def cfl_constant(self, dx: float) -> float:
+        # burgers/schemes.py:127
+        return 0.5 * dx ** (2 - self.alpha)
+
+
+@dataclass(frozen=True)
+class LaxFriedrichs(Rusanov):
+    """Global Lax-Friedrichs (``src/pyshocks/burgers/schemes.py:136-153``)."""
+
+    flux_code: ClassVar[int] = L.SHK_FLUX_LF
+
+
+@dataclass(frozen=True)
+class ESWENO32(BurgersScheme):
+    """Energy-stable WENO (``src/pyshocks/burgers/schemes.py:205-216``)."""
+
+    flux_code: ClassVar[int] = L.SHK_FLUX_ESWENO
+
+    def __post_init__(self) -> None:
+        if not isinstance(self.rec, rec_mod.ESWENO32):
+            raise TypeError("ESWENO32 scheme requires the ESWENO32 reconstruction.")
+
+
+@bind.register(ESWENO32)
+def _bind_burgers_esweno32(scheme: ESWENO32, grid: Grid, bc: Boundary) -> ESWENO32:
+    """``src/pyshocks/burgers/schemes.py:219-227`` with ``es_weno_parameters``
+    (``src/pyshocks/weno.py:265-281``) on ``u0 = 1``."""
+    i = grid.i_
+    eps = float(torch.sum(grid.dx[i].double() * 1.0)) * grid.dx_min**2
+    delta = grid.dx_min**2
+    return replace(scheme, rec=replace(scheme.rec, eps=eps, delta=delta))
+
+
+# }}}
+
+
+# {{{ linear advection and LWR traffic flow (flux plug-ins)
+
+
+@dataclass(frozen=True)
+class AdvectionRusanov(GpuConservationLawScheme):
+    """Linear advection ``u_t + c u_x = 0`` with the Rusanov flux (for ``c > 0``
+    the upwind flux of the reference's advection Godunov scheme)."""
+
+    velocity: float = 1.0
+    equation_code: ClassVar[int] = L.SHK_EQ_ADVECTION
+
+    @property
+    def speed(self) -> float:
+        return float(self.velocity)
+
+    def cfl_constant(self, dx: float) -> float:
+        return 0.5 * dx
+
+
+@flux.register(AdvectionRusanov)
+def _flux_advection(scheme, t, x, u):
+    return scheme.velocity * u
+
+
+@dataclass(frozen=True)
+class LWRRusanov(GpuConservationLawScheme):
+    """LWR traffic flow ``rho_t + (rho (1 - rho))_x = 0`` with the Rusanov flux
+    and wave speed ``1 - 2 rho``."""
+
+    equation_code: ClassVar[int] = L.SHK_EQ_LWR
+
+
+@flux.register(LWRRusanov)
+def _flux_lwr(scheme, t, x, u):
+    return (1 - u) * u
+
+
+# }}}
+
+
+# {{{ CUDA implementations of the generics
+
+
+def _check_state(grid: Grid, u: torch.Tensor) -> None:
+    if not (isinstance(u, torch.Tensor) and u.is_cuda):
+        raise TypeError("the GB300 path expects a CUDA tensor")
+    if u.dtype != torch.float64:
+        raise TypeError("single-instance entry points are float64 (use BatchedSolver for float32)")
+    if u.dim() != 1 or u.shape[0] != grid.x.shape[0] or not u.is_contiguous():
+        raise ValueError(f"expected a contiguous array of {grid.x.shape[0]} cells")
+
+
+def _check_bc(bc: Boundary) -> None:
+    if not isinstance(bc, PeriodicBoundary):
+        raise NotImplementedError(f"{type(bc).__name__} is not on the GB300 path (periodic only)")
+
+
+@apply_operator.register(GpuConservationLawScheme)
+def _apply_operator_gpu(scheme, grid: Grid, bc: Boundary, t: Any, u: torch.Tensor):
+    """``src/pyshocks/schemes.py:339-346`` in one kernel: periodic ghost fill,
+    reconstruction, numerical flux and flux difference."""
+    _check_bc(bc)
+    _check_state(grid, u)
+    lib = L.lib()
+    cs = scheme.c_scheme(grid.dx_min)
+    g = grid.nghosts
+    n = grid.ncells
+    out = torch.empty_like(u)
+    stream = L.stream_handle()
+    amax = None
+    if scheme.flux_code == L.SHK_FLUX_LF:
+        amax = torch.empty((), dtype=torch.float64, device=u.device)
+        L.check(lib.shk_max_wavespeed_f64(cs, u.data_ptr(), n, g, amax.data_ptr(), stream),
+                "max_wavespeed")
+    L.check(
+        lib.shk_apply_operator_f64(cs, u.data_ptr(), out.data_ptr(), n, g, float(grid.dx_min),
+                                   L.ptr(amax), stream),
+        "apply_operator",
+    )
+    return out
+
+
+@predict_timestep.register(GpuConservationLawScheme)
+def _predict_timestep_gpu(scheme, grid: Grid, bc: Boundary, t: Any, u: torch.Tensor):
+    """``0.5 dx^(2-alpha) / max|f'(u_i)|`` (``src/pyshocks/burgers/schemes.py:121-127``)
+    as a 0-d device tensor."""
+    _check_state(grid, u)
+    lib = L.lib()
+    dt = torch.empty((), dtype=torch.float64, device=u.device)
+    L.check(
+        lib.shk_predict_timestep_f64(scheme.c_scheme(grid.dx_min), u.data_ptr(), grid.ncells, grid.nghosts,
+                                     scheme.cfl_constant(grid.dx_min), 1.0, dt.data_ptr(),
+                                     L.stream_handle()),
+        "predict_timestep",
+    )
+    return dt
+
+
+def ssprk33_step(scheme, grid: Grid, bc: Boundary, dt: float, u: torch.Tensor) -> torch.Tensor:
+    """One fused SSPRK33 step (``src/pyshocks/timestepping.py:312-320``)."""
+    _check_bc(bc)
+    _check_state(grid, u)
+    if scheme.flux_code == L.SHK_FLUX_LF:
+        raise NotImplementedError("fused step of the global Lax-Friedrichs flux")
+    out = torch.empty_like(u)
+    L.check(
+        L.lib().shk_ssprk33_step_f64(scheme.c_scheme(grid.dx_min), u.data_ptr(), out.data_ptr(),
+                                     grid.ncells, grid.nghosts, float(grid.dx_min), float(dt),
+                                     L.stream_handle()),
+        "ssprk33_step",
+    )
+    return out
+
+
+# }}}
+
+
+# {{{ make_scheme_from_name
+
+
+_SCHEMES: dict[str, type[SchemeBase]] = {
+    "default": LaxFriedrichs,
+    "rusanov": Rusanov,
+    "lf": LaxFriedrichs,
+    "esweno32": ESWENO32,
+}
+
+
+def scheme_ids() -> tuple[str, ...]:
+    return tuple(_SCHEMES)
+
+
+def make_scheme_from_name(name: str, **kwargs: Any) -> SchemeBase:
+    """``src/pyshocks/burgers/__init__.py:82-98``."""
+    cls = _SCHEMES.get(name)
+    if cls is None:
+        raise ValueError(f"Scheme {name!r} not found. Try one of {', '.join(scheme_ids())}.")
+    return cls(**{f.name: kwargs[f.name] for f in fields(cls) if f.name in kwargs})
+
+
+# }}}

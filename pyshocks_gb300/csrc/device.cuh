@@ -1,0 +1,281 @@
+// Device-side building blocks of the WENO / flux / SSPRK33 kernels (sm_103a).
+//
+// Arithmetic follows the reference's formulas (alexfikl/pyshocks):
+//   smoothness  src/pyshocks/weno.py:114-140 with the JS53 coefficients :206-244
+//   interpolants src/pyshocks/weno.py:143-157
+//   weights      src/pyshocks/weno.py:247-256 (JS) and :284-296 (ES)
+//   sides        src/pyshocks/reconstruction.py:351-377 (ul is the mirror of ur)
+//   Rusanov      src/pyshocks/scalar.py:192-249
+//   upwind       src/pyshocks/scalar.py:91-132
+//   ES-WENO flux src/pyshocks/burgers/schemes.py:230-256
+//   SSPRK33      src/pyshocks/timestepping.py:312-320
+// reorganised to cut the FP64 instruction count (the FP64 pipe, not HBM,
+// bounds this path on GB300):
+//   * one set of smoothness indicators per cell serves both faces: the
+//     mirrored left reconstruction sees beta_k of the right one as beta_{2-k};
+//   * squares of second differences and half first differences are computed
+//     once per cell and shared by the three sub-stencils of three cells;
+//   * normalised weights d_k/s_k / sum_j d_j/s_j are evaluated in product form
+//     d_k P_k / sum_j d_j P_j with P_k = prod_{j != k} s_j, so one reciprocal of
+//     D_R * D_L serves both faces of a cell (f64 only; f32 divides per face to
+//     stay clear of underflow);
+//   * sub-stencil values are written as v_i + correction, so the reconstruction
+//     is v_i + N/D.
+// These are exact identities; results differ from the reference only by
+// rounding (the oracle tests bound the difference: 1e-10 after hundreds of
+// steps, measured ~4e-14).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/shocks.h"
+
+namespace shk {
+
+enum : int32_t {
+    ERR_NONFINITE = 1,
+    ERR_TIMEOUT = 2,
+    ERR_BOUNDS = 4,
+};
+
+// bounded-wait iteration limit for mbarrier polls (each try_wait may suspend
+// the thread for a short, hardware-defined time)
+constexpr long long kWaitLimit = 1LL << 20;
+
+// ---- bit tricks for max-reductions on |x| (integer pipe, exact) ---------
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+    return static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7fffffffffffffffULL;
+}
+__device__ __forceinline__ unsigned int abs_bits(float x) {
+    return __float_as_uint(x) & 0x7fffffffu;
+}
+__device__ __forceinline__ double from_bits(unsigned long long b) {
+    return __longlong_as_double(static_cast<long long>(b));
+}
+__device__ __forceinline__ float from_bits(unsigned int b) { return __uint_as_float(b); }
+
+template <class T> struct Bits;
+template <> struct Bits<double> { using type = unsigned long long; };
+template <> struct Bits<float> { using type = unsigned int; };
+
+// max(|a|, |b|) without the FP pipe (NaN-free inputs)
+template <class T>
+__device__ __forceinline__ T absmax(T a, T b) {
+    auto x = abs_bits(a), y = abs_bits(b);
+    return from_bits(x > y ? x : y);
+}
+
+// ---- physical fluxes ------------------------------------------------------
+// Burgers f = u^2/2 (src/pyshocks/burgers/schemes.py:37-39), f' = u
+// linear advection f = c u, f' = c
+// LWR traffic f = u (1 - u), f' = 1 - 2 u (examples/traffic-flow-model.py:18-24)
+template <int EQ, class T>
+__device__ __forceinline__ T phys_flux(T u, T c) {
+    if constexpr (EQ == SHK_EQ_BURGERS) return T(0.5) * (u * u);
+    else if constexpr (EQ == SHK_EQ_ADVECTION) return c * u;
+    else return u * (T(1) - u);
+}
+template <int EQ, class T>
+__device__ __forceinline__ T wave_speed(T u, T c) {
+    if constexpr (EQ == SHK_EQ_BURGERS) return u;
+    else if constexpr (EQ == SHK_EQ_ADVECTION) return c;
+    else return fma(T(-2), u, T(1));
+}
+
+// ---- WENO-JS 5/3 reconstruction of one cell -------------------------------
+// Inputs (window arrays, cell c): v_c, half differences H_k = (v_{k+1}-v_k)/2 for
+// k = c-2..c+1, half second differences D_k = H_k - H_{k-1} and
+// Q_k = 13/12 (2 D_k)^2 for k = c-1..c+1.
+// beta_0 = Q_{c-1} + (D_{c-1} + 2 H_{c-1})^2
+// beta_1 = Q_c     + (H_c + H_{c-1})^2
+// beta_2 = Q_{c+1} + (D_{c+1} - 2 H_c)^2
+// which are 13/12 q1^2 + 1/4 q2^2 of src/pyshocks/weno.py:219-228.
+template <class T>
+__device__ __forceinline__ void weno53_cell(T v, T Hm2, T Hm1, T H0, T Hp1, T Dm1, T D0,
+                                            T Dp1, T Qm1, T Q0, T Qp1, T eps, T& ul,
+                                            T& ur) {
+    const T h0 = fma(T(2), Hm1, Dm1);
+    const T h1 = H0 + Hm1;
+    const T h2 = fma(T(-2), H0, Dp1);
+    const T b0 = fma(h0, h0, Qm1);
+    const T b1 = fma(h1, h1, Q0);
+    const T b2 = fma(h2, h2, Qp1);
+    T s0 = eps + b0; s0 = s0 * s0;
+    T s1 = eps + b1; s1 = s1 * s1;
+    T s2 = eps + b2; s2 = s2 * s2;
+    // alpha_k = d_k / s_k (weno.py:254). f64: product form P_k = prod_{j!=k} s_j
+    // (proportional to 1/s_k, no reciprocal); f32: P_k = 1/s_k, which cannot
+    // underflow when eps^4 is below the float range.
+    T P0, P1, P2;
+    if constexpr (sizeof(T) == 8) {
+        P0 = s1 * s2; P1 = s0 * s2; P2 = s0 * s1;
+    } else {
+        P0 = T(1) / s0; P1 = T(1) / s1; P2 = T(1) / s2;
+    }
+    // 6 (uhat_k - v) of the right side (weno.py:231-239), d_k folded (1, 6, 3):
+    //   uhat_0: -2 d_{c-2} + 5 d_{c-1}       -> -4 H_{c-2} + 10 H_{c-1}
+    //   6 uhat_1:  6 (d_{c-1} + 2 d_c)       -> 12 H_{c-1} + 24 H_c
+    //   3 uhat_2:  3 (4 d_c - d_{c+1})       -> 24 H_c - 6 H_{c+1}
+    const T cr0 = fma(T(10), Hm1, T(-4) * Hm2);
+    const T cr1 = fma(T(24), H0, T(12) * Hm1);
+    const T cr2 = fma(T(-6), Hp1, T(24) * H0);
+    // mirrored left side (reconstruction.py:375)
+    const T cl0 = fma(T(-10), H0, T(4) * Hp1);
+    const T cl1 = fma(T(-24), Hm1, T(-12) * H0);
+    const T cl2 = fma(T(-24), Hm1, T(6) * Hm2);
+    const T nr = fma(P0, cr0, fma(P1, cr1, P2 * cr2));
+    const T nl = fma(P2, cl0, fma(P1, cl1, P0 * cl2));
+    const T m = T(36) * P1;
+    const T dr = fma(T(6), P0, fma(T(18), P2, m));
+    const T dl = fma(T(6), P2, fma(T(18), P0, m));
+    if constexpr (sizeof(T) == 8) {
+        const T r = T(1) / (dr * dl);
+        ur = fma(nr * dl, r, v);
+        ul = fma(nl * dr, r, v);
+    } else {
+        ur = v + nr / dr;
+        ul = v + nl / dl;
+    }
+}
+
+// ---- ES-WENO 3/2 reconstruction of one cell (weno.py:284-296) -----------------
+// d = (1/3, 2/3); beta_0 = (v_c - v_{c-1})^2, beta_1 = (v_{c+1} - v_c)^2,
+// tau = (v_{c+1} - 2 v_c + v_{c-1})^2; alpha_k = d_k (1 + tau / (eps + beta_k)).
+// Returns ul, ur and omega_0 of the right side (used by the ES-WENO flux).
+template <class T>
+__device__ __forceinline__ void esweno32_cell(T vm1, T v, T vp1, T eps, T& ul, T& ur,
+                                              T& w0) {
+    const T dm = v - vm1, dp = vp1 - v;
+    const T b0 = dm * dm, b1 = dp * dp;
+    const T dd = dp - dm;
+    const T tau = dd * dd;
+    const T third = T(1) / T(3);
+    const T a0 = third * (T(1) + tau / (eps + b0));
+    const T a1 = (T(2) * third) * (T(1) + tau / (eps + b1));
+    const T sr = a0 + a1;
+    w0 = a0 / sr;
+    const T w1 = a1 / sr;
+    // uhat_0 = 3/2 v_c - 1/2 v_{c-1}, uhat_1 = 1/2 (v_{c+1} + v_c) (weno.py:196-198)
+    ur = w0 * (T(1.5) * v - T(0.5) * vm1) + w1 * (T(0.5) * vp1 + T(0.5) * v);
+    // mirror: beta_0^L = beta_1, beta_1^L = beta_0
+    const T al0 = third * (T(1) + tau / (eps + b1));
+    const T al1 = (T(2) * third) * (T(1) + tau / (eps + b0));
+    const T sl = al0 + al1;
+    ul = (al0 / sl) * (T(1.5) * v - T(0.5) * vp1) + (al1 / sl) * (T(0.5) * vm1 + T(0.5) * v);
+}
+
+// ---- numerical fluxes at face j+1/2 -----------------------------------------
+// R = ur_j, L = ul_{j+1}, vj, vj1 cell values.
+template <int EQ, class T>
+__device__ __forceinline__ T rusanov_face(T R, T L, T vj, T vj1, T hnu, T c) {
+    // F = 1/2 (f(L) + f(R)) - 1/2 a nu (L - R), a = max|f'(v)| of the cells
+    const T a = absmax(wave_speed<EQ>(vj, c), wave_speed<EQ>(vj1, c));
+    const T diss = (hnu * a) * (L - R);
+    if constexpr (EQ == SHK_EQ_BURGERS) {
+        return fma(T(0.25), fma(L, L, R * R), -diss);
+    } else {
+        return fma(T(0.5), phys_flux<EQ>(L, c) + phys_flux<EQ>(R, c), -diss);
+    }
+}
+
+// global Lax-Friedrichs: the wave speed is the instance-wide max (scalar.py:277)
+template <int EQ, class T>
+__device__ __forceinline__ T lf_face(T R, T L, T hnu_amax, T c) {
+    const T diss = hnu_amax * (L - R);
+    if constexpr (EQ == SHK_EQ_BURGERS) {
+        return fma(T(0.25), fma(L, L, R * R), -diss);
+    } else {
+        return fma(T(0.5), phys_flux<EQ>(L, c) + phys_flux<EQ>(R, c), -diss);
+    }
+}
+
+// ES-WENO: upwind flux with a = u (scalar.py:123-132) plus the dissipative
+// g = -(mu + dw/8)(v_{j+1} - v_j), mu = sqrt(dw^2 + delta^2)/8 (burgers/schemes.py:242-251)
+template <int EQ, class T>
+__device__ __forceinline__ T esweno_face(T R, T L, T vj, T vj1, T w0j, T w0j1, T delta,
+                                         T c) {
+    const T aavg = (wave_speed<EQ>(R, c) + wave_speed<EQ>(L, c)) / T(2);
+    const T fnum = aavg > T(0) ? phys_flux<EQ>(R, c) : phys_flux<EQ>(L, c);
+    const T dw = w0j1 - w0j;
+    const T mu = sqrt(dw * dw + delta * delta) / T(8);
+    const T g = -(mu + dw / T(8)) * (vj1 - vj);
+    return fnum + g;
+}
+
+// ---- mbarrier / bulk copy (inline PTX) -------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile(
+        "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+        "r"(bytes)
+        : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+        "[%3];" ::"r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// bounded wait: returns false if the limit expired
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+    for (long long it = 0; it < kWaitLimit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void fence_proxy_async() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// ---- block reductions -------------------------------------------------------
+template <class U>
+__device__ __forceinline__ U warp_max(U x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        U y = __shfl_xor_sync(0xffffffffu, x, o);
+        x = y > x ? y : x;
+    }
+    return x;
+}
+template <class U>
+__device__ __forceinline__ U block_max(U x, U* scratch /* >= 32 */) {
+    x = warp_max(x);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) scratch[warp] = x;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    U y = threadIdx.x < nw ? scratch[threadIdx.x] : U(0);
+    if (warp == 0) y = warp_max(y);
+    return y;  // valid in thread 0
+}
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    return x;
+}
+
+}  // namespace shk

@@ -1,0 +1,980 @@
+// Forward kernels: spatial operator, CFL time step, fused SSPRK33 step, batched
+// persistent stepping with per-instance dt, and the C ABI around them.
+//
+// Reference path replaced (alexfikl/pyshocks):
+//   apply_operator      src/pyshocks/schemes.py:339-346
+//   periodic ghost fill src/pyshocks/scalar.py:529-540
+//   numerical fluxes    src/pyshocks/scalar.py:91-132,192-278,
+//                       src/pyshocks/burgers/schemes.py:98-153,230-256
+//   predict_timestep    src/pyshocks/burgers/schemes.py:42-49,121-127
+//   step / SSPRK33      src/pyshocks/timestepping.py:89-152,312-320
+//
+// Periodic boundaries are applied by circular indexing of the n interior
+// cells: with stencil reach 3 and 3 ghost cells the reference's interior
+// outputs equal the circular ones (its zero padding reaches ghost outputs only).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "device.cuh"
+
+namespace shk {
+
+constexpr int kThreads = 256;
+constexpr int kDefaultTile = 1024;
+
+// halo of a window: 9 cells are needed for three fused stages, rounded up so
+// that the window start stays 16-byte aligned for cp.async.bulk
+template <class T> __host__ __device__ constexpr int step_halo() { return sizeof(T) == 8 ? 10 : 12; }
+template <class T> __host__ __device__ constexpr int op_halo() { return 4; }
+
+__host__ __device__ inline int64_t imin64(int64_t a, int64_t b) { return a < b ? a : b; }
+
+__host__ __device__ inline int64_t imod(int64_t a, int64_t n) {
+    int64_t r = a % n;
+    return r < 0 ? r + n : r;
+}
+
+// ---------------------------------------------------------------------------
+// shared-memory layout of one work item (window of W cells)
+// ---------------------------------------------------------------------------
+template <class T>
+struct Smem {
+    T* U;   // u at the start of the step (window)
+    T* S;   // stage state k1 / k2
+    T* H;   // half differences
+    T* D;   // half second differences; reused for face fluxes F
+    T* Q;   // 13/12 (2D)^2; reused for ES-WENO omega_0
+    T* UL;  // ul (value at the left face of the cell)
+    T* UR;  // ur (value at the right face of the cell)
+
+    __device__ static size_t bytes(int W) { return size_t(7) * W * sizeof(T); }
+    __host__ static size_t host_bytes(int W) { return size_t(7) * W * sizeof(T); }
+    __device__ void carve(unsigned char* base, int W) {
+        T* p = reinterpret_cast<T*>(base);
+        U = p; S = p + W; H = p + 2 * W; D = p + 3 * W; Q = p + 4 * W;
+        UL = p + 5 * W; UR = p + 6 * W;
+    }
+};
+
+template <class T>
+struct OpParams {
+    T eps, delta, hnu, c;  // WENO eps, ES-WENO delta, nu/2, advection speed
+    T hnu_amax;            // LF: nu/2 * global max |f'|
+};
+
+// ---------------------------------------------------------------------------
+// one evaluation of the numerical fluxes F_j (face j+1/2) for j in [lo-1, hi)
+// from the stage input v (valid on [lo-3, hi+3)). Leaves F in sm.D.
+// ---------------------------------------------------------------------------
+template <class T, int EQ, int REC, int FLUX>
+__device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Smem<T>& sm,
+                                            const OpParams<T>& p) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if constexpr (REC == SHK_REC_WENOJS53) {
+        // phase A: H_c = (v_{c+1} - v_c)/2, c in [lo-3, hi+2)
+        for (int c = lo - 3 + tid; c < hi + 2; c += nt) sm.H[c] = T(0.5) * (v[c + 1] - v[c]);
+        __syncthreads();
+        // phase B: D_c = H_c - H_{c-1}, Q_c = 13/12 (2 D_c)^2, c in [lo-2, hi+2)
+        for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
+            const T d = sm.H[c] - sm.H[c - 1];
+            sm.D[c] = d;
+            sm.Q[c] = (T(13.0 / 3.0) * d) * d;
+        }
+        __syncthreads();
+        // phase C: ul, ur of cells [lo-1, hi+1)
+        for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
+            T ul, ur;
+            weno53_cell<T>(v[c], sm.H[c - 2], sm.H[c - 1], sm.H[c], sm.H[c + 1], sm.D[c - 1],
+                           sm.D[c], sm.D[c + 1], sm.Q[c - 1], sm.Q[c], sm.Q[c + 1], p.eps, ul,
+                           ur);
+            sm.UL[c] = ul;
+            sm.UR[c] = ur;
+        }
+        __syncthreads();
+    } else {
+        for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
+            T ul, ur, w0;
+            esweno32_cell<T>(v[c - 1], v[c], v[c + 1], p.eps, ul, ur, w0);
+            sm.UL[c] = ul;
+            sm.UR[c] = ur;
+            sm.Q[c] = w0;
+        }
+        __syncthreads();
+    }
+    // phase D: F_j, j in [lo-1, hi)
+    for (int j = lo - 1 + tid; j < hi; j += nt) {
+        T f;
+        if constexpr (FLUX == SHK_FLUX_RUSANOV) {
+            f = rusanov_face<EQ, T>(sm.UR[j], sm.UL[j + 1], v[j], v[j + 1], p.hnu, p.c);
+        } else if constexpr (FLUX == SHK_FLUX_LF) {
+            f = lf_face<EQ, T>(sm.UR[j], sm.UL[j + 1], p.hnu_amax, p.c);
+        } else {
+            f = esweno_face<EQ, T>(sm.UR[j], sm.UL[j + 1], v[j], v[j + 1], sm.Q[j], sm.Q[j + 1],
+                                   p.delta, p.c);
+        }
+        sm.D[j] = f;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// window loader: cells g0 .. g0+W-1 of a periodic instance (mod n) into dst.
+// Uses cp.async.bulk (TMA 1D, no multicast) into the CTA's own shared memory
+// when every piece is 16-byte aligned, plain coalesced loads otherwise.
+// Returns false if the bulk copy did not complete within the wait limit.
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ bool load_window(T* dst, const T* base, int64_t n, int64_t g0, int W,
+                            uint64_t* bar, uint32_t& phase) {
+    const size_t sz = sizeof(T);
+    bool bulk = (reinterpret_cast<uintptr_t>(base) % 16 == 0) &&
+                (reinterpret_cast<uintptr_t>(dst) % 16 == 0);
+    {
+        int64_t pos = g0;
+        const int64_t end = g0 + W;
+        int npieces = 0;
+        while (pos < end && bulk) {
+            const int64_t src = imod(pos, n);
+            const int64_t len = min(end - pos, n - src);
+            if ((src * sz) % 16 || (len * sz) % 16 || ((pos - g0) * sz) % 16) bulk = false;
+            pos += len;
+            if (++npieces > 8) bulk = false;  // tiny instances: plain loads
+        }
+    }
+    if (!bulk) {
+        for (int w = threadIdx.x; w < W; w += blockDim.x) dst[w] = base[imod(g0 + w, n)];
+        __syncthreads();
+        return true;
+    }
+    // order earlier generic-proxy accesses of dst before the async-proxy writes
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(bar, static_cast<uint32_t>(W * sz));
+        int64_t pos = g0;
+        const int64_t end = g0 + W;
+        while (pos < end) {
+            const int64_t src = imod(pos, n);
+            const int64_t len = min(end - pos, n - src);
+            bulk_g2s(dst + (pos - g0), base + src, static_cast<uint32_t>(len * sz), bar);
+            pos += len;
+        }
+    }
+    bool ok = mbar_wait_bounded(bar, phase);
+    if (!ok) ok = mbar_wait_bounded(bar, phase);  // second bounded wait for copies in flight
+    phase ^= 1u;
+    return __syncthreads_and(ok) != 0;
+}
+
+// ---------------------------------------------------------------------------
+// per-instance CFL time step (timestepping.py:139-145 with the Rusanov
+// estimate of burgers/schemes.py:121-127 and the driver's theta)
+// ---------------------------------------------------------------------------
+struct DtState {
+    double dt;
+    bool active;  // t < tfinal (timestepping.py:133-134)
+    bool finite;
+};
+__host__ __device__ inline DtState compute_dt(double smax, double cfl, double theta, double t,
+                                              double tfinal) {
+    DtState s;
+    s.active = t < tfinal;
+    double dt = theta * (cfl / smax);
+    if (tfinal != INFINITY) {
+        const double dtmin = tfinal - t;
+        dt = (dt < dtmin ? dt : dtmin) + 1.0e-15;
+    }
+    s.dt = dt;
+    s.finite = isfinite(dt);
+    return s;
+}
+
+// ---------------------------------------------------------------------------
+// fused SSPRK33 step of one tile: window [s - HL, s + te + HL) -> u_out[s, s + te)
+// returns the thread's max |f'(u_new)| bits
+// ---------------------------------------------------------------------------
+template <class T, int EQ, int REC, int FLUX>
+__device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, T dtdx,
+                                            const OpParams<T>& p) {
+    constexpr int HL = step_halo<T>();
+    const int tid = threadIdx.x, nt = blockDim.x;
+    // stage 1: k1 = u + dt L(u) on [HL-6, HL+te+6)
+    {
+        const int lo = HL - 6, hi = HL + te + 6;
+        face_fluxes<T, EQ, REC, FLUX>(sm.U, lo, hi, sm, p);
+        for (int i = lo + tid; i < hi; i += nt) sm.S[i] = fma(dtdx, sm.D[i - 1] - sm.D[i], sm.U[i]);
+        __syncthreads();
+    }
+    // stage 2: k2 = 3/4 u + 1/4 (k1 + dt L(k1)) on [HL-3, HL+te+3) (in place over k1)
+    {
+        const int lo = HL - 3, hi = HL + te + 3;
+        face_fluxes<T, EQ, REC, FLUX>(sm.S, lo, hi, sm, p);
+        for (int i = lo + tid; i < hi; i += nt) {
+            const T k = fma(dtdx, sm.D[i - 1] - sm.D[i], sm.S[i]);
+            sm.S[i] = fma(T(1.0 / 4.0), k, T(3.0 / 4.0) * sm.U[i]);
+        }
+        __syncthreads();
+    }
+    // stage 3: u+ = 1/3 u + 2/3 (k2 + dt L(k2)) on the tile
+    using B = typename Bits<T>::type;
+    B mx = 0;
+    {
+        const int lo = HL, hi = HL + te;
+        face_fluxes<T, EQ, REC, FLUX>(sm.S, lo, hi, sm, p);
+        for (int i = lo + tid; i < hi; i += nt) {
+            const T k = fma(dtdx, sm.D[i - 1] - sm.D[i], sm.S[i]);
+            const T un = fma(T(2.0 / 3.0), k, T(1.0 / 3.0) * sm.U[i]);
+            gout[i - HL] = un;
+            const B b = abs_bits(wave_speed<EQ>(un, p.c));
+            mx = b > mx ? b : mx;
+        }
+    }
+    return mx;
+}
+
+// ---------------------------------------------------------------------------
+// batched persistent stepping kernel
+// ---------------------------------------------------------------------------
+struct PlanDev {
+    const int32_t* item_inst;
+    const int32_t* item_tile;
+    const int64_t* offsets;  // [B+1]
+    const double* cfl;       // [B] 0.5 dx^(2-alpha)
+    const double* inv_dx;    // [B]
+    const double* tfinal;    // [B]
+    double theta;
+    unsigned long long* amax;  // [2][B] bits of max |f'(u)| (as double)
+    double* t;                 // [B]
+    double* dt_hist;           // [max_steps][B] or null
+    int64_t* step;
+    unsigned int* done;
+    int32_t* status;
+    double* partial;  // [nitems]
+    int32_t B, nitems, tile, max_steps;
+};
+
+template <class T>
+__device__ __forceinline__ unsigned long long to_double_bits(typename Bits<T>::type b) {
+    if constexpr (sizeof(T) == 8) return b;
+    else return abs_bits(static_cast<double>(from_bits(b)));
+}
+
+__device__ void finalize_step(const PlanDev& P, int64_t k) {
+    const int cur = static_cast<int>(k & 1);
+    for (int b = threadIdx.x; b < P.B; b += blockDim.x) {
+        unsigned long long* am = P.amax + size_t(cur) * P.B + b;
+        const DtState s = compute_dt(from_bits(*am), P.cfl[b], P.theta, P.t[b], P.tfinal[b]);
+        double rec = 0.0;
+        if (s.active) {
+            if (s.finite) {
+                P.t[b] = P.t[b] + s.dt;
+                rec = s.dt;
+            } else {
+                atomicOr(P.status, ERR_NONFINITE);
+            }
+        }
+        if (P.dt_hist && k < P.max_steps) P.dt_hist[size_t(k) * P.B + b] = rec;
+        *am = 0ull;
+    }
+}
+
+template <class T, int EQ, int REC, int FLUX>
+__global__ void __launch_bounds__(kThreads) batched_step_kernel(PlanDev P, const T* __restrict__ uin,
+                                                                T* __restrict__ uout, OpParams<T> p) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ unsigned long long red[32];
+    __shared__ int is_last;
+    constexpr int HL = step_halo<T>();
+    using B = typename Bits<T>::type;
+
+    Smem<T> sm;
+    sm.carve(smem_raw, P.tile + 2 * HL);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const int64_t k = *reinterpret_cast<volatile int64_t*>(P.step);
+    const int cur = static_cast<int>(k & 1), nxt = cur ^ 1;
+    bool ok = true;
+
+    for (int item = blockIdx.x; item < P.nitems && ok; item += gridDim.x) {
+        const int b = P.item_inst[item];
+        const int64_t off = P.offsets[b];
+        const int64_t n = P.offsets[b + 1] - off;
+        const int64_t s0 = int64_t(P.item_tile[item]) * P.tile;
+        const int te = static_cast<int>(imin64(P.tile, n - s0));
+        const DtState ds =
+            compute_dt(from_bits(P.amax[size_t(cur) * P.B + b]), P.cfl[b], P.theta, P.t[b], P.tfinal[b]);
+        B mx = 0;
+        if (!(ds.active && ds.finite)) {
+            // instance finished or frozen: copy the tile through
+            for (int i = threadIdx.x; i < te; i += blockDim.x) {
+                const T v = uin[off + s0 + i];
+                uout[off + s0 + i] = v;
+                const B bb = abs_bits(wave_speed<EQ>(v, p.c));
+                mx = bb > mx ? bb : mx;
+            }
+        } else {
+            ok = load_window<T>(sm.U, uin + off, n, s0 - HL, te + 2 * HL, &bar, phase);
+            if (!ok) {
+                if (threadIdx.x == 0) atomicOr(P.status, ERR_TIMEOUT);
+                break;
+            }
+            const T dtdx = static_cast<T>(ds.dt * P.inv_dx[b]);
+            mx = step_tile<T, EQ, REC, FLUX>(sm, uout + off + s0, te, dtdx, p);
+        }
+        const B bm = block_max<B>(mx, reinterpret_cast<B*>(red));
+        if (threadIdx.x == 0) atomicMax(P.amax + size_t(nxt) * P.B + b, to_double_bits<T>(bm));
+        __syncthreads();
+    }
+
+    // completion: the last CTA of the step advances t, records dt, resets the
+    // consumed maxima and increments the step counter (no host round trip)
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned prev = atomicAdd(P.done, 1u);
+        is_last = (prev == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (is_last) {
+        __threadfence();
+        finalize_step(P, k);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            *reinterpret_cast<volatile unsigned*>(P.done) = 0u;
+            *reinterpret_cast<volatile int64_t*>(P.step) = k + 1;
+            __threadfence();
+        }
+    }
+}
+
+// max |f'(u)| per instance into amax[cur] (plan reset / priming)
+template <class T, int EQ>
+__global__ void __launch_bounds__(kThreads) batched_max_kernel(PlanDev P, const T* __restrict__ u, T c,
+                                                               int slot) {
+    __shared__ unsigned long long red[32];
+    using B = typename Bits<T>::type;
+    for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
+        const int b = P.item_inst[item];
+        const int64_t off = P.offsets[b];
+        const int64_t n = P.offsets[b + 1] - off;
+        const int64_t s0 = int64_t(P.item_tile[item]) * P.tile;
+        const int te = static_cast<int>(imin64(P.tile, n - s0));
+        B mx = 0;
+        for (int i = threadIdx.x; i < te; i += blockDim.x) {
+            const B bb = abs_bits(wave_speed<EQ>(u[off + s0 + i], c));
+            mx = bb > mx ? bb : mx;
+        }
+        const B bm = block_max<B>(mx, reinterpret_cast<B*>(red));
+        if (threadIdx.x == 0) atomicMax(P.amax + size_t(slot) * P.B + b, to_double_bits<T>(bm));
+        __syncthreads();
+    }
+}
+
+// deterministic FP64 reductions: per-item partials, then per-instance ordered sums
+template <class T>
+__global__ void __launch_bounds__(kThreads) batched_partial_kernel(PlanDev P, const T* __restrict__ u,
+                                                                   int mode) {
+    __shared__ double red[32];
+    for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
+        const int b = P.item_inst[item];
+        const int64_t off = P.offsets[b];
+        const int64_t n = P.offsets[b + 1] - off;
+        const int64_t s0 = int64_t(P.item_tile[item]) * P.tile;
+        const int te = static_cast<int>(imin64(P.tile, n - s0));
+        double acc = 0.0;
+        for (int i = threadIdx.x; i < te; i += blockDim.x) {
+            const double v = static_cast<double>(u[off + s0 + i]);
+            if (mode == 0) acc += v;
+            else if (mode == 1) acc += fabs(v);
+            else acc = fmax(acc, fabs(v));
+        }
+        // fixed-shape tree: deterministic for a given launch shape
+        if (mode == -1) {
+            for (int o = 16; o > 0; o >>= 1) acc = fmax(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+        } else {
+            acc = warp_sum(acc);
+        }
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double r = red[0];
+            for (int w = 1; w < (blockDim.x >> 5); ++w) r = mode == -1 ? fmax(r, red[w]) : r + red[w];
+            P.partial[item] = r;
+        }
+        __syncthreads();
+    }
+}
+__global__ void instance_sum_kernel(PlanDev P, const int32_t* item_first, int mode, double* out) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= P.B) return;
+    double r = 0.0;
+    for (int i = item_first[b]; i < item_first[b + 1]; ++i)
+        r = mode == -1 ? fmax(r, P.partial[i]) : r + P.partial[i];
+    out[b] = r;
+}
+
+// ---------------------------------------------------------------------------
+// single-instance kernels on the reference's ghosted layout (n + 2g cells)
+// ---------------------------------------------------------------------------
+template <class T, int EQ, int REC, int FLUX>
+__global__ void __launch_bounds__(kThreads) apply_operator_kernel(const T* __restrict__ u, T* __restrict__ out,
+                                                                  int64_t n, int g, int tile, T dx,
+                                                                  const double* amax, OpParams<T> p,
+                                                                  int32_t* err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    constexpr int HL = op_halo<T>();
+    Smem<T> sm;
+    sm.carve(smem_raw, tile + 2 * HL);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    if constexpr (FLUX == SHK_FLUX_LF) p.hnu_amax = p.hnu * static_cast<T>(*amax);
+    const int64_t s0 = int64_t(blockIdx.x) * tile;
+    const int te = static_cast<int>(imin64(tile, n - s0));
+    if (!load_window<T>(sm.U, u + g, n, s0 - HL, te + 2 * HL, &bar, phase)) {
+        if (threadIdx.x == 0 && err) atomicOr(err, ERR_TIMEOUT);
+        return;
+    }
+    face_fluxes<T, EQ, REC, FLUX>(sm.U, HL, HL + te, sm, p);
+    for (int i = threadIdx.x; i < te; i += blockDim.x) {
+        const int w = HL + i;
+        // -(f[1:] - f[:-1]) / dx  (schemes.py:346)
+        const T r = -(sm.D[w] - sm.D[w - 1]) / dx;
+        const int64_t gi = s0 + i;
+        out[g + gi] = r;
+        // ghost cells of the output: periodic image of the interior output
+        if (gi < g) out[g + n + gi] = r;
+        if (gi >= n - g) out[gi - (n - g)] = r;
+    }
+}
+
+template <class T, int EQ>
+__global__ void max_wavespeed_kernel(const T* __restrict__ u, int64_t n, T c, unsigned long long* out) {
+    __shared__ unsigned long long red[32];
+    using B = typename Bits<T>::type;
+    B mx = 0;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+         i += int64_t(gridDim.x) * blockDim.x) {
+        const B bb = abs_bits(wave_speed<EQ>(u[i], c));
+        mx = bb > mx ? bb : mx;
+    }
+    const B bm = block_max<B>(mx, reinterpret_cast<B*>(red));
+    if (threadIdx.x == 0) atomicMax(out, to_double_bits<T>(bm));
+}
+
+__global__ void finalize_dt_kernel(double* dt, double cfl, double theta) {
+    const double smax = from_bits(*reinterpret_cast<unsigned long long*>(dt));
+    // theta * (0.5 dx^(2-alpha) / smax)   (burgers/schemes.py:127, examples/burgers.py:162)
+    *dt = theta * (cfl / smax);
+}
+
+template <class T, int EQ, int REC, int FLUX>
+__global__ void __launch_bounds__(kThreads) single_step_kernel(const T* __restrict__ u, T* __restrict__ uout,
+                                                               int64_t n, int g, int tile, T dtdx,
+                                                               OpParams<T> p, int32_t* err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    constexpr int HL = step_halo<T>();
+    Smem<T> sm;
+    sm.carve(smem_raw, tile + 2 * HL);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const int64_t s0 = int64_t(blockIdx.x) * tile;
+    const int te = static_cast<int>(imin64(tile, n - s0));
+    if (!load_window<T>(sm.U, u + g, n, s0 - HL, te + 2 * HL, &bar, phase)) {
+        if (threadIdx.x == 0 && err) atomicOr(err, ERR_TIMEOUT);
+        return;
+    }
+    step_tile<T, EQ, REC, FLUX>(sm, uout + g + s0, te, dtdx, p);
+    __syncthreads();
+    // periodic ghost image of the new state
+    for (int i = threadIdx.x; i < te; i += blockDim.x) {
+        const int64_t gi = s0 + i;
+        const T v = uout[g + gi];
+        if (gi < g) uout[g + n + gi] = v;
+        if (gi >= n - g) uout[gi - (n - g)] = v;
+    }
+}
+
+}  // namespace shk
+
+// ===========================================================================
+// host side
+// ===========================================================================
+using namespace shk;
+
+namespace {
+
+cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+int cuda_check(cudaError_t e) {
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "libshocks: CUDA error %s\n", cudaGetErrorString(e));
+        return SHK_ECUDA;
+    }
+    return SHK_OK;
+}
+#define SHK_CUDA(call)                                  \
+    do {                                                \
+        int _st = cuda_check(call);                     \
+        if (_st != SHK_OK) return _st;                  \
+    } while (0)
+
+bool valid_scheme(const shk_scheme* s) {
+    if (!s) return false;
+    if (s->flux < 0 || s->flux > SHK_FLUX_ESWENO) return false;
+    if (s->rec < 0 || s->rec > SHK_REC_ESWENO32) return false;
+    if (s->equation < 0 || s->equation > SHK_EQ_LWR) return false;
+    if ((s->flux == SHK_FLUX_ESWENO) != (s->rec == SHK_REC_ESWENO32)) return false;
+    return true;
+}
+
+template <class T>
+OpParams<T> make_params(const shk_scheme* s) {
+    OpParams<T> p;
+    p.eps = static_cast<T>(s->eps);
+    p.delta = static_cast<T>(s->delta);
+    p.hnu = static_cast<T>(0.5 * s->nu);
+    p.c = static_cast<T>(s->speed);
+    p.hnu_amax = T(0);
+    return p;
+}
+
+int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// dispatch helpers: call F.template operator()<T, EQ, REC, FLUX>()
+template <class T, class F>
+int dispatch_scheme(const shk_scheme* s, F&& f) {
+    switch (s->equation) {
+#define SHK_EQ_CASE(EQ)                                                                 \
+    case EQ:                                                                            \
+        if (s->rec == SHK_REC_ESWENO32) return f.template operator()<T, EQ, SHK_REC_ESWENO32, SHK_FLUX_ESWENO>(); \
+        if (s->flux == SHK_FLUX_LF) return f.template operator()<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_LF>(); \
+        return f.template operator()<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_RUSANOV>();
+        SHK_EQ_CASE(SHK_EQ_BURGERS)
+        SHK_EQ_CASE(SHK_EQ_ADVECTION)
+        SHK_EQ_CASE(SHK_EQ_LWR)
+#undef SHK_EQ_CASE
+    }
+    return SHK_EINVAL;
+}
+
+
+// launch functors (namespace scope: member templates are not allowed in local classes)
+struct ApplyOpLaunch {
+    const double* u; double* out; int64_t n; int g; int tile; double dx; const double* amax;
+    OpParams<double> p; size_t smem; int blocks; cudaStream_t st;
+    template <class T, int EQ, int REC, int FLUX> int operator()() {
+        auto k = apply_operator_kernel<T, EQ, REC, FLUX>;
+        SHK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<blocks, kThreads, smem, st>>>(u, out, n, g, tile, dx, amax, p, nullptr);
+        return cuda_check(cudaGetLastError());
+    }
+};
+
+struct SingleStepLaunch {
+    const double* u; double* uo; int64_t n; int g; int tile; double dtdx;
+    OpParams<double> p; size_t smem; int blocks; cudaStream_t st;
+    template <class T, int EQ, int REC, int FLUX> int operator()() {
+        if constexpr (FLUX == SHK_FLUX_LF) {
+            return SHK_EUNSUPPORTED;
+        } else {
+            auto k = single_step_kernel<T, EQ, REC, FLUX>;
+            SHK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k<<<blocks, kThreads, smem, st>>>(u, uo, n, g, tile, dtdx, p, nullptr);
+            return cuda_check(cudaGetLastError());
+        }
+    }
+};
+
+template <class TS>
+struct BatchedStepLaunch {
+    PlanDev D; const TS* uin; TS* uout; OpParams<TS> p; size_t smem; int grid; cudaStream_t st;
+    template <class T, int EQ, int REC, int FLUX> int operator()() {
+        if constexpr (FLUX == SHK_FLUX_LF) {
+            return SHK_EUNSUPPORTED;
+        } else {
+            auto k = batched_step_kernel<T, EQ, REC, FLUX>;
+            SHK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            k<<<grid, kThreads, smem, st>>>(D, uin, uout, p);
+            return cuda_check(cudaGetLastError());
+        }
+    }
+};
+
+}  // namespace
+
+struct shk_plan {
+    shk_scheme scheme;
+    int dtype = SHK_F64;
+    int B = 0, tile = 0, nitems = 0, max_steps = 0, grid = 0;
+    int64_t total_cells = 0;
+    double theta = 1.0;
+    // device buffers
+    int32_t* item_inst = nullptr;
+    int32_t* item_tile = nullptr;
+    int32_t* item_first = nullptr;
+    int64_t* offsets = nullptr;
+    double* cfl = nullptr;
+    double* inv_dx = nullptr;
+    double* tfinal = nullptr;
+    unsigned long long* amax = nullptr;
+    double* t = nullptr;
+    double* dt_hist = nullptr;
+    int64_t* step = nullptr;
+    unsigned int* done = nullptr;
+    int32_t* status = nullptr;
+    double* partial = nullptr;
+    // host mirror of the number of steps launched since reset
+    int64_t host_steps = 0;
+    // captured two-step graph
+    cudaGraphExec_t graph = nullptr;
+    void* graph_a = nullptr;
+    void* graph_b = nullptr;
+
+    PlanDev dev() const {
+        PlanDev P;
+        P.item_inst = item_inst; P.item_tile = item_tile; P.offsets = offsets; P.cfl = cfl;
+        P.inv_dx = inv_dx; P.tfinal = tfinal; P.theta = theta; P.amax = amax; P.t = t;
+        P.dt_hist = dt_hist; P.step = step; P.done = done; P.status = status;
+        P.partial = partial; P.B = B; P.nitems = nitems; P.tile = tile; P.max_steps = max_steps;
+        return P;
+    }
+};
+
+namespace {
+template <class T>
+int launch_max(shk_plan* P, const void* u, int slot, cudaStream_t st) {
+    const PlanDev D = P->dev();
+    const T c = static_cast<T>(P->scheme.speed);
+    const T* uu = static_cast<const T*>(u);
+    switch (P->scheme.equation) {
+        case SHK_EQ_BURGERS: batched_max_kernel<T, SHK_EQ_BURGERS><<<P->grid, kThreads, 0, st>>>(D, uu, c, slot); break;
+        case SHK_EQ_ADVECTION: batched_max_kernel<T, SHK_EQ_ADVECTION><<<P->grid, kThreads, 0, st>>>(D, uu, c, slot); break;
+        default: batched_max_kernel<T, SHK_EQ_LWR><<<P->grid, kThreads, 0, st>>>(D, uu, c, slot); break;
+    }
+    return cuda_check(cudaGetLastError());
+}
+
+template <class T>
+int launch_step(shk_plan* P, const void* uin, void* uout, cudaStream_t st) {
+    const PlanDev D = P->dev();
+    const size_t smem = Smem<T>::host_bytes(P->tile + 2 * step_halo<T>());
+    OpParams<T> p = make_params<T>(&P->scheme);
+    BatchedStepLaunch<T> f{D, static_cast<const T*>(uin), static_cast<T*>(uout), p, smem, P->grid, st};
+    return dispatch_scheme<T>(&P->scheme, f);
+}
+}  // namespace
+
+extern "C" {
+
+const char* shk_strerror(int status) {
+    switch (status) {
+        case SHK_OK: return "ok";
+        case SHK_EINVAL: return "invalid argument";
+        case SHK_ENONFINITE: return "Time step is not finite";
+        case SHK_ETIMEOUT: return "bounded device wait expired";
+        case SHK_ECUDA: return "CUDA runtime error";
+        case SHK_ENOMEM: return "out of device memory";
+        case SHK_EUNSUPPORTED: return "unsupported scheme combination";
+        default: return "unknown status";
+    }
+}
+
+int shk_version(void) { return 1; }
+
+int shk_max_wavespeed_f64(const shk_scheme* scheme, const double* u, int64_t n, int32_t nghosts,
+                          double* amax, void* stream) {
+    if (!valid_scheme(scheme) || !u || !amax || n <= 0 || nghosts < 0) return SHK_EINVAL;
+    cudaStream_t st = as_stream(stream);
+    SHK_CUDA(cudaMemsetAsync(amax, 0, sizeof(double), st));
+    const int blocks = static_cast<int>(imin64((n + kThreads - 1) / kThreads, 4 * sm_count()));
+    const double c = scheme->speed;
+    auto* out = reinterpret_cast<unsigned long long*>(amax);
+    switch (scheme->equation) {
+        case SHK_EQ_BURGERS: max_wavespeed_kernel<double, SHK_EQ_BURGERS><<<blocks, kThreads, 0, st>>>(u + nghosts, n, c, out); break;
+        case SHK_EQ_ADVECTION: max_wavespeed_kernel<double, SHK_EQ_ADVECTION><<<blocks, kThreads, 0, st>>>(u + nghosts, n, c, out); break;
+        default: max_wavespeed_kernel<double, SHK_EQ_LWR><<<blocks, kThreads, 0, st>>>(u + nghosts, n, c, out); break;
+    }
+    return cuda_check(cudaGetLastError());
+}
+
+int shk_apply_operator_f64(const shk_scheme* scheme, const double* u, double* out, int64_t n,
+                           int32_t nghosts, double dx, const double* amax, void* stream) {
+    if (!valid_scheme(scheme) || !u || !out || n < 3 || nghosts < 3 || !(dx > 0)) return SHK_EINVAL;
+    if (scheme->flux == SHK_FLUX_LF && !amax) return SHK_EINVAL;
+    cudaStream_t st = as_stream(stream);
+    const int tile = 512;
+    const int W = tile + 2 * op_halo<double>();
+    const size_t smem = Smem<double>::host_bytes(W);
+    const int blocks = static_cast<int>((n + tile - 1) / tile);
+    OpParams<double> p = make_params<double>(scheme);
+    ApplyOpLaunch f{u, out, n, nghosts, tile, dx, amax, p, smem, blocks, st};
+    return dispatch_scheme<double>(scheme, f);
+}
+
+int shk_predict_timestep_f64(const shk_scheme* scheme, const double* u, int64_t n, int32_t nghosts,
+                             double cfl, double theta, double* dt, void* stream) {
+    int st = shk_max_wavespeed_f64(scheme, u, n, nghosts, dt, stream);
+    if (st != SHK_OK) return st;
+    finalize_dt_kernel<<<1, 1, 0, as_stream(stream)>>>(dt, cfl, theta);
+    return cuda_check(cudaGetLastError());
+}
+
+int shk_ssprk33_step_f64(const shk_scheme* scheme, const double* u, double* u_out, int64_t n,
+                         int32_t nghosts, double dx, double dt, void* stream) {
+    if (!valid_scheme(scheme) || !u || !u_out || n < 3 || nghosts < 3 || !(dx > 0)) return SHK_EINVAL;
+    if (!std::isfinite(dt)) return SHK_ENONFINITE;
+    if (scheme->flux == SHK_FLUX_LF) return SHK_EUNSUPPORTED;  // global max per stage
+    cudaStream_t st = as_stream(stream);
+    const int tile = 512;
+    const int W = tile + 2 * step_halo<double>();
+    const size_t smem = Smem<double>::host_bytes(W);
+    const int blocks = static_cast<int>((n + tile - 1) / tile);
+    OpParams<double> p = make_params<double>(scheme);
+    SingleStepLaunch f{u, u_out, n, nghosts, tile, dt / dx, p, smem, blocks, st};
+    return dispatch_scheme<double>(scheme, f);
+}
+
+// ---------------------------------------------------------------------------
+// plans
+// ---------------------------------------------------------------------------
+int shk_plan_destroy(shk_plan* plan) {
+    if (!plan) return SHK_OK;
+    if (plan->graph) cudaGraphExecDestroy(plan->graph);
+    void* ptrs[] = {plan->item_inst, plan->item_tile, plan->item_first, plan->offsets, plan->cfl,
+                    plan->inv_dx, plan->tfinal, plan->amax, plan->t, plan->dt_hist, plan->step,
+                    plan->done, plan->status, plan->partial};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete plan;
+    return SHK_OK;
+}
+
+int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_offsets,
+                    const double* h_dx, const double* h_cfl, double theta,
+                    const shk_plan_opts* opts, shk_plan** out) {
+    if (!out) return SHK_EINVAL;
+    *out = nullptr;
+    if (!valid_scheme(scheme) || batch <= 0 || !h_offsets || !h_dx || !h_cfl) return SHK_EINVAL;
+    if (scheme->flux == SHK_FLUX_LF) return SHK_EUNSUPPORTED;
+    const int dtype = opts ? opts->dtype : SHK_F64;
+    if (dtype != SHK_F64 && dtype != SHK_F32) return SHK_EINVAL;
+    int tile = (opts && opts->tile > 0) ? opts->tile : kDefaultTile;
+    const int align = dtype == SHK_F64 ? 2 : 4;
+    if (tile % align || tile < 16 || tile > 8192) return SHK_EINVAL;
+    std::vector<int32_t> inst, tl, first(batch + 1, 0);
+    for (int b = 0; b < batch; ++b) {
+        const int64_t n = h_offsets[b + 1] - h_offsets[b];
+        if (n < 3 || !(h_dx[b] > 0)) return SHK_EINVAL;
+        const int64_t ntiles = (n + tile - 1) / tile;
+        first[b] = static_cast<int32_t>(inst.size());
+        for (int64_t j = 0; j < ntiles; ++j) {
+            inst.push_back(b);
+            tl.push_back(static_cast<int32_t>(j));
+        }
+    }
+    first[batch] = static_cast<int32_t>(inst.size());
+    auto* P = new (std::nothrow) shk_plan();
+    if (!P) return SHK_ENOMEM;
+    P->scheme = *scheme;
+    P->dtype = dtype;
+    P->B = batch;
+    P->tile = tile;
+    P->nitems = static_cast<int>(inst.size());
+    P->max_steps = opts ? std::max(0, opts->max_steps) : 0;
+    P->theta = theta;
+    P->total_cells = h_offsets[batch] - h_offsets[0];
+    std::vector<double> inv(batch), inf(batch, DBL_MAX);
+    for (int b = 0; b < batch; ++b) inv[b] = 1.0 / h_dx[b];
+    auto alloc = [&](void** p, size_t bytes) { return cudaMalloc(p, bytes) == cudaSuccess; };
+    bool ok = alloc((void**)&P->item_inst, sizeof(int32_t) * P->nitems) &&
+              alloc((void**)&P->item_tile, sizeof(int32_t) * P->nitems) &&
+              alloc((void**)&P->item_first, sizeof(int32_t) * (batch + 1)) &&
+              alloc((void**)&P->offsets, sizeof(int64_t) * (batch + 1)) &&
+              alloc((void**)&P->cfl, sizeof(double) * batch) &&
+              alloc((void**)&P->inv_dx, sizeof(double) * batch) &&
+              alloc((void**)&P->tfinal, sizeof(double) * batch) &&
+              alloc((void**)&P->amax, sizeof(unsigned long long) * 2 * batch) &&
+              alloc((void**)&P->t, sizeof(double) * batch) &&
+              alloc((void**)&P->step, sizeof(int64_t)) && alloc((void**)&P->done, sizeof(unsigned)) &&
+              alloc((void**)&P->status, sizeof(int32_t)) &&
+              alloc((void**)&P->partial, sizeof(double) * P->nitems);
+    if (ok && P->max_steps > 0)
+        ok = alloc((void**)&P->dt_hist, sizeof(double) * size_t(P->max_steps) * batch);
+    if (!ok) {
+        shk_plan_destroy(P);
+        return SHK_ENOMEM;
+    }
+    ok = cudaMemcpy(P->item_inst, inst.data(), sizeof(int32_t) * P->nitems, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(P->item_tile, tl.data(), sizeof(int32_t) * P->nitems, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(P->item_first, first.data(), sizeof(int32_t) * (batch + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(P->offsets, h_offsets, sizeof(int64_t) * (batch + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(P->cfl, h_cfl, sizeof(double) * batch, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(P->inv_dx, inv.data(), sizeof(double) * batch, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(P->tfinal, inf.data(), sizeof(double) * batch, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(P->amax, 0, sizeof(unsigned long long) * 2 * batch) == cudaSuccess &&
+         cudaMemset(P->t, 0, sizeof(double) * batch) == cudaSuccess &&
+         cudaMemset(P->step, 0, sizeof(int64_t)) == cudaSuccess &&
+         cudaMemset(P->done, 0, sizeof(unsigned)) == cudaSuccess &&
+         cudaMemset(P->status, 0, sizeof(int32_t)) == cudaSuccess;
+    if (!ok) {
+        shk_plan_destroy(P);
+        return SHK_ECUDA;
+    }
+    // persistent grid: resident CTAs per SM x SMs
+    int per_sm = opts && opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 0;
+    if (per_sm == 0) {
+        const size_t smem = dtype == SHK_F64 ? Smem<double>::host_bytes(tile + 2 * step_halo<double>())
+                                             : Smem<float>::host_bytes(tile + 2 * step_halo<float>());
+        per_sm = std::max(1, static_cast<int>((200 * 1024) / std::max<size_t>(smem, 1)));
+        per_sm = std::min(per_sm, 8);
+    }
+    P->grid = std::max(1, std::min(P->nitems, per_sm * sm_count()));
+    *out = P;
+    return SHK_OK;
+}
+
+int shk_plan_state(shk_plan* plan, double** t, double** dt_hist, int64_t** step_counter) {
+    if (!plan) return SHK_EINVAL;
+    if (t) *t = plan->t;
+    if (dt_hist) *dt_hist = plan->dt_hist;
+    if (step_counter) *step_counter = plan->step;
+    return SHK_OK;
+}
+
+int shk_plan_copy_time(shk_plan* plan, double* t_out, void* stream) {
+    if (!plan || !t_out) return SHK_EINVAL;
+    return cuda_check(cudaMemcpyAsync(t_out, plan->t, sizeof(double) * plan->B,
+                                      cudaMemcpyDeviceToDevice, as_stream(stream)));
+}
+
+int shk_plan_copy_dt_history(shk_plan* plan, double* out, void* stream) {
+    if (!plan || !out || !plan->dt_hist) return SHK_EINVAL;
+    return cuda_check(cudaMemcpyAsync(out, plan->dt_hist,
+                                      sizeof(double) * size_t(plan->max_steps) * plan->B,
+                                      cudaMemcpyDeviceToDevice, as_stream(stream)));
+}
+
+int shk_plan_status(shk_plan* plan, int32_t* h_status, void* stream) {
+    if (!plan || !h_status) return SHK_EINVAL;
+    SHK_CUDA(cudaMemcpyAsync(h_status, plan->status, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             as_stream(stream)));
+    SHK_CUDA(cudaStreamSynchronize(as_stream(stream)));
+    return SHK_OK;
+}
+
+
+int shk_plan_reset(shk_plan* plan, const void* u, const double* t0, const double* tfinal,
+                   void* stream) {
+    if (!plan || !u) return SHK_EINVAL;
+    cudaStream_t st = as_stream(stream);
+    const int B = plan->B;
+    SHK_CUDA(cudaMemsetAsync(plan->amax, 0, sizeof(unsigned long long) * 2 * B, st));
+    SHK_CUDA(cudaMemsetAsync(plan->step, 0, sizeof(int64_t), st));
+    SHK_CUDA(cudaMemsetAsync(plan->done, 0, sizeof(unsigned), st));
+    SHK_CUDA(cudaMemsetAsync(plan->status, 0, sizeof(int32_t), st));
+    if (t0) SHK_CUDA(cudaMemcpyAsync(plan->t, t0, sizeof(double) * B, cudaMemcpyDeviceToDevice, st));
+    else SHK_CUDA(cudaMemsetAsync(plan->t, 0, sizeof(double) * B, st));
+    if (tfinal) {
+        SHK_CUDA(cudaMemcpyAsync(plan->tfinal, tfinal, sizeof(double) * B, cudaMemcpyDeviceToDevice, st));
+    } else {
+        std::vector<double> inf(B, DBL_MAX);
+        SHK_CUDA(cudaMemcpyAsync(plan->tfinal, inf.data(), sizeof(double) * B, cudaMemcpyHostToDevice, st));
+        SHK_CUDA(cudaStreamSynchronize(st));
+    }
+    if (plan->dt_hist)
+        SHK_CUDA(cudaMemsetAsync(plan->dt_hist, 0, sizeof(double) * size_t(plan->max_steps) * B, st));
+    plan->host_steps = 0;
+    return plan->dtype == SHK_F64 ? launch_max<double>(plan, u, 0, st) : launch_max<float>(plan, u, 0, st);
+}
+
+int shk_plan_step(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps, void* stream) {
+    if (!plan || !u_a || !u_b || u_a == u_b || nsteps < 0) return SHK_EINVAL;
+    cudaStream_t st = as_stream(stream);
+    for (int i = 0; i < nsteps; ++i) {
+        const bool even = (plan->host_steps % 2) == 0;
+        void* in = even ? u_a : u_b;
+        void* out = even ? u_b : u_a;
+        const int r = plan->dtype == SHK_F64 ? launch_step<double>(plan, in, out, st)
+                                             : launch_step<float>(plan, in, out, st);
+        if (r != SHK_OK) return r;
+        plan->host_steps++;
+    }
+    return SHK_OK;
+}
+
+int shk_plan_step_graph(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps, void* stream) {
+    if (!plan || !u_a || !u_b || u_a == u_b || nsteps < 0 || nsteps % 2) return SHK_EINVAL;
+    if (plan->host_steps % 2) return SHK_EINVAL;
+    cudaStream_t st = as_stream(stream);
+    if (st == nullptr) return SHK_EINVAL;  // capture needs a non-default stream
+    if (!plan->graph || plan->graph_a != u_a || plan->graph_b != u_b) {
+        if (plan->graph) {
+            cudaGraphExecDestroy(plan->graph);
+            plan->graph = nullptr;
+        }
+        cudaGraph_t g;
+        SHK_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const int64_t saved = plan->host_steps;
+        int r = shk_plan_step(plan, u_a, u_b, 2, stream);
+        plan->host_steps = saved;
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (r != SHK_OK) return r;
+        SHK_CUDA(e);
+        e = cudaGraphInstantiate(&plan->graph, g, 0);
+        cudaGraphDestroy(g);
+        SHK_CUDA(e);
+        plan->graph_a = u_a;
+        plan->graph_b = u_b;
+    }
+    for (int i = 0; i < nsteps / 2; ++i) SHK_CUDA(cudaGraphLaunch(plan->graph, st));
+    plan->host_steps += nsteps;
+    return SHK_OK;
+}
+
+int shk_plan_reduce(shk_plan* plan, const void* u, int32_t p, double* out, void* stream) {
+    if (!plan || !u || !out || (p != 0 && p != 1 && p != -1)) return SHK_EINVAL;
+    cudaStream_t st = as_stream(stream);
+    const PlanDev D = plan->dev();
+    if (plan->dtype == SHK_F64)
+        batched_partial_kernel<double><<<plan->grid, kThreads, 0, st>>>(D, static_cast<const double*>(u), p);
+    else
+        batched_partial_kernel<float><<<plan->grid, kThreads, 0, st>>>(D, static_cast<const float*>(u), p);
+    SHK_CUDA(cudaGetLastError());
+    instance_sum_kernel<<<(plan->B + 127) / 128, 128, 0, st>>>(D, plan->item_first, p, out);
+    return cuda_check(cudaGetLastError());
+}
+
+}  // extern "C"

@@ -1,0 +1,93 @@
+"""Reconstructions on the GB300 path (mirrors ``src/pyshocks/reconstruction.py``).
+
+The reconstruction objects are the reference's frozen dataclasses; the
+arithmetic runs inside the flux kernels of ``libshocks.so`` (there is no
+standalone reconstruction kernel: ul/ur never leave shared memory).
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, fields
+from typing import Any
+
+from pyshocks_gb300 import _lib as L
+
+
+@dataclass(frozen=True)
+class Reconstruction:
+    """``src/pyshocks/reconstruction.py:48-76``."""
+
+    @property
+    def name(self) -> str:
+        return type(self).__name__.lower()
+
+    @property
+    def order(self) -> int:
+        raise NotImplementedError(type(self).__name__)
+
+    @property
+    def stencil_width(self) -> int:
+        raise NotImplementedError(type(self).__name__)
+
+
+@dataclass(frozen=True)
+class WENOJS(Reconstruction):
+    """``src/pyshocks/reconstruction.py:305-317``."""
+
+    eps: float
+
+    @property
+    def stencil_width(self) -> int:
+        return self.order
+
+
+@dataclass(frozen=True)
+class WENOJS53(WENOJS):
+    """Fifth-order WENO-JS (``src/pyshocks/reconstruction.py:335-348``)."""
+
+    eps: float = 1.0e-12
+
+    @property
+    def order(self) -> int:
+        return 3
+
+    code = L.SHK_REC_WENOJS53
+
+
+@dataclass(frozen=True)
+class ESWENO32(Reconstruction):
+    """ES-WENO weights of [Yamaleev2009] (``src/pyshocks/reconstruction.py:386-411``)."""
+
+    eps: float = 1.0e-6
+    delta: float = 1.0e-6
+
+    @property
+    def order(self) -> int:
+        return 2
+
+    @property
+    def stencil_width(self) -> int:
+        return 2
+
+    code = L.SHK_REC_ESWENO32
+
+
+_RECONSTRUCTION: dict[str, type[Reconstruction]] = {
+    "wenojs53": WENOJS53,
+    "esweno32": ESWENO32,
+}
+
+
+def reconstruction_ids() -> tuple[str, ...]:
+    return tuple(_RECONSTRUCTION)
+
+
+def make_reconstruction_from_name(name: str, **kwargs: Any) -> Reconstruction:
+    """``src/pyshocks/reconstruction.py:547-566``: unknown keyword arguments are
+    ignored, as in the reference."""
+    cls = _RECONSTRUCTION.get(name)
+    if cls is None:
+        raise ValueError(
+            f"Reconstruction {name!r} not found. Try one of {', '.join(reconstruction_ids())}."
+        )
+    return cls(**{f.name: kwargs[f.name] for f in fields(cls) if f.name in kwargs})

@@ -1,0 +1,257 @@
+"""Parity of the CUDA forward path (``libshocks.so``) with the oracle.
+
+Tolerances (float64): single operator / step evaluations within 1e-12 of the
+oracle relative to the data scale; the full ``t_final = 1`` Burgers run within
+1e-10 max-abs (the stated parity bar); dt sequences within 1e-13 relative.
+"""
+
+from __future__ import annotations
+
+import pathlib
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import numpy_ref as R
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = pathlib.Path(__file__).parent / "golden"
+
+
+def _golden(name):
+    return dict(np.load(GOLDEN / f"{name}.npz"))
+
+
+@pytest.fixture(scope="module")
+def gb():
+    import pyshocks_gb300 as gb
+
+    return gb
+
+
+def _scheme(gb, kind, eq="burgers", eps=1.0e-6):
+    from pyshocks_gb300 import burgers
+
+    rec = gb.reconstruction.make_reconstruction_from_name("wenojs53", eps=eps)
+    if kind == "rusanov":
+        return burgers.Rusanov(rec=rec) if eq == "burgers" else (
+            burgers.LWRRusanov(rec=rec) if eq == "lwr" else burgers.AdvectionRusanov(rec=rec))
+    if kind == "lf":
+        return burgers.LaxFriedrichs(rec=rec)
+    if kind == "esweno":
+        return burgers.ESWENO32(rec=gb.reconstruction.make_reconstruction_from_name("esweno32"))
+    raise ValueError(kind)
+
+
+def _oracle_spec(kind, eq="burgers", eps=1.0e-6, grid=None):
+    if kind == "esweno":
+        e, d = R.es_weno_parameters(grid, np.ones_like(grid.x))
+        return R.SchemeSpec(flux_kind="esweno", rec="esweno32", eps=e, delta=d, equation=eq)
+    return R.SchemeSpec(flux_kind=kind, rec="wenojs53", eps=eps, equation=eq)
+
+
+CASES = [
+    ("rusanov", "burgers", 64),
+    ("rusanov", "burgers", 256),
+    ("rusanov", "burgers", 1000),
+    ("rusanov", "burgers", 3001),
+    ("lf", "burgers", 256),
+    ("lf", "burgers", 1500),
+    ("esweno", "burgers", 64),
+    ("esweno", "burgers", 777),
+    ("rusanov", "lwr", 512),
+    ("rusanov", "advection", 300),
+]
+
+
+@pytest.mark.parametrize(("kind", "eq", "n"), CASES)
+def test_apply_operator_matches_oracle(gb, kind, eq, n):
+    rng = np.random.default_rng(n)
+    og = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+    u0 = R.lwr_ic(rng, og.f) if eq == "lwr" else R.random_fourier_ic(rng, og.f)
+    spec = _oracle_spec(kind, eq, grid=og)
+    ref = R.apply_operator(spec, og, u0)
+
+    grid = gb.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
+    bc = gb.scalar.PeriodicBoundary()
+    scheme = gb.bind(_scheme(gb, kind, eq), grid, bc)
+    u = torch.tensor(u0, device="cuda")
+    out = gb.apply_operator(scheme, grid, bc, 0.0, u).cpu().numpy()
+    scale = np.max(np.abs(ref[3:-3]))
+    err = np.max(np.abs(out[3:-3] - ref[3:-3])) / scale
+    assert err < 1.0e-12, err
+    # ghost cells hold the periodic image of the interior output
+    np.testing.assert_array_equal(out[:3], out[n : n + 3])
+    np.testing.assert_array_equal(out[-3:], out[3:6])
+
+    dt = gb.predict_timestep(scheme, grid, bc, 0.0, u)
+    assert float(dt) == R.predict_timestep(spec, og, u0)
+
+
+@pytest.mark.parametrize(("kind", "eq", "n"), [c for c in CASES if c[0] != "lf"])
+def test_fused_step_matches_oracle(gb, kind, eq, n):
+    from pyshocks_gb300 import burgers
+
+    rng = np.random.default_rng(7 + n)
+    og = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+    u0 = R.lwr_ic(rng, og.f) if eq == "lwr" else R.random_fourier_ic(rng, og.f)
+    spec = _oracle_spec(kind, eq, grid=og)
+    dt = 0.9 * R.predict_timestep(spec, og, u0)
+    ref = R.ssprk33(lambda t, v: R.apply_operator(spec, og, v), dt, 0.0, u0)
+
+    grid = gb.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
+    bc = gb.scalar.PeriodicBoundary()
+    scheme = gb.bind(_scheme(gb, kind, eq), grid, bc)
+    out = burgers.ssprk33_step(scheme, grid, bc, dt, torch.tensor(u0, device="cuda"))
+    out = out.cpu().numpy()
+    err = np.max(np.abs(out[3:-3] - ref[3:-3])) / np.max(np.abs(ref[3:-3]))
+    assert err < 1.0e-12, err
+
+
+@pytest.mark.parametrize("name,kind", [("config1_rusanov_n256", "rusanov"),
+                                       ("config1_esweno_n256", "esweno"),
+                                       ("config1_lf_n256", "lf")])
+def test_config1_step_api_matches_reference(gb, name, kind):
+    """N=256 Burgers to t_final = 1 through the reference-style ``step()`` API:
+    within 1e-10 max-abs of the reference's own solution (golden vectors from
+    its source) and the same number of steps."""
+    g = _golden(name)
+    grid = gb.make_uniform_cell_grid(-1.0, 1.0, 256, nghosts=3)
+    bc = gb.scalar.PeriodicBoundary()
+    scheme = gb.bind(_scheme(gb, kind), grid, bc)
+    stepper = gb.timestepping.make_time_stepper(scheme, grid, bc, theta=1.0)
+    dts = []
+    ev = None
+    for ev in gb.timestepping.step(stepper, torch.tensor(g["u0"], device="cuda"), tfinal=1.0):
+        if ev.iteration > 0:
+            dts.append(ev.dt)
+    u = ev.u.cpu().numpy()
+    assert len(dts) == len(g["dts"])
+    assert np.max(np.abs(np.array(dts) - g["dts"]) / g["dts"]) < 1.0e-12
+    err = np.max(np.abs(u[3:-3] - g["u"][3:-3]))
+    assert err < 1.0e-10, err
+
+
+def test_config1_batched_plan_matches_reference(gb):
+    """The same workload through the batched persistent plan (device-side dt,
+    final-time clip and +1e-15)."""
+    from pyshocks_gb300.batched import BatchedSolver
+
+    g = _golden("config1_rusanov_n256")
+    scheme = _scheme(gb, "rusanov")
+    solver = BatchedSolver(scheme, [256], 2.0 / 256, theta=1.0, max_steps=512)
+    solver.reset(torch.tensor(g["u0"][3:-3]), tfinal=1.0)
+    solver.step(len(g["dts"]) + 3)  # extra steps must be no-ops (t >= tfinal)
+    u = solver.u.cpu().numpy()
+    t = float(solver.time()[0])
+    assert abs(t - float(g["t"])) < 1.0e-13
+    hist = solver.dt_history()[:, 0].cpu().numpy()
+    assert np.max(np.abs(hist[: len(g["dts"])] - g["dts"]) / g["dts"]) < 1.0e-12
+    assert np.all(hist[len(g["dts"]):] == 0.0)
+    err = np.max(np.abs(u - g["u"][3:-3]))
+    assert err < 1.0e-10, err
+    assert solver.status() == 0
+
+
+@pytest.mark.parametrize("tile", [0, 64])
+def test_batched_uneven_matches_oracle(gb, tile):
+    """Uneven instance sizes (aligned, odd, tiny, multi-tile), fixed step count
+    (no final time: dt + 1e-15 every step), per-instance dt."""
+    from pyshocks_gb300.batched import BatchedSolver
+
+    sizes = [64, 50, 7, 1024, 333, 2048, 96]
+    nsteps = 25
+    u0s, refs, dts_ref = [], [], []
+    for b, n in enumerate(sizes):
+        og = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+        u0 = R.random_fourier_ic(np.random.default_rng(100 + b), og.f)
+        spec = R.SchemeSpec()
+        u, dts = R.evolve(spec, og, u0, theta=0.8, maxit=nsteps)
+        u0s.append(u0[3:-3])
+        refs.append(u[3:-3])
+        dts_ref.append(dts)
+    scheme = _scheme(gb, "rusanov")
+    solver = BatchedSolver(scheme, sizes, [2.0 / n for n in sizes], theta=0.8, tile=tile,
+                           max_steps=nsteps)
+    solver.reset(torch.tensor(np.concatenate(u0s)))
+    solver.step(nsteps)
+    hist = solver.dt_history().cpu().numpy()
+    for b, n in enumerate(sizes):
+        u = solver.instance(b).cpu().numpy()
+        err = np.max(np.abs(u - refs[b])) / max(1.0, np.max(np.abs(refs[b])))
+        assert err < 1.0e-11, (b, n, err)
+        rel = np.max(np.abs(hist[:, b] - dts_ref[b]) / np.array(dts_ref[b]))
+        assert rel < 1.0e-12, (b, rel)
+    assert solver.status() == 0
+
+
+def test_batched_graph_equals_stream(gb):
+    from pyshocks_gb300.batched import BatchedSolver
+
+    sizes = [1024, 2048, 512, 4096]
+    rng = np.random.default_rng(5)
+    u0 = np.concatenate([R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes])
+    scheme = _scheme(gb, "rusanov")
+    s1 = BatchedSolver(scheme, sizes, [2.0 / n for n in sizes])
+    s2 = BatchedSolver(scheme, sizes, [2.0 / n for n in sizes])
+    s1.reset(torch.tensor(u0))
+    s1.step(10)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        s2.reset(torch.tensor(u0, device="cuda"))
+        s2.step(10, graph=True)
+    side.synchronize()
+    assert torch.equal(s1.u, s2.u)
+    assert torch.equal(s1.time(), s2.time())
+
+
+def test_batched_float32_error_and_conservation(gb):
+    """FP32 state: error against the FP64 oracle reported/bounded; the FP64
+    conserved-mass sums drift only by rounding."""
+    from pyshocks_gb300.batched import BatchedSolver
+
+    sizes = [1024, 2048, 4096]
+    nsteps = 50
+    rng = np.random.default_rng(9)
+    u0 = [R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes]
+    scheme = _scheme(gb, "rusanov")
+    s64 = BatchedSolver(scheme, sizes, [2.0 / n for n in sizes])
+    s32 = BatchedSolver(scheme, sizes, [2.0 / n for n in sizes], dtype=torch.float32)
+    s64.reset(torch.tensor(np.concatenate(u0)))
+    s32.reset(torch.tensor(np.concatenate(u0)))
+    m0 = s64.reduce(0).cpu().numpy()
+    s64.step(nsteps)
+    s32.step(nsteps)
+    m64 = s64.reduce(0).cpu().numpy()
+    m32 = s32.reduce(0).cpu().numpy()
+    # mass is conserved to rounding (periodic flux form)
+    assert np.max(np.abs(m64 - m0) / np.array(sizes)) < 1.0e-13
+    assert np.max(np.abs(m32 - m0) / np.array(sizes)) < 1.0e-5
+    diff = (s32.u.double() - s64.u).abs()
+    assert float(diff.max()) < 1.0e-3
+    # reductions agree with torch
+    for b in range(len(sizes)):
+        ref = float(s64.instance(b).sum())
+        assert abs(m64[b] - ref) < 1.0e-10 * max(1.0, abs(ref))
+
+
+def test_nonfinite_dt_freezes_instance_and_sets_status(gb):
+    """A zero state gives an infinite dt (0.5 dx / 0): the reference raises
+    ValueError("Time step is not finite"); the batched plan flags it and
+    freezes that instance while the others advance."""
+    from pyshocks_gb300.batched import BatchedSolver
+
+    sizes = [64, 64]
+    u0 = np.concatenate([np.zeros(64), 0.5 + 0.2 * np.sin(np.linspace(0, 2 * np.pi, 64, endpoint=False))])
+    solver = BatchedSolver(_scheme(gb, "rusanov"), sizes, 2.0 / 64)
+    solver.reset(torch.tensor(u0))
+    solver.step(3)
+    st = solver.status()
+    assert st & 1
+    u = solver.u.cpu().numpy()
+    np.testing.assert_array_equal(u[:64], 0.0)
+    assert float(solver.time()[0]) == 0.0 and float(solver.time()[1]) > 0.0
+    with pytest.raises(ValueError):
+        solver.check_status()
