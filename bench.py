@@ -300,32 +300,38 @@ def bench_gpu(args, rank: int, world: int) -> None:
     value = total_cells * k / (ms_max * 1e-3)
     per_launch_s = ms * 1e-3 / k
 
-    # e2e through the public API with pinned host buffers
-    host_in = u0.cpu().pin_memory()
-    host_out = torch.empty_like(host_in).pin_memory()
-    ke = max(2, min(args.steps, 6))
-    with torch.cuda.stream(stream):
-        for _ in range(1):
-            solver.reset(host_in.to(dev, non_blocking=True))
-            solver.step(1)
-            host_out.copy_(solver.u, non_blocking=True)
-        stream.synchronize()
-        barrier()
-        t0 = time.perf_counter()
-        f0 = torch.cuda.Event(enable_timing=True)
-        f1 = torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        for _ in range(ke):
-            dev_in = host_in.to(dev, non_blocking=True)
-            solver.reset(dev_in)
-            solver.step(1)
-            host_out.copy_(solver.u, non_blocking=True)
-        f1.record(stream)
-        f1.synchronize()
-        wall = time.perf_counter() - t0
-        e2e_ms = f0.elapsed_time(f1)
-    # wall clock: host staging, copies and kernels of every e2e step
-    e2e_value = total_cells * ke / max(wall, e2e_ms * 1e-3)
+    e2e = None
+    host_bytes = cells * 8
+    if not args.profile:
+        # e2e through the public API with pinned host buffers
+        host_in = u0.cpu().pin_memory()
+        host_out = torch.empty_like(host_in).pin_memory()
+        ke = max(2, min(args.steps, 6))
+        with torch.cuda.stream(stream):
+            for _ in range(1):
+                solver.reset(host_in.to(dev, non_blocking=True))
+                solver.step(1)
+                host_out.copy_(solver.u, non_blocking=True)
+            stream.synchronize()
+            barrier()
+            t0 = time.perf_counter()
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for _ in range(ke):
+                dev_in = host_in.to(dev, non_blocking=True)
+                solver.reset(dev_in)
+                solver.step(1)
+                host_out.copy_(solver.u, non_blocking=True)
+            f1.record(stream)
+            f1.synchronize()
+            wall = time.perf_counter() - t0
+            e2e_ms = f0.elapsed_time(f1)
+        # wall clock: host staging, copies and kernels of every e2e step
+        e2e_value = total_cells * ke / max(wall, e2e_ms * 1e-3)
+        e2e = {"value": e2e_value, "unit": "cell-steps/s",
+               "h2d_bytes_per_step": int(host_in.numel() * 8),
+               "d2h_bytes_per_step": int(host_out.numel() * 8)}
 
     peaks = _measured_peaks()
     consts = _profile_constants()
@@ -338,7 +344,7 @@ def bench_gpu(args, rank: int, world: int) -> None:
     traffic = None
     if "dram_bytes_per_cell_step" in consts:
         traffic = consts["dram_bytes_per_cell_step"] * cells
-    fp64_peak = ctypes_fp_peak(L)
+    fp64_peak = None if args.profile else ctypes_fp_peak(L)
     fp64 = None
     if "fp64_flop_per_cell_step" in consts and fp64_peak:
         fl = consts["fp64_flop_per_cell_step"] * cells / per_launch_s
@@ -350,7 +356,7 @@ def bench_gpu(args, rank: int, world: int) -> None:
                 "peak_source": "shk_measure_fp_peak FMA chains on this GPU (of measured)"}
 
     cpu = None
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and not args.no_cpu and not args.profile:
         rate, used = run_cpu_sample(sizes, params, n_inst=args.cpu_instances, nsteps=1)
         cpu = {"value": rate, "unit": "cell-steps/s", "cores": used, "kind": "port",
                "sample": f"first {args.cpu_instances} instances of the batch, one step, "
@@ -372,9 +378,7 @@ def bench_gpu(args, rank: int, world: int) -> None:
             "data": "synthetic",
             "config": _config(args),
             "clocks": clk.summary(),
-            "e2e": {"value": e2e_value, "unit": "cell-steps/s",
-                    "h2d_bytes_per_step": int(host_in.numel() * 8),
-                    "d2h_bytes_per_step": int(host_out.numel() * 8)},
+            "e2e": e2e,
             "gpu_launches": k,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
@@ -402,6 +406,8 @@ def main() -> None:
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-instances", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="timed region only (no e2e, CPU baseline or FP peak): for ncu")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -129,7 +129,8 @@ def test_config1_step_api_matches_reference(gb, name, kind):
             dts.append(ev.dt)
     u = ev.u.cpu().numpy()
     assert len(dts) == len(g["dts"])
-    assert np.max(np.abs(np.array(dts) - g["dts"]) / g["dts"]) < 1.0e-12
+    # absolute: the last (clipped) dt = tfinal - t inherits the rounding of t
+    assert np.max(np.abs(np.array(dts) - g["dts"])) < 1.0e-14
     err = np.max(np.abs(u[3:-3] - g["u"][3:-3]))
     assert err < 1.0e-10, err
 
@@ -148,7 +149,7 @@ def test_config1_batched_plan_matches_reference(gb):
     t = float(solver.time()[0])
     assert abs(t - float(g["t"])) < 1.0e-13
     hist = solver.dt_history()[:, 0].cpu().numpy()
-    assert np.max(np.abs(hist[: len(g["dts"])] - g["dts"]) / g["dts"]) < 1.0e-12
+    assert np.max(np.abs(hist[: len(g["dts"])] - g["dts"])) < 1.0e-14
     assert np.all(hist[len(g["dts"]):] == 0.0)
     err = np.max(np.abs(u - g["u"][3:-3]))
     assert err < 1.0e-10, err
