@@ -239,15 +239,17 @@ def test_batched_float32_error_and_conservation(gb):
 
 
 def test_nonfinite_dt_freezes_instance_and_sets_status(gb):
-    """A zero state gives an infinite dt (0.5 dx / 0): the reference raises
-    ValueError("Time step is not finite"); the batched plan flags it and
+    """The reference only raises ValueError("Time step is not finite")
+    (timestepping.py:144-145) when the final-time clip is skipped, i.e.
+    tfinal = inf (timestepping.py:140): then an all-zero state gives
+    dt = 0.5 dx / 0 = inf. The batched plan flags it in the status word and
     freezes that instance while the others advance."""
     from pyshocks_gb300.batched import BatchedSolver
 
     sizes = [64, 64]
     u0 = np.concatenate([np.zeros(64), 0.5 + 0.2 * np.sin(np.linspace(0, 2 * np.pi, 64, endpoint=False))])
     solver = BatchedSolver(_scheme(gb, "rusanov"), sizes, 2.0 / 64)
-    solver.reset(torch.tensor(u0))
+    solver.reset(torch.tensor(u0), tfinal=float("inf"))
     solver.step(3)
     st = solver.status()
     assert st & 1
@@ -256,3 +258,15 @@ def test_nonfinite_dt_freezes_instance_and_sets_status(gb):
     assert float(solver.time()[0]) == 0.0 and float(solver.time()[1]) > 0.0
     with pytest.raises(ValueError):
         solver.check_status()
+
+
+def test_clipped_dt_stays_finite_like_the_reference(gb):
+    """With tfinal = None the reference clips dt to finfo.max - t, so even a
+    zero state gives a finite (huge) dt and no error (timestepping.py:140-145)."""
+    from pyshocks_gb300.batched import BatchedSolver
+
+    solver = BatchedSolver(_scheme(gb, "rusanov"), [64], 2.0 / 64, max_steps=2)
+    solver.reset(torch.zeros(64, dtype=torch.float64))
+    solver.step(1)
+    assert solver.status() == 0
+    assert float(solver.dt_history()[0, 0]) == float(np.finfo(np.float64).max)
