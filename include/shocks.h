@@ -30,7 +30,8 @@ typedef enum {
     SHK_ETIMEOUT = 3,     /* a bounded device-side wait expired                     */
     SHK_ECUDA = 4,        /* a CUDA runtime call failed                              */
     SHK_ENOMEM = 5,       /* allocation failed (plan creation only)                  */
-    SHK_EUNSUPPORTED = 6  /* combination not implemented                             */
+    SHK_EUNSUPPORTED = 6, /* combination not implemented                             */
+    SHK_ETOOLARGE = 7     /* size beyond the static scratch of a no-allocation call  */
 } shk_status;
 
 /* numerical flux (burgers/schemes.py:98-153,205-256) */
@@ -150,6 +151,29 @@ int shk_plan_status(shk_plan* plan, int32_t* h_status, void* stream);
  * out[b] = sum_i u_b[i] (p = 0), sum |u_b[i]| (p = 1) or max |u_b[i]| (p = -1),
  * accumulated in double for either state precision. */
 int shk_plan_reduce(shk_plan* plan, const void* u, int32_t p, double* out, void* stream);
+
+/* ---- no-allocation variant --------------------------------------------- */
+
+/* Lax-Friedrichs apply_operator for callers that cannot allocate device
+ * memory. No counterpart in the reference. Same inputs, outputs and result as
+ * shk_max_wavespeed_f64 followed by shk_apply_operator_f64 with
+ * SHK_FLUX_LF, but the wave-speed scratch is a fixed array inside the library
+ * instead of caller memory, so the call allocates nothing. Meant for hosts
+ * that own the whole device memory pool, e.g. a JAX custom-call handler
+ * (JAX preallocates most of the GPU and gives the handler only its operand
+ * buffers).
+ *  - n is limited to shk_apply_operator_lf_noalloc_max_cells() interior cells
+ *    (2,097,152); larger n returns SHK_ETOOLARGE before any launch.
+ *  - The first call on each device looks up the scratch address on that device
+ *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - The scratch (32 KiB per GPU, held from library load to process exit) is
+ *    shared by all calls and keeps the last call's contents; every slot a call
+ *    reads is written by that call first. Calls that overlap on the GPU race on
+ *    it: serialise them (one stream, or events between streams). */
+int shk_apply_operator_lf_noalloc_f64(const shk_scheme* scheme, const double* u,
+                                      double* out, int64_t n, int32_t nghosts, double dx,
+                                      void* stream);
+int64_t shk_apply_operator_lf_noalloc_max_cells(void);
 
 /* ---- measurement ------------------------------------------------------- */
 

@@ -22,6 +22,7 @@ SHK_ETIMEOUT = 3
 SHK_ECUDA = 4
 SHK_ENOMEM = 5
 SHK_EUNSUPPORTED = 6
+SHK_ETOOLARGE = 7
 
 SHK_FLUX_RUSANOV, SHK_FLUX_LF, SHK_FLUX_ESWENO = 0, 1, 2
 SHK_REC_WENOJS53, SHK_REC_ESWENO32 = 0, 1
@@ -83,6 +84,8 @@ SIGNATURES: dict[str, tuple] = {
     "shk_plan_copy_dt_history": (ctypes.c_int, [_P, _P, _P]),
     "shk_plan_status": (ctypes.c_int, [_P, ctypes.POINTER(_I32), _P]),
     "shk_plan_reduce": (ctypes.c_int, [_P, _P, _I32, _P, _P]),
+    "shk_apply_operator_lf_noalloc_f64": (ctypes.c_int, [_SCH, _P, _P, _I64, _I32, _D, _P]),
+    "shk_apply_operator_lf_noalloc_max_cells": (ctypes.c_int64, []),
     "shk_measure_fp_peak": (ctypes.c_int, [_I32, _I32, ctypes.POINTER(_D)]),
 }
 
@@ -106,6 +109,7 @@ def errstr(status: int) -> str:
         SHK_ECUDA: "CUDA runtime error",
         SHK_ENOMEM: "out of device memory",
         SHK_EUNSUPPORTED: "unsupported scheme combination",
+        SHK_ETOOLARGE: "size exceeds the static scratch of the no-allocation entry point",
     }
     return names.get(status, f"unknown status {status}")
 

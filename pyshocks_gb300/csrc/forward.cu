@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -708,6 +709,7 @@ const char* shk_strerror(int status) {
         case SHK_ECUDA: return "CUDA runtime error";
         case SHK_ENOMEM: return "out of device memory";
         case SHK_EUNSUPPORTED: return "unsupported scheme combination";
+        case SHK_ETOOLARGE: return "size exceeds the static scratch of the no-allocation entry point";
         default: return "unknown status";
     }
 }
@@ -978,3 +980,123 @@ int shk_plan_reduce(shk_plan* plan, const void* u, int32_t p, double* out, void*
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Lax-Friedrichs operator without any device allocation
+// ===========================================================================
+// Some callers cannot allocate device memory of their own. The main case for
+// this library is an integration as a JAX custom call: JAX reserves most of the
+// GPU for its own pool up front and hands a handler only its input and output
+// buffers, so a cudaMalloc in the handler competes with (or fails against)
+// that pool. The regular Lax-Friedrichs path needs one scratch value (the
+// instance-wide max |f'(u)|) that the caller allocates; this variant keeps its
+// scratch -- one partial maximum per 512-cell tile plus the final maximum -- in
+// a fixed array compiled into the library instead.
+//
+// The array lives in every GPU's memory from the moment the library is loaded
+// on that GPU until the process exits (kNoAllocMaxTiles + 1 doubles, 32 KiB).
+// All calls share it: a call overwrites every slot it reads, so nothing has to
+// start at zero, but two calls that overlap on the GPU (different streams, or
+// different host threads) race on it and must be serialised by the caller.
+namespace {
+
+constexpr int kNoAllocTile = 512;          // cells per tile, as shk_apply_operator_f64
+constexpr int kNoAllocMaxTiles = 4096;     // => at most 2,097,152 interior cells per call
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxTiles + 1];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+double* g_noalloc_addr[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device. In host code the
+// symbol itself is only a host-side stand-in, so the address must come from
+// cudaGetSymbolAddress, once per device, with that device current.
+int noalloc_scratch(double** out) {
+    int dev = 0;
+    SHK_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return SHK_EUNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            std::fprintf(stderr, "libshocks: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+            return SHK_ECUDA;
+        }
+        g_noalloc_addr[dev] = static_cast<double*>(p);
+    }
+    *out = g_noalloc_addr[dev];
+    return SHK_OK;
+}
+
+// per-tile max |f'(u)| into partial[tile]
+template <int EQ>
+__global__ void __launch_bounds__(kThreads) noalloc_tile_max_kernel(const double* __restrict__ u, int64_t n,
+                                                                    double c, double* partial) {
+    __shared__ unsigned long long red[32];
+    const int64_t s0 = int64_t(blockIdx.x) * kNoAllocTile;
+    const int te = static_cast<int>(imin64(kNoAllocTile, n - s0));
+    unsigned long long mx = 0;
+    for (int i = threadIdx.x; i < te; i += blockDim.x) {
+        const unsigned long long b = abs_bits(wave_speed<EQ>(u[s0 + i], c));
+        mx = b > mx ? b : mx;
+    }
+    const unsigned long long bm = block_max<unsigned long long>(mx, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = from_bits(bm);
+}
+
+// max of the ntiles partials into partial[kNoAllocMaxTiles]
+__global__ void __launch_bounds__(kThreads) noalloc_reduce_kernel(double* partial, int ntiles) {
+    __shared__ unsigned long long red[32];
+    unsigned long long mx = 0;
+    for (int i = threadIdx.x; i < ntiles; i += blockDim.x) {
+        const unsigned long long b = abs_bits(partial[i]);
+        mx = b > mx ? b : mx;
+    }
+    const unsigned long long bm = block_max<unsigned long long>(mx, red);
+    if (threadIdx.x == 0) partial[kNoAllocMaxTiles] = from_bits(bm);
+}
+
+}  // namespace
+
+extern "C" int shk_apply_operator_lf_noalloc_f64(const shk_scheme* scheme, const double* u,
+                                                 double* out, int64_t n, int32_t nghosts,
+                                                 double dx, void* stream) {
+    if (!valid_scheme(scheme) || scheme->flux != SHK_FLUX_LF || !u || !out || n < 3 ||
+        nghosts < 3 || !(dx > 0))
+        return SHK_EINVAL;
+    const int64_t ntiles = (n + kNoAllocTile - 1) / kNoAllocTile;
+    if (ntiles > kNoAllocMaxTiles) {
+        std::fprintf(stderr,
+                     "libshocks: shk_apply_operator_lf_noalloc_f64: n = %lld exceeds the static "
+                     "scratch limit of %lld cells\n",
+                     static_cast<long long>(n),
+                     static_cast<long long>(kNoAllocMaxTiles) * kNoAllocTile);
+        return SHK_ETOOLARGE;
+    }
+    double* scratch = nullptr;
+    const int st0 = noalloc_scratch(&scratch);
+    if (st0 != SHK_OK) return st0;
+    cudaStream_t st = as_stream(stream);
+    const double c = scheme->speed;
+    const int nt = static_cast<int>(ntiles);
+    switch (scheme->equation) {
+        case SHK_EQ_BURGERS: noalloc_tile_max_kernel<SHK_EQ_BURGERS><<<nt, kThreads, 0, st>>>(u + nghosts, n, c, scratch); break;
+        case SHK_EQ_ADVECTION: noalloc_tile_max_kernel<SHK_EQ_ADVECTION><<<nt, kThreads, 0, st>>>(u + nghosts, n, c, scratch); break;
+        default: noalloc_tile_max_kernel<SHK_EQ_LWR><<<nt, kThreads, 0, st>>>(u + nghosts, n, c, scratch); break;
+    }
+    SHK_CUDA(cudaGetLastError());
+    noalloc_reduce_kernel<<<1, kThreads, 0, st>>>(scratch, nt);
+    SHK_CUDA(cudaGetLastError());
+    // the operator itself is the regular one, reading the max from the scratch
+    const int W = kNoAllocTile + 2 * op_halo<double>();
+    const size_t smem = Smem<double>::host_bytes(W);
+    OpParams<double> p = make_params<double>(scheme);
+    ApplyOpLaunch f{u, out, n, nghosts, kNoAllocTile, dx, scratch + kNoAllocMaxTiles, p, smem, nt, st};
+    return dispatch_scheme<double>(scheme, f);
+}
+
+extern "C" int64_t shk_apply_operator_lf_noalloc_max_cells(void) {
+    return static_cast<int64_t>(kNoAllocMaxTiles) * kNoAllocTile;
+}
