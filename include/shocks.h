@@ -147,6 +147,32 @@ int shk_plan_copy_dt_history(shk_plan* plan, double* out, void* stream);
 /* copy the device status word to *h_status (synchronises `stream`). */
 int shk_plan_status(shk_plan* plan, int32_t* h_status, void* stream);
 
+/* ---- discrete adjoint (dt frozen, as adjoint_step: timestepping.py:155-215) -- */
+
+/* p_out = (d advance(u) / d u)^T p_next for one SSPRK33 step of a ghosted single
+ * instance (the `jac.T @ p` of timestepping.py:205-206, matrix-free). Rusanov +
+ * WENO-JS53 only. Cotangents live on interior cells: ghost entries of p_next
+ * are ignored and those of p_out are set to zero. */
+int shk_ssprk33_vjp_f64(const shk_scheme* scheme, const double* u, const double* p_next,
+                        double* p_out, int64_t n, int32_t nghosts, double dx, double dt,
+                        void* stream);
+
+/* forward run of `nsteps` steps (as shk_plan_step) that also copies the state
+ * before every step k with k % stride == 0 into ckpt[k / stride] (caller-owned,
+ * ceil(nsteps/stride) packed states). The plan needs max_steps >= nsteps: the
+ * dt history is the frozen dt of the adjoint (timestepping.py:200-201). */
+int shk_plan_forward_checkpointed(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps,
+                                  void* ckpt, int32_t stride, void* stream);
+
+/* reverse sweep of the last checkpointed forward run: p_a holds dJ/du(T) on
+ * entry; after the call dJ/du(0) is in p_a if nsteps is even, else in p_b.
+ * Segments of `stride` steps are recomputed from the checkpoints into `seg`
+ * (caller-owned, stride packed states) with the recorded dt, then stepped
+ * backwards (sqrt(nsteps) checkpointing when stride ~ sqrt(nsteps)). Rusanov +
+ * WENO-JS53 only. */
+int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t nsteps,
+                     void* seg, void* p_a, void* p_b, void* stream);
+
 /* FP64 reductions over the batch (grid.py:444-506, conservation checks):
  * out[b] = sum_i u_b[i] (p = 0), sum |u_b[i]| (p = 1) or max |u_b[i]| (p = -1),
  * accumulated in double for either state precision. */

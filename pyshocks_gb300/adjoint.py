@@ -1,0 +1,109 @@
+"""Discrete adjoint of the batched SSPRK33 / WENO-JS5 / Rusanov solve.
+
+The reference differentiates one step with ``jax.jacfwd(advance)`` and applies
+``p <- jac.T @ p`` backwards over checkpoints saved at *every* step, with the
+time step re-read from the checkpoints rather than differentiated
+(``src/pyshocks/timestepping.py:155-215``). Here:
+
+* the transpose Jacobian-vector product of a step is a matrix-free CUDA kernel
+  (``shk_plan_adjoint``): no dense ``(N+6)^2`` Jacobian;
+* states are checkpointed every ``stride ~ sqrt(nsteps)`` steps on the device and
+  each segment is recomputed with the recorded dt before it is swept
+  backwards;
+* dt is frozen exactly as in the reference.
+
+Cotangents are defined on the interior cells (the packed layout). With the
+reference's ghosted layout, a cotangent with zero ghost entries maps to the
+same interior result, because interior outputs do not depend on input ghosts
+(the boundary fill overwrites them).
+"""
+
+from __future__ import annotations
+
+import math
+
+import torch
+
+from pyshocks_gb300 import _lib as L
+from pyshocks_gb300.batched import BatchedSolver
+
+
+class CheckpointedSolve:
+    """Forward run with sqrt(n) checkpoints and its reverse sweep.
+
+    :arg solver: a :class:`BatchedSolver` created with ``max_steps >= nsteps``.
+    :arg nsteps: number of SSPRK33 steps of the forward run.
+    :arg stride: checkpoint interval (default ``ceil(sqrt(nsteps))``).
+    """
+
+    def __init__(self, solver: BatchedSolver, nsteps: int, stride: int | None = None):
+        if solver.max_steps < nsteps:
+            raise ValueError("the solver's dt history must hold every step (max_steps >= nsteps)")
+        self.solver = solver
+        self.nsteps = int(nsteps)
+        self.stride = int(stride or max(1, math.ceil(math.sqrt(max(1, nsteps)))))
+        nck = max(1, -(-self.nsteps // self.stride))
+        dev, dt = solver.device, solver.dtype
+        self.ckpt = torch.empty((nck, solver.total), dtype=dt, device=dev)
+        self.seg = torch.empty((self.stride, solver.total), dtype=dt, device=dev)
+        self.p_a = torch.empty(solver.total, dtype=dt, device=dev)
+        self.p_b = torch.empty(solver.total, dtype=dt, device=dev)
+
+    def forward(self, u0: torch.Tensor, *, t0=None, tfinal=None) -> torch.Tensor:
+        """Run the forward solve from *u0*; returns the final packed state."""
+        s = self.solver
+        s.reset(u0, t0=t0, tfinal=tfinal)
+        L.check(
+            s.lib.shk_plan_forward_checkpointed(
+                s._plan, s.buf_a.data_ptr(), s.buf_b.data_ptr(), self.nsteps,
+                self.ckpt.data_ptr(), self.stride, L.stream_handle()),
+            "plan_forward_checkpointed",
+        )
+        s._steps += self.nsteps
+        return s.u
+
+    def backward(self, p_final: torch.Tensor) -> torch.Tensor:
+        """``dJ/du0`` given ``dJ/du(T)`` (packed); dt frozen."""
+        s = self.solver
+        self.p_a.copy_(p_final.reshape(-1).to(self.p_a))
+        L.check(
+            s.lib.shk_plan_adjoint(
+                s._plan, self.ckpt.data_ptr(), self.stride, self.nsteps, self.seg.data_ptr(),
+                self.p_a.data_ptr(), self.p_b.data_ptr(), L.stream_handle()),
+            "plan_adjoint",
+        )
+        return (self.p_a if self.nsteps % 2 == 0 else self.p_b).clone()
+
+
+class _SolveFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, u0, solve, t0, tfinal):
+        ctx.solve = solve
+        return solve.forward(u0.detach(), t0=t0, tfinal=tfinal).clone()
+
+    @staticmethod
+    def backward(ctx, grad):
+        return ctx.solve.backward(grad.contiguous()), None, None, None
+
+
+def solve(u0: torch.Tensor, checkpointed: CheckpointedSolve, *, t0=None, tfinal=None):
+    """Differentiable batched solve: ``u(T) = solve(u0)``; ``backward`` runs the
+    hand-written adjoint with the dt sequence of the forward run frozen."""
+    return _SolveFn.apply(u0, checkpointed, t0, tfinal)
+
+
+def vjp_step(scheme, grid, dt: float, u: torch.Tensor, p_next: torch.Tensor) -> torch.Tensor:
+    """``(d advance / d u)^T p_next`` of one SSPRK33 step of a ghosted single
+    instance (``jac.T @ p`` of ``src/pyshocks/timestepping.py:205-206``)."""
+    for name, t in (("u", u), ("p", p_next)):
+        if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()
+                and t.shape[0] == grid.x.shape[0]):
+            raise ValueError(f"{name}: expected a contiguous float64 CUDA array of {grid.x.shape[0]}")
+    out = torch.empty_like(u)
+    L.check(
+        L.lib().shk_ssprk33_vjp_f64(scheme.c_scheme(grid.dx_min), u.data_ptr(), p_next.data_ptr(),
+                                    out.data_ptr(), grid.ncells, grid.nghosts,
+                                    float(grid.dx_min), float(dt), L.stream_handle()),
+        "ssprk33_vjp",
+    )
+    return out

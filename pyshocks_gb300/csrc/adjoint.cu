@@ -1,0 +1,581 @@
+// Discrete adjoint of the SSPRK33 / WENO-JS5 / Rusanov step (dt frozen).
+//
+// Reference: adjoint_step (src/pyshocks/timestepping.py:155-215) builds the
+// dense Jacobian of one step with jax.jacfwd(advance) (:174) and applies
+// p <- jac.T @ p (:206), with dt re-read from the forward checkpoints
+// (:200-201), i.e. not differentiated. Here the transpose Jacobian-vector
+// product of one step is evaluated matrix-free, one tile per work item:
+//
+//   forward:  k1 = u + dt L(u)
+//             k2 = 3/4 u + 1/4 (k1 + dt L(k1))
+//             u+ = 1/3 u + 2/3 (k2 + dt L(k2))          (timestepping.py:318-320)
+//   reverse:  k2b = 2/3 (p + dt J(k2)^T p)
+//             k1b = 1/4 (k2b + dt J(k1)^T k2b)
+//             ub  = 1/3 p + 3/4 k2b + k1b + dt J(u)^T k1b
+//
+// J(v)^T w of L(v) = -(F_{i+1/2} - F_{i-1/2})/dx is assembled from the
+// derivatives of the Rusanov flux (scalar.py:248, a = max(|f'(v_i)|,
+// |f'(v_{i+1})|) from cell values, scalar.py:243-246) and of the WENO-JS5
+// reconstruction (weno.py:114-157,247-256), differentiated by hand in the
+// product form of device.cuh. Non-differentiable points follow the JAX/torch
+// conventions: d|x|/dx = 0 at 0, and max() splits the cotangent evenly at
+// ties. The states k1, k2 are recomputed from u in shared memory (halo 18).
+//
+// Periodic boundaries are circular indexing, and cotangents live on interior
+// cells only (the reference's ghost rows carry zero cotangent when J only
+// involves interior cells, see pyshocks_gb300/adjoint.py).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <vector>
+
+#include "stencil.cuh"
+
+namespace shk {
+
+constexpr int kAdjTile = 512;
+template <class T> __host__ __device__ constexpr int adj_uhalo() { return 20; }  // 18 needed
+template <class T> __host__ __device__ constexpr int adj_phalo() { return sizeof(T) == 8 ? 10 : 12; }  // 9 needed
+constexpr int kAdjArrays = 20;
+
+template <class T>
+struct AdjSmem {
+    T *U, *K1, *K2, *PB, *CB, *Z, *ACC;
+    T *H, *D, *Q, *UL, *UR;
+    T *GL, *GR, *GA;
+    T *T0, *T1, *T2, *T3, *T4;
+
+    __host__ static size_t host_bytes(int W) { return size_t(kAdjArrays) * W * sizeof(T); }
+    __device__ void carve(unsigned char* base, int W) {
+        T* p = reinterpret_cast<T*>(base);
+        T** slots[kAdjArrays] = {&U, &K1, &K2, &PB, &CB, &Z, &ACC, &H, &D, &Q,
+                                 &UL, &UR, &GL, &GR, &GA, &T0, &T1, &T2, &T3, &T4};
+        for (int i = 0; i < kAdjArrays; ++i) *slots[i] = p + size_t(i) * W;
+    }
+    // forward-stage view (face_fluxes writes the face fluxes into D)
+    __device__ Smem<T> fwd(T* state_out) const {
+        Smem<T> s;
+        s.U = U; s.S = state_out; s.H = H; s.D = D; s.Q = Q; s.UL = UL; s.UR = UR;
+        return s;
+    }
+};
+
+// f'(u) of the physical flux and s'(u) of the wave speed
+template <int EQ, class T>
+__device__ __forceinline__ T flux_prime(T u, T c) {
+    if constexpr (EQ == SHK_EQ_BURGERS) return u;
+    else if constexpr (EQ == SHK_EQ_ADVECTION) return c;
+    else return fma(T(-2), u, T(1));
+}
+template <int EQ, class T>
+__device__ __forceinline__ T speed_prime() {
+    if constexpr (EQ == SHK_EQ_BURGERS) return T(1);
+    else if constexpr (EQ == SHK_EQ_ADVECTION) return T(0);
+    else return T(-2);
+}
+template <class T>
+__device__ __forceinline__ T sgn(T x) { return x > T(0) ? T(1) : (x < T(0) ? T(-1) : T(0)); }
+
+// d max(|s(x)|, |s(y)|) / dx   (ties split evenly, d|s|/ds = 0 at 0)
+template <int EQ, class T>
+__device__ __forceinline__ T damax_dx(T x, T y, T c) {
+    const T sx = wave_speed<EQ>(x, c), sy = wave_speed<EQ>(y, c);
+    const auto bx = abs_bits(sx), by = abs_bits(sy);
+    const T chi = bx > by ? T(1) : (bx == by ? T(0.5) : T(0));
+    return chi * sgn(sx) * speed_prime<EQ, T>();
+}
+
+// Backward of weno53_cell (device.cuh): given the cotangents of ur (urb) and
+// ul (ulb) of cell c, the contributions t_o to the cotangents of v_{c+o},
+// o = -2..2. Inputs as for weno53_cell.
+template <class T>
+__device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1, T D0, T Dp1,
+                                                T Qm1, T Q0, T Qp1, T eps, T urb, T ulb, T& t0,
+                                                T& t1, T& t2, T& t3, T& t4) {
+    // forward quantities (as weno53_cell)
+    const T h0 = fma(T(2), Hm1, Dm1);
+    const T h1 = H0 + Hm1;
+    const T h2 = fma(T(-2), H0, Dp1);
+    const T e0 = eps + fma(h0, h0, Qm1);
+    const T e1 = eps + fma(h1, h1, Q0);
+    const T e2 = eps + fma(h2, h2, Qp1);
+    const T s0 = e0 * e0, s1 = e1 * e1, s2 = e2 * e2;
+    T P0, P1, P2;
+    if constexpr (sizeof(T) == 8) {
+        P0 = s1 * s2; P1 = s0 * s2; P2 = s0 * s1;
+    } else {
+        P0 = T(1) / s0; P1 = T(1) / s1; P2 = T(1) / s2;
+    }
+    const T cr0 = fma(T(10), Hm1, T(-4) * Hm2);
+    const T cr1 = fma(T(24), H0, T(12) * Hm1);
+    const T cr2 = fma(T(-6), Hp1, T(24) * H0);
+    const T cl0 = fma(T(-10), H0, T(4) * Hp1);
+    const T cl1 = fma(T(-24), Hm1, T(-12) * H0);
+    const T cl2 = fma(T(-24), Hm1, T(6) * Hm2);
+    const T nr = fma(P0, cr0, fma(P1, cr1, P2 * cr2));
+    const T nl = fma(P2, cl0, fma(P1, cl1, P0 * cl2));
+    const T m = T(36) * P1;
+    const T dr = fma(T(6), P0, fma(T(18), P2, m));
+    const T dl = fma(T(6), P2, fma(T(18), P0, m));
+    T gR, gL, dR, dL, ie0, ie1, ie2;
+    if constexpr (sizeof(T) == 8) {
+        const T r = T(1) / (dr * dl);
+        const T rl = dl * r, rr = dr * r;  // 1/dr, 1/dl
+        gR = urb * rl;
+        gL = ulb * rr;
+        dR = nr * rl;  // ur - v
+        dL = nl * rr;  // ul - v
+        const T e01 = e0 * e1;
+        const T q = T(1) / (e01 * e2);
+        ie0 = (e1 * e2) * q;
+        ie1 = (e0 * e2) * q;
+        ie2 = e01 * q;
+    } else {
+        const T ird = T(1) / dr, ild = T(1) / dl;
+        gR = urb * ird;
+        gL = ulb * ild;
+        dR = nr * ird;
+        dL = nl * ild;
+        ie0 = T(1) / e0;
+        ie1 = T(1) / e1;
+        ie2 = T(1) / e2;
+    }
+    // interpolation part (weights held fixed): d_k P_k / D folded with the
+    // sub-stencil values 6 uhat_k
+    const T rho0 = gR * P0, rho1 = T(6) * gR * P1, rho2 = T(3) * gR * P2;
+    const T lam0 = gL * P2, lam1 = T(6) * gL * P1, lam2 = T(3) * gL * P0;
+    // smoothness part: d ur / d beta_j = -2 P_j (cr_j - W_j (ur - v)) / (e_j D_R), W = (6, 36, 18);
+    // the left side sees beta_j through its mirrored sub-stencil 2 - j
+    const T x0 = fma(gR, fma(T(-6), dR, cr0), gL * fma(T(-18), dL, cl2));
+    const T x1 = fma(gR, fma(T(-36), dR, cr1), gL * fma(T(-36), dL, cl1));
+    const T x2 = fma(gR, fma(T(-18), dR, cr2), gL * fma(T(-6), dL, cl0));
+    const T bb0 = T(-2) * (P0 * ie0) * x0;
+    const T bb1 = T(-2) * (P1 * ie1) * x1;
+    const T bb2 = T(-2) * (P2 * ie2) * x2;
+    // beta_j = h_j^2 + 13/3 D_j^2 with h_j = B_j v / 2, D_j = A_j v / 2
+    const T bh0 = bb0 * h0, bh1 = bb1 * h1, bh2 = bb2 * h2;
+    const T bd0 = bb0 * (T(13.0 / 3.0) * Dm1);
+    const T bd1 = bb1 * (T(13.0 / 3.0) * D0);
+    const T bd2 = bb2 * (T(13.0 / 3.0) * Dp1);
+    // taps: A_0 (1,-2,1,0,0) B_0 (1,-4,3,0,0) A_1 (0,1,-2,1,0) B_1 (0,-1,0,1,0)
+    //       A_2 (0,0,1,-2,1) B_2 (0,0,3,-4,1); 6 uhat right (2,-7,11,0,0) (0,-1,5,2,0)
+    //       (0,0,2,5,-1); left (0,0,11,-7,2) (0,2,5,-1,0) (-1,5,2,0,0)
+    t0 = fma(T(2), rho0, -lam2) + (bh0 + bd0);
+    t1 = fma(T(-7), rho0, -rho1) + fma(T(2), lam1, T(5) * lam2) +
+         (fma(T(-4), bh0, T(-2) * bd0) + (bd1 - bh1));
+    t2 = fma(T(11), rho0 + lam0, fma(T(5), rho1 + lam1, T(2) * (rho2 + lam2))) +
+         (fma(T(3), bh0 + bh2, bd0 + bd2) - T(2) * bd1);
+    t3 = fma(T(2), rho1, T(5) * rho2) - fma(T(7), lam0, lam1) +
+         ((bh1 + bd1) + fma(T(-4), bh2, T(-2) * bd2));
+    t4 = fma(T(2), lam0, -rho2) + (bh2 + bd2);
+}
+
+// z_i = dt (J_L(v)^T w)_i for i in [lo, hi); v valid on [lo-6, hi+6), w on
+// [lo-3, hi+3). Rusanov flux, WENO-JS5 reconstruction.
+template <class T, int EQ>
+__device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const AdjSmem<T>& a,
+                          const OpParams<T>& p, T dtdx) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int c = lo - 5 + tid; c < hi + 4; c += nt) a.H[c] = T(0.5) * (v[c + 1] - v[c]);
+    __syncthreads();
+    for (int c = lo - 4 + tid; c < hi + 4; c += nt) {
+        const T d = a.H[c] - a.H[c - 1];
+        a.D[c] = d;
+        a.Q[c] = (T(13.0 / 3.0) * d) * d;
+    }
+    __syncthreads();
+    for (int c = lo - 3 + tid; c < hi + 3; c += nt) {
+        T ul, ur;
+        weno53_cell<T>(v[c], a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
+                       a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, ul, ur);
+        a.UL[c] = ul;
+        a.UR[c] = ur;
+    }
+    __syncthreads();
+    // face j+1/2: F = 1/2 (f(L) + f(R)) - nu/2 a (L - R), L = ul_{j+1}, R = ur_j
+    for (int j = lo - 3 + tid; j < hi + 2; j += nt) {
+        const T fb = (w[j + 1] - w[j]) * dtdx;
+        const T L = a.UL[j + 1], R = a.UR[j];
+        const T ha = p.hnu * absmax(wave_speed<EQ>(v[j], p.c), wave_speed<EQ>(v[j + 1], p.c));
+        a.GL[j] = fb * fma(T(0.5), flux_prime<EQ>(L, p.c), -ha);
+        a.GR[j] = fb * fma(T(0.5), flux_prime<EQ>(R, p.c), ha);
+        a.GA[j] = -(fb * p.hnu) * (L - R);
+    }
+    __syncthreads();
+    for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
+        T t0, t1, t2, t3, t4;
+        weno53_cell_vjp<T>(a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
+                           a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, a.GR[c],
+                           a.GL[c - 1], t0, t1, t2, t3, t4);
+        a.T0[c] = t0; a.T1[c] = t1; a.T2[c] = t2; a.T3[c] = t3; a.T4[c] = t4;
+    }
+    __syncthreads();
+    for (int i = lo + tid; i < hi; i += nt) {
+        T acc = (a.T0[i + 2] + a.T1[i + 1]) + a.T2[i] + (a.T3[i - 1] + a.T4[i - 2]);
+        // wave-speed terms: face i-1/2 (cells i-1, i) and face i+1/2 (cells i, i+1)
+        acc = fma(a.GA[i - 1], damax_dx<EQ>(v[i], v[i - 1], p.c), acc);
+        acc = fma(a.GA[i], damax_dx<EQ>(v[i], v[i + 1], p.c), acc);
+        z[i] = acc;
+    }
+    __syncthreads();
+}
+
+// one adjoint step of a tile: p_out[s, s+te) from u_m (window, halo 20) and
+// p_next (window, halo 10/12). gout points at p_out + s.
+template <class T, int EQ>
+__device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const OpParams<T>& p) {
+    constexpr int HU = adj_uhalo<T>();
+    const int tid = threadIdx.x, nt = blockDim.x;
+    // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12)
+    {
+        const int lo = HU - 15, hi = HU + te + 15;
+        face_fluxes<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_RUSANOV>(a.U, lo, hi, a.fwd(a.K1), p);
+        for (int i = lo + tid; i < hi; i += nt) a.K1[i] = fma(dtdx, a.D[i - 1] - a.D[i], a.U[i]);
+        __syncthreads();
+    }
+    {
+        const int lo = HU - 12, hi = HU + te + 12;
+        face_fluxes<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_RUSANOV>(a.K1, lo, hi, a.fwd(a.K2), p);
+        for (int i = lo + tid; i < hi; i += nt) {
+            const T k = fma(dtdx, a.D[i - 1] - a.D[i], a.K1[i]);
+            a.K2[i] = fma(T(1.0 / 4.0), k, T(3.0 / 4.0) * a.U[i]);
+        }
+        __syncthreads();
+    }
+    // reverse stage 3: k2b = 2/3 (p + dt J(k2)^T p) on [HU-6, HU+te+6)
+    {
+        const int lo = HU - 6, hi = HU + te + 6;
+        vjp_stage<T, EQ>(a.K2, a.PB, a.Z, lo, hi, a, p, dtdx);
+        for (int i = lo + tid; i < hi; i += nt) a.CB[i] = T(2.0 / 3.0) * (a.PB[i] + a.Z[i]);
+        __syncthreads();
+        for (int i = HU + tid; i < HU + te; i += nt)
+            a.ACC[i] = fma(T(3.0 / 4.0), a.CB[i], T(1.0 / 3.0) * a.PB[i]);
+        __syncthreads();
+    }
+    // reverse stage 2: k1b = 1/4 (k2b + dt J(k1)^T k2b) on [HU-3, HU+te+3)
+    {
+        const int lo = HU - 3, hi = HU + te + 3;
+        vjp_stage<T, EQ>(a.K1, a.CB, a.Z, lo, hi, a, p, dtdx);
+        for (int i = lo + tid; i < hi; i += nt) a.CB[i] = T(1.0 / 4.0) * (a.CB[i] + a.Z[i]);
+        __syncthreads();
+    }
+    // reverse stage 1: ub = 1/3 p + 3/4 k2b + k1b + dt J(u)^T k1b on the tile
+    {
+        const int lo = HU, hi = HU + te;
+        vjp_stage<T, EQ>(a.U, a.CB, a.Z, lo, hi, a, p, dtdx);
+        for (int i = lo + tid; i < hi; i += nt) gout[i - HU] = a.ACC[i] + (a.CB[i] + a.Z[i]);
+    }
+}
+
+template <class T>
+__device__ __forceinline__ bool adjoint_load(const AdjSmem<T>& a, const T* um, const T* pn,
+                                             int64_t n, int64_t s0, int te, uint64_t* bar,
+                                             uint32_t& phase) {
+    constexpr int HU = adj_uhalo<T>(), HP = adj_phalo<T>();
+    if (!load_window<T>(a.U, um, n, s0 - HU, te + 2 * HU, bar, phase)) return false;
+    return load_window<T>(a.PB + (HU - HP), pn, n, s0 - HP, te + 2 * HP, bar, phase);
+}
+
+template <class T, int EQ>
+__global__ void __launch_bounds__(kThreads) batched_adjoint_kernel(PlanDev P, const T* __restrict__ um,
+                                                                   const T* __restrict__ pnext,
+                                                                   T* __restrict__ pout,
+                                                                   const double* __restrict__ dt_row,
+                                                                   OpParams<T> p) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    AdjSmem<T> a;
+    a.carve(smem_raw, P.tile + 2 * adj_uhalo<T>());
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
+        const int b = P.item_inst[item];
+        const int64_t off = P.offsets[b];
+        const int64_t n = P.offsets[b + 1] - off;
+        const int64_t s0 = int64_t(P.item_tile[item]) * P.tile;
+        const int te = static_cast<int>(imin64(P.tile, n - s0));
+        const double dt = dt_row[b];
+        if (dt == 0.0) {  // no step was taken: identity
+            for (int i = threadIdx.x; i < te; i += blockDim.x) pout[off + s0 + i] = pnext[off + s0 + i];
+            __syncthreads();
+            continue;
+        }
+        if (!adjoint_load<T>(a, um + off, pnext + off, n, s0, te, &bar, phase)) {
+            if (threadIdx.x == 0) atomicOr(P.status, ERR_TIMEOUT);
+            return;
+        }
+        const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
+        adjoint_tile<T, EQ>(a, pout + off + s0, te, dtdx, p);
+        __syncthreads();
+    }
+}
+
+// forward step with a recorded dt (no CFL, no time update): recompute of the
+// states between checkpoints
+template <class T, int EQ>
+__global__ void __launch_bounds__(kThreads) replay_step_kernel(PlanDev P, const T* __restrict__ uin,
+                                                               T* __restrict__ uout,
+                                                               const double* __restrict__ dt_row,
+                                                               OpParams<T> p) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    constexpr int HL = step_halo<T>();
+    Smem<T> sm;
+    sm.carve(smem_raw, P.tile + 2 * HL);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
+        const int b = P.item_inst[item];
+        const int64_t off = P.offsets[b];
+        const int64_t n = P.offsets[b + 1] - off;
+        const int64_t s0 = int64_t(P.item_tile[item]) * P.tile;
+        const int te = static_cast<int>(imin64(P.tile, n - s0));
+        const double dt = dt_row[b];
+        if (dt == 0.0) {
+            for (int i = threadIdx.x; i < te; i += blockDim.x) uout[off + s0 + i] = uin[off + s0 + i];
+            __syncthreads();
+            continue;
+        }
+        if (!load_window<T>(sm.U, uin + off, n, s0 - HL, te + 2 * HL, &bar, phase)) {
+            if (threadIdx.x == 0) atomicOr(P.status, ERR_TIMEOUT);
+            return;
+        }
+        const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
+        step_tile<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_RUSANOV>(sm, uout + off + s0, te, dtdx, p);
+        __syncthreads();
+    }
+}
+
+// single instance on the reference's ghosted layout (drop-in adjoint_step)
+template <class T, int EQ>
+__global__ void __launch_bounds__(kThreads) single_vjp_kernel(const T* __restrict__ u, const T* __restrict__ pn,
+                                                              T* __restrict__ pout, int64_t n, int g,
+                                                              int tile, T dtdx, OpParams<T> p,
+                                                              int32_t* err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    AdjSmem<T> a;
+    a.carve(smem_raw, tile + 2 * adj_uhalo<T>());
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const int64_t s0 = int64_t(blockIdx.x) * tile;
+    const int te = static_cast<int>(imin64(tile, n - s0));
+    if (!adjoint_load<T>(a, u + g, pn + g, n, s0, te, &bar, phase)) {
+        if (threadIdx.x == 0 && err) atomicOr(err, ERR_TIMEOUT);
+        return;
+    }
+    adjoint_tile<T, EQ>(a, pout + g + s0, te, dtdx, p);
+    // ghost cotangents are zero (interior-only adjoint)
+    if (blockIdx.x == 0)
+        for (int i = threadIdx.x; i < g; i += blockDim.x) {
+            pout[i] = T(0);
+            pout[g + n + i] = T(0);
+        }
+}
+
+}  // namespace shk
+
+// ===========================================================================
+// host side
+// ===========================================================================
+using namespace shk;
+
+namespace {
+
+int acuda(cudaError_t e) {
+    if (e != cudaSuccess) {
+        std::fprintf(stderr, "libshocks: CUDA error %s\n", cudaGetErrorString(e));
+        return SHK_ECUDA;
+    }
+    return SHK_OK;
+}
+#define ADJ_CUDA(call)                          \
+    do {                                        \
+        int _st = acuda(call);                  \
+        if (_st != SHK_OK) return _st;          \
+    } while (0)
+
+template <class T>
+OpParams<T> adj_params(const shk_scheme* s) {
+    OpParams<T> p;
+    p.eps = static_cast<T>(s->eps);
+    p.delta = static_cast<T>(s->delta);
+    p.hnu = static_cast<T>(0.5 * s->nu);
+    p.c = static_cast<T>(s->speed);
+    p.hnu_amax = T(0);
+    return p;
+}
+
+bool adjoint_supported(const shk_scheme* s) {
+    return s && s->flux == SHK_FLUX_RUSANOV && s->rec == SHK_REC_WENOJS53 && s->equation >= 0 &&
+           s->equation <= SHK_EQ_LWR;
+}
+
+template <class T, class F>
+int by_equation(int eq, F&& f) {
+    switch (eq) {
+        case SHK_EQ_BURGERS: return f.template operator()<T, SHK_EQ_BURGERS>();
+        case SHK_EQ_ADVECTION: return f.template operator()<T, SHK_EQ_ADVECTION>();
+        case SHK_EQ_LWR: return f.template operator()<T, SHK_EQ_LWR>();
+    }
+    return SHK_EINVAL;
+}
+
+template <class TS>
+struct AdjLaunch {
+    PlanDev D; const void* um; const void* pn; void* po; const double* dt_row; OpParams<TS> p;
+    size_t smem; int grid; cudaStream_t st;
+    template <class T, int EQ> int operator()() {
+        auto k = batched_adjoint_kernel<T, EQ>;
+        ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(um), static_cast<const T*>(pn),
+                                         static_cast<T*>(po), dt_row, p);
+        return acuda(cudaGetLastError());
+    }
+};
+
+template <class TS>
+struct ReplayLaunch {
+    PlanDev D; const void* uin; void* uout; const double* dt_row; OpParams<TS> p;
+    size_t smem; int grid; cudaStream_t st;
+    template <class T, int EQ> int operator()() {
+        auto k = replay_step_kernel<T, EQ>;
+        ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(uin), static_cast<T*>(uout), dt_row, p);
+        return acuda(cudaGetLastError());
+    }
+};
+
+struct SingleVjpLaunch {
+    const double* u; const double* pn; double* po; int64_t n; int g; int tile; double dtdx;
+    OpParams<double> p; size_t smem; int blocks; cudaStream_t st;
+    template <class T, int EQ> int operator()() {
+        auto k = single_vjp_kernel<T, EQ>;
+        ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k<<<blocks, kThreads, smem, st>>>(u, pn, po, n, g, tile, dtdx, p, nullptr);
+        return acuda(cudaGetLastError());
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int shk_ssprk33_vjp_f64(const shk_scheme* scheme, const double* u, const double* p_next,
+                        double* p_out, int64_t n, int32_t nghosts, double dx, double dt,
+                        void* stream) {
+    if (!adjoint_supported(scheme) || !u || !p_next || !p_out || n < 3 || nghosts < 3 ||
+        !(dx > 0) || !(dt >= 0))
+        return SHK_EINVAL;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int tile = kAdjTile;
+    const int W = tile + 2 * adj_uhalo<double>();
+    const size_t smem = AdjSmem<double>::host_bytes(W);
+    const int blocks = static_cast<int>((n + tile - 1) / tile);
+    SingleVjpLaunch f{u, p_next, p_out, n, nghosts, tile, dt / dx, adj_params<double>(scheme),
+                      smem, blocks, st};
+    return by_equation<double>(scheme->equation, f);
+}
+
+int shk_plan_forward_checkpointed(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps,
+                                  void* ckpt, int32_t stride, void* stream) {
+    PlanDev D;
+    int dtype = 0, grid = 0;
+    shk_scheme sch;
+    int64_t total = 0;
+    if (!plan || !u_a || !u_b || !ckpt || nsteps < 0 || stride <= 0) return SHK_EINVAL;
+    int64_t hsteps = 0;
+    int r = plan_view(plan, &D, &dtype, &grid, &sch, &total, &hsteps);
+    if (r != SHK_OK) return r;
+    // checkpoints and the dt history are indexed from the last reset
+    if (!D.dt_hist || D.max_steps < nsteps || hsteps != 0) return SHK_EINVAL;
+    const size_t bytes = size_t(total) * (dtype == SHK_F64 ? 8 : 4);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    for (int k = 0; k < nsteps; ++k) {
+        if (k % stride == 0) {
+            // the state before step k is in u_a for even k, u_b for odd k
+            const void* cur = (k % 2 == 0) ? u_a : u_b;
+            ADJ_CUDA(cudaMemcpyAsync(static_cast<char*>(ckpt) + size_t(k / stride) * bytes, cur,
+                                     bytes, cudaMemcpyDeviceToDevice, st));
+        }
+        r = shk_plan_step(plan, u_a, u_b, 1, stream);
+        if (r != SHK_OK) return r;
+    }
+    return SHK_OK;
+}
+
+int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t nsteps, void* seg,
+                     void* p_a, void* p_b, void* stream) {
+    PlanDev D;
+    int dtype = 0, grid = 0;
+    shk_scheme sch;
+    int64_t total = 0;
+    if (!plan || !ckpt || !seg || !p_a || !p_b || p_a == p_b || nsteps < 0 || stride <= 0)
+        return SHK_EINVAL;
+    int r = plan_view(plan, &D, &dtype, &grid, &sch, &total, nullptr);
+    if (r != SHK_OK) return r;
+    if (!adjoint_supported(&sch)) return SHK_EUNSUPPORTED;
+    if (!D.dt_hist || D.max_steps < nsteps) return SHK_EINVAL;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const size_t esz = dtype == SHK_F64 ? 8 : 4;
+    const size_t bytes = size_t(total) * esz;
+    const int W = D.tile + 2 * adj_uhalo<double>();
+    const size_t asmem = dtype == SHK_F64 ? AdjSmem<double>::host_bytes(W) : AdjSmem<float>::host_bytes(W);
+    const size_t fsmem = dtype == SHK_F64 ? Smem<double>::host_bytes(D.tile + 2 * step_halo<double>())
+                                          : Smem<float>::host_bytes(D.tile + 2 * step_halo<float>());
+    // adjoint grid: resident CTAs for its larger shared-memory footprint
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int per_sm = std::max(1, static_cast<int>((220 * 1024) / std::max<size_t>(asmem, 1)));
+    const int agrid = std::max(1, std::min(D.nitems, per_sm * sms));
+    auto seg_at = [&](int j) { return static_cast<char*>(seg) + size_t(j) * bytes; };
+    const int nseg = (nsteps + stride - 1) / stride;
+    void* cur = p_a;
+    void* nxt = p_b;
+    for (int sgi = nseg - 1; sgi >= 0; --sgi) {
+        const int base = sgi * stride;
+        const int cnt = std::min(stride, nsteps - base);
+        ADJ_CUDA(cudaMemcpyAsync(seg_at(0), static_cast<const char*>(ckpt) + size_t(sgi) * bytes,
+                                 bytes, cudaMemcpyDeviceToDevice, st));
+        for (int j = 1; j < cnt; ++j) {
+            const double* row = D.dt_hist + size_t(base + j - 1) * D.B;
+            if (dtype == SHK_F64) {
+                ReplayLaunch<double> f{D, seg_at(j - 1), seg_at(j), row, adj_params<double>(&sch), fsmem, grid, st};
+                r = by_equation<double>(sch.equation, f);
+            } else {
+                ReplayLaunch<float> f{D, seg_at(j - 1), seg_at(j), row, adj_params<float>(&sch), fsmem, grid, st};
+                r = by_equation<float>(sch.equation, f);
+            }
+            if (r != SHK_OK) return r;
+        }
+        for (int j = cnt - 1; j >= 0; --j) {
+            const double* row = D.dt_hist + size_t(base + j) * D.B;
+            if (dtype == SHK_F64) {
+                AdjLaunch<double> f{D, seg_at(j), cur, nxt, row, adj_params<double>(&sch), asmem, agrid, st};
+                r = by_equation<double>(sch.equation, f);
+            } else {
+                AdjLaunch<float> f{D, seg_at(j), cur, nxt, row, adj_params<float>(&sch), asmem, agrid, st};
+                r = by_equation<float>(sch.equation, f);
+            }
+            if (r != SHK_OK) return r;
+            std::swap(cur, nxt);
+        }
+    }
+    return SHK_OK;
+}
+
+}  // extern "C"

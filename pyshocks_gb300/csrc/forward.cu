@@ -24,250 +24,13 @@
 #include <new>
 #include <vector>
 
-#include "device.cuh"
+#include "stencil.cuh"
 
 namespace shk {
-
-constexpr int kThreads = 256;
-constexpr int kDefaultTile = 1024;
-
-// halo of a window: 9 cells are needed for three fused stages, rounded up so
-// that the window start stays 16-byte aligned for cp.async.bulk
-template <class T> __host__ __device__ constexpr int step_halo() { return sizeof(T) == 8 ? 10 : 12; }
-template <class T> __host__ __device__ constexpr int op_halo() { return 4; }
-
-__host__ __device__ inline int64_t imin64(int64_t a, int64_t b) { return a < b ? a : b; }
-
-__host__ __device__ inline int64_t imod(int64_t a, int64_t n) {
-    int64_t r = a % n;
-    return r < 0 ? r + n : r;
-}
-
-// ---------------------------------------------------------------------------
-// shared-memory layout of one work item (window of W cells)
-// ---------------------------------------------------------------------------
-template <class T>
-struct Smem {
-    T* U;   // u at the start of the step (window)
-    T* S;   // stage state k1 / k2
-    T* H;   // half differences
-    T* D;   // half second differences; reused for face fluxes F
-    T* Q;   // 13/12 (2D)^2; reused for ES-WENO omega_0
-    T* UL;  // ul (value at the left face of the cell)
-    T* UR;  // ur (value at the right face of the cell)
-
-    __device__ static size_t bytes(int W) { return size_t(7) * W * sizeof(T); }
-    __host__ static size_t host_bytes(int W) { return size_t(7) * W * sizeof(T); }
-    __device__ void carve(unsigned char* base, int W) {
-        T* p = reinterpret_cast<T*>(base);
-        U = p; S = p + W; H = p + 2 * W; D = p + 3 * W; Q = p + 4 * W;
-        UL = p + 5 * W; UR = p + 6 * W;
-    }
-};
-
-template <class T>
-struct OpParams {
-    T eps, delta, hnu, c;  // WENO eps, ES-WENO delta, nu/2, advection speed
-    T hnu_amax;            // LF: nu/2 * global max |f'|
-};
-
-// ---------------------------------------------------------------------------
-// one evaluation of the numerical fluxes F_j (face j+1/2) for j in [lo-1, hi)
-// from the stage input v (valid on [lo-3, hi+3)). Leaves F in sm.D.
-// ---------------------------------------------------------------------------
-template <class T, int EQ, int REC, int FLUX>
-__device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Smem<T>& sm,
-                                            const OpParams<T>& p) {
-    const int tid = threadIdx.x, nt = blockDim.x;
-    if constexpr (REC == SHK_REC_WENOJS53) {
-        // phase A: H_c = (v_{c+1} - v_c)/2, c in [lo-3, hi+2)
-        for (int c = lo - 3 + tid; c < hi + 2; c += nt) sm.H[c] = T(0.5) * (v[c + 1] - v[c]);
-        __syncthreads();
-        // phase B: D_c = H_c - H_{c-1}, Q_c = 13/12 (2 D_c)^2, c in [lo-2, hi+2)
-        for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
-            const T d = sm.H[c] - sm.H[c - 1];
-            sm.D[c] = d;
-            sm.Q[c] = (T(13.0 / 3.0) * d) * d;
-        }
-        __syncthreads();
-        // phase C: ul, ur of cells [lo-1, hi+1)
-        for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
-            T ul, ur;
-            weno53_cell<T>(v[c], sm.H[c - 2], sm.H[c - 1], sm.H[c], sm.H[c + 1], sm.D[c - 1],
-                           sm.D[c], sm.D[c + 1], sm.Q[c - 1], sm.Q[c], sm.Q[c + 1], p.eps, ul,
-                           ur);
-            sm.UL[c] = ul;
-            sm.UR[c] = ur;
-        }
-        __syncthreads();
-    } else {
-        for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
-            T ul, ur, w0;
-            esweno32_cell<T>(v[c - 1], v[c], v[c + 1], p.eps, ul, ur, w0);
-            sm.UL[c] = ul;
-            sm.UR[c] = ur;
-            sm.Q[c] = w0;
-        }
-        __syncthreads();
-    }
-    // phase D: F_j, j in [lo-1, hi)
-    for (int j = lo - 1 + tid; j < hi; j += nt) {
-        T f;
-        if constexpr (FLUX == SHK_FLUX_RUSANOV) {
-            f = rusanov_face<EQ, T>(sm.UR[j], sm.UL[j + 1], v[j], v[j + 1], p.hnu, p.c);
-        } else if constexpr (FLUX == SHK_FLUX_LF) {
-            f = lf_face<EQ, T>(sm.UR[j], sm.UL[j + 1], p.hnu_amax, p.c);
-        } else {
-            f = esweno_face<EQ, T>(sm.UR[j], sm.UL[j + 1], v[j], v[j + 1], sm.Q[j], sm.Q[j + 1],
-                                   p.delta, p.c);
-        }
-        sm.D[j] = f;
-    }
-    __syncthreads();
-}
-
-// ---------------------------------------------------------------------------
-// window loader: cells g0 .. g0+W-1 of a periodic instance (mod n) into dst.
-// Uses cp.async.bulk (TMA 1D, no multicast) into the CTA's own shared memory
-// when every piece is 16-byte aligned, plain coalesced loads otherwise.
-// Returns false if the bulk copy did not complete within the wait limit.
-// ---------------------------------------------------------------------------
-template <class T>
-__device__ bool load_window(T* dst, const T* base, int64_t n, int64_t g0, int W,
-                            uint64_t* bar, uint32_t& phase) {
-    const size_t sz = sizeof(T);
-    bool bulk = (reinterpret_cast<uintptr_t>(base) % 16 == 0) &&
-                (reinterpret_cast<uintptr_t>(dst) % 16 == 0);
-    {
-        int64_t pos = g0;
-        const int64_t end = g0 + W;
-        int npieces = 0;
-        while (pos < end && bulk) {
-            const int64_t src = imod(pos, n);
-            const int64_t len = min(end - pos, n - src);
-            if ((src * sz) % 16 || (len * sz) % 16 || ((pos - g0) * sz) % 16) bulk = false;
-            pos += len;
-            if (++npieces > 8) bulk = false;  // tiny instances: plain loads
-        }
-    }
-    if (!bulk) {
-        for (int w = threadIdx.x; w < W; w += blockDim.x) dst[w] = base[imod(g0 + w, n)];
-        __syncthreads();
-        return true;
-    }
-    // order earlier generic-proxy accesses of dst before the async-proxy writes
-    fence_proxy_async();
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        mbar_expect_tx(bar, static_cast<uint32_t>(W * sz));
-        int64_t pos = g0;
-        const int64_t end = g0 + W;
-        while (pos < end) {
-            const int64_t src = imod(pos, n);
-            const int64_t len = min(end - pos, n - src);
-            bulk_g2s(dst + (pos - g0), base + src, static_cast<uint32_t>(len * sz), bar);
-            pos += len;
-        }
-    }
-    bool ok = mbar_wait_bounded(bar, phase);
-    if (!ok) ok = mbar_wait_bounded(bar, phase);  // second bounded wait for copies in flight
-    phase ^= 1u;
-    return __syncthreads_and(ok) != 0;
-}
-
-// ---------------------------------------------------------------------------
-// per-instance CFL time step (timestepping.py:139-145 with the Rusanov
-// estimate of burgers/schemes.py:121-127 and the driver's theta)
-// ---------------------------------------------------------------------------
-struct DtState {
-    double dt;
-    bool active;  // t < tfinal (timestepping.py:133-134)
-    bool finite;
-};
-__host__ __device__ inline DtState compute_dt(double smax, double cfl, double theta, double t,
-                                              double tfinal) {
-    DtState s;
-    s.active = t < tfinal;
-    double dt = theta * (cfl / smax);
-    if (tfinal != INFINITY) {
-        const double dtmin = tfinal - t;
-        dt = (dt < dtmin ? dt : dtmin) + 1.0e-15;
-    }
-    s.dt = dt;
-    s.finite = isfinite(dt);
-    return s;
-}
-
-// ---------------------------------------------------------------------------
-// fused SSPRK33 step of one tile: window [s - HL, s + te + HL) -> u_out[s, s + te)
-// returns the thread's max |f'(u_new)| bits
-// ---------------------------------------------------------------------------
-template <class T, int EQ, int REC, int FLUX>
-__device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, T dtdx,
-                                            const OpParams<T>& p) {
-    constexpr int HL = step_halo<T>();
-    const int tid = threadIdx.x, nt = blockDim.x;
-    // stage 1: k1 = u + dt L(u) on [HL-6, HL+te+6)
-    {
-        const int lo = HL - 6, hi = HL + te + 6;
-        face_fluxes<T, EQ, REC, FLUX>(sm.U, lo, hi, sm, p);
-        for (int i = lo + tid; i < hi; i += nt) sm.S[i] = fma(dtdx, sm.D[i - 1] - sm.D[i], sm.U[i]);
-        __syncthreads();
-    }
-    // stage 2: k2 = 3/4 u + 1/4 (k1 + dt L(k1)) on [HL-3, HL+te+3) (in place over k1)
-    {
-        const int lo = HL - 3, hi = HL + te + 3;
-        face_fluxes<T, EQ, REC, FLUX>(sm.S, lo, hi, sm, p);
-        for (int i = lo + tid; i < hi; i += nt) {
-            const T k = fma(dtdx, sm.D[i - 1] - sm.D[i], sm.S[i]);
-            sm.S[i] = fma(T(1.0 / 4.0), k, T(3.0 / 4.0) * sm.U[i]);
-        }
-        __syncthreads();
-    }
-    // stage 3: u+ = 1/3 u + 2/3 (k2 + dt L(k2)) on the tile
-    using B = typename Bits<T>::type;
-    B mx = 0;
-    {
-        const int lo = HL, hi = HL + te;
-        face_fluxes<T, EQ, REC, FLUX>(sm.S, lo, hi, sm, p);
-        for (int i = lo + tid; i < hi; i += nt) {
-            const T k = fma(dtdx, sm.D[i - 1] - sm.D[i], sm.S[i]);
-            const T un = fma(T(2.0 / 3.0), k, T(1.0 / 3.0) * sm.U[i]);
-            gout[i - HL] = un;
-            const B b = abs_bits(wave_speed<EQ>(un, p.c));
-            mx = b > mx ? b : mx;
-        }
-    }
-    return mx;
-}
 
 // ---------------------------------------------------------------------------
 // batched persistent stepping kernel
 // ---------------------------------------------------------------------------
-struct PlanDev {
-    const int32_t* item_inst;
-    const int32_t* item_tile;
-    const int64_t* offsets;  // [B+1]
-    const double* cfl;       // [B] 0.5 dx^(2-alpha)
-    const double* inv_dx;    // [B]
-    const double* tfinal;    // [B]
-    double theta;
-    unsigned long long* amax;  // [2][B] bits of max |f'(u)| (as double)
-    double* t;                 // [B]
-    double* dt_hist;           // [max_steps][B] or null
-    int64_t* step;
-    unsigned int* done;
-    int32_t* status;
-    double* partial;  // [nitems]
-    int32_t B, nitems, tile, max_steps;
-};
-
-template <class T>
-__device__ __forceinline__ unsigned long long to_double_bits(typename Bits<T>::type b) {
-    if constexpr (sizeof(T) == 8) return b;
-    else return abs_bits(static_cast<double>(from_bits(b)));
-}
-
 __device__ void finalize_step(const PlanDev& P, int64_t k) {
     const int cur = static_cast<int>(k & 1);
     for (int b = threadIdx.x; b < P.B; b += blockDim.x) {
@@ -697,6 +460,20 @@ int launch_step(shk_plan* P, const void* uin, void* uout, cudaStream_t st) {
     return dispatch_scheme<T>(&P->scheme, f);
 }
 }  // namespace
+
+namespace shk {
+int plan_view(shk_plan* plan, PlanDev* dev, int* dtype, int* grid, shk_scheme* scheme,
+              int64_t* total_cells, int64_t* host_steps) {
+    if (!plan) return SHK_EINVAL;
+    if (host_steps) *host_steps = plan->host_steps;
+    *dev = plan->dev();
+    *dtype = plan->dtype;
+    *grid = plan->grid;
+    *scheme = plan->scheme;
+    *total_cells = plan->total_cells;
+    return SHK_OK;
+}
+}  // namespace shk
 
 extern "C" {
 

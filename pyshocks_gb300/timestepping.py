@@ -186,3 +186,56 @@ def predict_maxit_from_timestep(tfinal: float, dt: float) -> tuple[int, float]:
     """``src/pyshocks/timestepping.py:251-261``."""
     maxit = int(tfinal / dt)
     return maxit, tfinal / maxit + 1.0e-15
+
+
+def adjoint_step(
+    stepper: Stepper,
+    p0: torch.Tensor,
+    *,
+    maxit: int,
+    apply_boundary: Callable[[float, torch.Tensor, torch.Tensor], torch.Tensor] | None = None,
+) -> Iterator[AdjointStepCompleted]:
+    """``src/pyshocks/timestepping.py:155-215``: the reverse sweep over the
+    checkpoints saved by :func:`step`, with dt re-read from them (frozen).
+
+    For a stepper built by :func:`make_time_stepper` each transpose step is one
+    matrix-free CUDA kernel (``shk_ssprk33_vjp_f64``) instead of a dense
+    ``jax.jacfwd`` Jacobian. Cotangents live on interior cells (ghost entries of
+    *p0* are ignored and returned as zero)."""
+    if stepper.checkpoint is None:
+        raise ValueError("Adjoint time stepping requires a checkpoint.")
+    src = stepper.source
+    from pyshocks_gb300 import adjoint as adj
+    from pyshocks_gb300 import burgers
+
+    fused = isinstance(src, OperatorSource) and isinstance(
+        src.scheme, burgers.GpuConservationLawScheme) and src.scheme.flux_code == burgers.L.SHK_FLUX_RUSANOV
+
+    def _vjp(dt, t, u, p):
+        if fused:
+            return adj.vjp_step(src.scheme, src.grid, dt, u, p)
+        # generic closures: differentiate advance() with torch (dt, t constant)
+        _, fn = torch.func.vjp(lambda v: advance(stepper, dt, t, v), u)
+        return fn(p)[0]
+
+    chk = load(stepper.checkpoint, maxit)
+    assert chk["m"] == maxit
+    t = tfinal = chk["t"]
+    p = p0
+    if fused:
+        g = src.grid.nghosts
+        p = p.clone()
+        p[:g] = 0
+        p[p.shape[0] - g:] = 0
+    if apply_boundary is not None:
+        p = apply_boundary(chk["t"], chk["u"], p)
+    yield AdjointStepCompleted(t=t, tfinal=tfinal, dt=0.0, iteration=maxit, u=chk["u"], p=p)
+    for m in range(maxit - 1, -1, -1):
+        chk = load(stepper.checkpoint, m)
+        dt = t - chk["t"]
+        assert chk["m"] == m
+        p = _vjp(dt, chk["t"], chk["u"], p)
+        if apply_boundary is not None:
+            p = apply_boundary(chk["t"], chk["u"], p)
+        t = chk["t"]
+        yield AdjointStepCompleted(t=t, tfinal=tfinal, dt=dt, iteration=m, u=chk["u"], p=p)

@@ -1,0 +1,190 @@
+"""Discrete adjoint kernels against the torch-CPU float64 autograd oracle (the
+stand-in for ``jax.jacfwd`` in ``src/pyshocks/timestepping.py:174``) and
+central finite differences with the dt sequence frozen.
+
+Tolerances: one-step VJPs within 1e-11 of autograd relative to the cotangent
+scale; multi-step gradients within 1e-9 relative; finite differences
+(h = 1e-6) within 1e-5 relative.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import numpy_ref as R
+from oracle import torch_ref as T
+
+pytestmark = pytest.mark.gpu
+
+
+def _scheme(eq="burgers"):
+    from pyshocks_gb300 import burgers, reconstruction
+
+    rec = reconstruction.make_reconstruction_from_name("wenojs53", eps=1.0e-6)
+    return {"burgers": burgers.Rusanov(rec=rec), "lwr": burgers.LWRRusanov(rec=rec),
+            "advection": burgers.AdvectionRusanov(rec=rec)}[eq]
+
+
+def _state(n, seed, eq):
+    og = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+    rng = np.random.default_rng(seed)
+    return R.lwr_ic(rng, og.f) if eq == "lwr" else R.random_fourier_ic(rng, og.f)
+
+
+@pytest.mark.parametrize(("n", "eq"), [(64, "burgers"), (300, "burgers"), (1024, "burgers"),
+                                        (3001, "burgers"), (512, "lwr"), (256, "advection")])
+def test_single_step_vjp_matches_autograd(n, eq):
+    import pyshocks_gb300 as gb
+    from pyshocks_gb300 import adjoint
+
+    u0 = _state(n, n, eq)
+    rng = np.random.default_rng(n + 1)
+    p = rng.standard_normal(n + 6)
+    dx = 2.0 / n
+    ut = torch.tensor(u0[3:-3])[None]
+    dt = 0.8 * float(T.predict_dt(ut, dx, equation=eq)[0])
+    ref = T.step_vjp(ut, torch.tensor(p[3:-3])[None], dt, dx, equation=eq)[0].numpy()
+
+    grid = gb.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
+    out = adjoint.vjp_step(_scheme(eq), grid, dt, torch.tensor(u0, device="cuda"),
+                           torch.tensor(p, device="cuda")).cpu().numpy()
+    err = np.max(np.abs(out[3:-3] - ref)) / np.max(np.abs(ref))
+    assert err < 1.0e-11, err
+    np.testing.assert_array_equal(out[:3], 0.0)
+    np.testing.assert_array_equal(out[-3:], 0.0)
+
+
+def test_vjp_at_ties_splits_the_max_evenly():
+    """Constant plateaus make |u_i| = |u_{i+1}|: max() ties, where the cotangent
+    is split evenly (JAX/torch convention). Inside a plateau L(u) = 0 exactly,
+    so the ties survive exactly into k1 and k2 on both sides of the comparison
+    (ties created only in exact arithmetic, e.g. a symmetric +a/-a jump, break
+    differently under different roundings and are not a meaningful check)."""
+    import pyshocks_gb300 as gb
+    from pyshocks_gb300 import adjoint
+
+    n = 128
+    u = np.full(n, 0.3)
+    u[20:70] = 0.95
+    u[90:100] = -0.5
+    ug = np.concatenate([u[-3:], u, u[:3]])
+    p = np.random.default_rng(2).standard_normal(n + 6)
+    dx = 2.0 / n
+    dt = 0.5 * dx / 0.95
+    ref = T.step_vjp(torch.tensor(u)[None], torch.tensor(p[3:-3])[None], dt, dx)[0].numpy()
+    grid = gb.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
+    out = adjoint.vjp_step(_scheme(), grid, dt, torch.tensor(ug, device="cuda"),
+                           torch.tensor(p, device="cuda")).cpu().numpy()[3:-3]
+    assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < 1.0e-11
+
+
+def test_adjoint_step_generator_matches_autograd():
+    """The reference-style ``step`` + ``adjoint_step`` pair (InMemoryCheckpoint,
+    dt = t_{m+1} - t_m re-read from checkpoints) against autograd through the
+    same frozen dt sequence."""
+    import pyshocks_gb300 as gb
+    from pyshocks_gb300.checkpointing import InMemoryCheckpoint
+
+    n, maxit = 128, 30
+    g = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+    u0 = R.exact_cell_average_sine(g)
+    grid = gb.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
+    bc = gb.scalar.PeriodicBoundary()
+    stepper = gb.timestepping.make_time_stepper(_scheme(), grid, bc, theta=1.0,
+                                                checkpoint=InMemoryCheckpoint("Iteration"))
+    ev = None
+    for ev in gb.timestepping.step(stepper, torch.tensor(u0, device="cuda"), maxit=maxit):
+        pass
+    uT = ev.u
+    p0 = uT.clone()  # J = 1/2 |u(T)|^2 over the interior
+    dts = []
+    for ev in gb.timestepping.adjoint_step(stepper, p0, maxit=maxit):
+        if ev.iteration < maxit:
+            dts.append(ev.dt)
+    grad = ev.p.cpu().numpy()[3:-3]
+    dts = torch.tensor(dts[::-1]).reshape(-1, 1)
+    u0t = torch.tensor(u0[3:-3])[None]
+    ref, _, _ = T.adjoint_gradient(u0t, torch.zeros_like(u0t), 2.0 / n, maxit, dts=dts)
+    ref = ref[0].numpy()
+    assert np.max(np.abs(grad - ref)) / np.max(np.abs(ref)) < 1.0e-9
+
+
+@pytest.mark.parametrize("stride", [None, 1, 7])
+def test_batched_checkpointed_gradient_matches_autograd(stride):
+    """Uneven batch, sqrt(n) checkpoints (and the extremes stride 1, 7),
+    J = 1/2 sum (u(T) - u_target)^2 per instance."""
+    from pyshocks_gb300.adjoint import CheckpointedSolve
+    from pyshocks_gb300.batched import BatchedSolver
+
+    sizes = [64, 50, 1024, 333]
+    nsteps = 23
+    rng = np.random.default_rng(4)
+    u0 = [R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes]
+    tgt = [R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes]
+    solver = BatchedSolver(_scheme(), sizes, [2.0 / n for n in sizes], theta=0.9, max_steps=nsteps)
+    cs = CheckpointedSolve(solver, nsteps, stride=stride)
+    uT = cs.forward(torch.tensor(np.concatenate(u0)))
+    tg = torch.tensor(np.concatenate(tgt), device="cuda")
+    grad = cs.backward(uT - tg).cpu().numpy()
+    hist = solver.dt_history().cpu()
+    for b, n in enumerate(sizes):
+        ref, _, _ = T.adjoint_gradient(torch.tensor(u0[b])[None], torch.tensor(tgt[b])[None],
+                                       2.0 / n, nsteps, dts=hist[:, b].reshape(-1, 1))
+        ref = ref[0].numpy()
+        got = grad[int(solver.offsets[b]):int(solver.offsets[b + 1])]
+        assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 1.0e-9, b
+
+
+def test_gradient_against_central_differences():
+    """dJ/du0 . v against (J(u0 + h v) - J(u0 - h v)) / 2h, h = 1e-6, with the dt
+    sequence of the unperturbed run frozen (the reference's convention)."""
+    from pyshocks_gb300.adjoint import CheckpointedSolve
+    from pyshocks_gb300.batched import BatchedSolver
+
+    n, nsteps, B = 256, 40, 2
+    rng = np.random.default_rng(8)
+    u0 = np.concatenate([R.exact_cell_average_sine(R.make_uniform_cell_grid(-1, 1, n, 3))[3:-3]
+                         for _ in range(B)])
+    tgt = u0 + 0.05 * rng.standard_normal(u0.size)
+    solver = BatchedSolver(_scheme(), [n] * B, 2.0 / n, max_steps=nsteps)
+    cs = CheckpointedSolve(solver, nsteps)
+    uT = cs.forward(torch.tensor(u0))
+    tg = torch.tensor(tgt, device="cuda")
+    grad = cs.backward(uT - tg).cpu().numpy()
+    dts = solver.dt_history().cpu()
+    h = 1.0e-6
+    for k in range(4):
+        v = rng.standard_normal(u0.size)
+        js = []
+        for sgn in (+1, -1):
+            up = torch.tensor(u0 + sgn * h * v)
+            J = 0.0
+            for b in range(B):
+                sl = slice(b * n, (b + 1) * n)
+                out, _ = T.forward(up[sl][None], 2.0 / n, nsteps, dts=dts[:, b].reshape(-1, 1))
+                J += 0.5 * float(torch.sum((out[0] - torch.tensor(tgt[sl])) ** 2))
+            js.append(J)
+        fd = (js[0] - js[1]) / (2 * h)
+        ad = float(np.dot(grad, v))
+        assert abs(fd - ad) <= 1.0e-5 * max(1.0, abs(ad)), (k, fd, ad)
+
+
+def test_autograd_function_backward():
+    """``adjoint.solve`` inside a torch graph: loss.backward() runs the kernel."""
+    from pyshocks_gb300 import adjoint
+    from pyshocks_gb300.batched import BatchedSolver
+
+    n, nsteps = 128, 12
+    u0 = torch.tensor(R.exact_cell_average_sine(R.make_uniform_cell_grid(-1, 1, n, 3))[3:-3],
+                      device="cuda", requires_grad=True)
+    solver = BatchedSolver(_scheme(), [n], 2.0 / n, max_steps=nsteps)
+    cs = adjoint.CheckpointedSolve(solver, nsteps)
+    uT = adjoint.solve(u0, cs)
+    loss = 0.5 * torch.sum(uT**2)
+    loss.backward()
+    ref, _, _ = T.adjoint_gradient(u0.detach().cpu()[None], torch.zeros(1, n, dtype=torch.float64),
+                                   2.0 / n, nsteps, dts=solver.dt_history().cpu())
+    err = (u0.grad.cpu() - ref[0]).abs().max() / ref.abs().max()
+    assert float(err) < 1.0e-9
