@@ -373,6 +373,11 @@ def bench_gpu(args, rank: int, world: int) -> None:
         fp64 = {"peak": fp64_peak / 1e12, "unit": "TFLOP/s",
                 "peak_source": "shk_measure_fp_peak FMA chains on this GPU (of measured)"}
 
+    extra = None
+    if rank == 0 and not args.profile and not args.no_extra:
+        extra = {"fp32_forward": bench_fp32(scheme, sizes, u0, stream, args),
+                 "adjoint": bench_adjoint(scheme, dev, args)}
+
     cpu = None
     if rank == 0 and not args.no_cpu and not args.profile:
         rate, used = run_cpu_sample(sizes, params, n_inst=args.cpu_instances, nsteps=1)
@@ -404,8 +409,69 @@ def bench_gpu(args, rank: int, world: int) -> None:
                          "algo_bytes_per_launch": algo_bytes, "peak_source": peak_src},
             "fp64_pipe": fp64,
             "cpu_baseline": cpu,
+            "extra": extra,
         }
         print(json.dumps(line), flush=True)
+
+
+def bench_fp32(scheme, sizes, u0, stream, args) -> dict:
+    """Same batch and steps with float32 state (FP64 dt and reductions)."""
+    import torch
+
+    from pyshocks_gb300.batched import BatchedSolver
+
+    s32 = BatchedSolver(scheme, sizes, 2.0 / sizes.astype(np.float64), dtype=torch.float32)
+    k = args.steps + (args.steps % 2)
+    with torch.cuda.stream(stream):
+        s32.reset(u0)
+        s32.step(4, graph=True)
+        stream.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s32.step(k, graph=True)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    cells = int(np.sum(sizes))
+    rate = cells * k / (ms * 1e-3)
+    return {"metric": "WENO5 cell-steps/s (float32 state)", "value": rate, "unit": "cell-steps/s",
+            "ms_per_step": ms / k, "algo_gb_per_s": 8 * rate / 1e9}
+
+
+def bench_adjoint(scheme, dev, args) -> dict:
+    """The adjoint configuration: B=256 Burgers instances, N=4096, config-1 initial
+    condition, J = 1/2 |u(T) - u_target|^2, sqrt(n)-checkpointed reverse sweep,
+    float64. One gradient = one instance's full dJ/du0."""
+    import torch
+
+    from pyshocks_gb300.adjoint import CheckpointedSolve
+    from pyshocks_gb300.batched import BatchedSolver
+
+    n, B, nsteps = 4096, 256, args.adjoint_steps
+    # exact cell averages of 0.5 + sin(pi x) on [-1, 1]
+    f = np.linspace(-1.0, 1.0, n + 1)
+    u1 = 0.5 + (np.cos(np.pi * f[:-1]) - np.cos(np.pi * f[1:])) / (np.pi * (2.0 / n))
+    u0 = torch.tensor(np.tile(u1, B), device=dev)
+    solver = BatchedSolver(scheme, [n] * B, 2.0 / n, max_steps=nsteps)
+    cs = CheckpointedSolve(solver, nsteps)
+    rng = np.random.default_rng(SEED + 3)
+    target = (u0 + 0.05 * torch.tensor(rng.standard_normal(u0.numel()), device=dev)).contiguous()
+    cs.forward(u0)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    uT = cs.forward(u0)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    g = cs.backward(uT - target)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    if solver.status() or not torch.isfinite(g).all():
+        raise RuntimeError("adjoint run failed")
+    return {"metric": "adjoint grads/s", "value": B / (t2 - t0), "unit": "gradients/s",
+            "config": {"batch": B, "n": n, "steps": nsteps, "checkpoint_stride": cs.stride},
+            "forward_s": t1 - t0, "reverse_s": t2 - t1,
+            "adjoint_cell_steps_per_s": n * B * nsteps / (t2 - t1)}
 
 
 def ctypes_fp_peak(L):
@@ -424,6 +490,9 @@ def main() -> None:
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-instances", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the float32 and adjoint measurements")
+    ap.add_argument("--adjoint-steps", type=int, default=4000)
     ap.add_argument("--profile", action="store_true",
                     help="timed region only (no e2e, CPU baseline or FP peak): for ncu")
     args = ap.parse_args()

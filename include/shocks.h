@@ -36,8 +36,9 @@ typedef enum {
 
 /* numerical flux (burgers/schemes.py:98-153,205-256) */
 enum { SHK_FLUX_RUSANOV = 0, SHK_FLUX_LF = 1, SHK_FLUX_ESWENO = 2 };
-/* reconstruction (reconstruction.py:335-348,386-439) */
-enum { SHK_REC_WENOJS53 = 0, SHK_REC_ESWENO32 = 1 };
+/* reconstruction (reconstruction.py:335-348,386-439); SHK_REC_LEARNED: learned
+ * WENO weights (an MLP over the normalised stencil, float32 state only) */
+enum { SHK_REC_WENOJS53 = 0, SHK_REC_ESWENO32 = 1, SHK_REC_LEARNED = 2 };
 /* physical flux f(u) and wave speed f'(u) */
 enum { SHK_EQ_BURGERS = 0, SHK_EQ_ADVECTION = 1, SHK_EQ_LWR = 2 };
 /* state precision */
@@ -55,6 +56,9 @@ typedef struct {
     double delta;      /* ES-WENO delta (bound to dx^2 by burgers bind)       */
     double nu;         /* Rusanov artificial viscosity dx^(alpha-1); 1 if alpha=1 */
     double speed;      /* linear advection velocity (SHK_EQ_ADVECTION)        */
+    const float* mlp;  /* SHK_REC_LEARNED: 1347 float32 parameters (device)    */
+    float tau;         /* SHK_REC_LEARNED: JS weight marking a non-smooth sub-stencil */
+    float band;        /* SHK_REC_LEARNED: max network weight on such sub-stencils */
 } shk_scheme;
 
 const char* shk_strerror(int status);
@@ -200,6 +204,28 @@ int shk_apply_operator_lf_noalloc_f64(const shk_scheme* scheme, const double* u,
                                       double* out, int64_t n, int32_t nghosts, double dx,
                                       void* stream);
 int64_t shk_apply_operator_lf_noalloc_max_cells(void);
+
+/* ---- learned WENO weights: training (no reference counterpart) ---------- */
+
+/* number of MLP parameters (1347) and the workspace a batch of n samples needs */
+int shk_mlp_num_params(void);
+int64_t shk_mlp_workspace_bytes(int64_t n);
+
+/* loss (1/n) sum_i w_i (face_i - target_i)^2 of the raw network over n
+ * stencils (n x 5 float32) and its gradient w.r.t. the parameters (fp32
+ * forward/backward, deterministic reduction). *loss is device memory (double). */
+int shk_mlp_loss_grad_f32(const float* params, const float* stencils, const float* target,
+                          const float* weight, int64_t n, float* grad, double* loss,
+                          void* workspace, int64_t workspace_bytes, void* stream);
+
+/* one Adam step on the parameters (step >= 1 for the bias corrections) */
+int shk_mlp_adam_f32(float* params, const float* grad, float* m, float* v, float lr,
+                     float beta1, float beta2, float eps, int32_t step, void* stream);
+
+/* learned face values of n stencils (n x 5) with the tensor-core inference and
+ * the WENO-JS trust band of the flux kernel (scheme->mlp, eps, tau, band) */
+int shk_learned_faces_f32(const shk_scheme* scheme, const float* stencils, float* out,
+                          int64_t n, void* stream);
 
 /* ---- measurement ------------------------------------------------------- */
 

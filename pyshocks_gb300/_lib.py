@@ -25,7 +25,7 @@ SHK_EUNSUPPORTED = 6
 SHK_ETOOLARGE = 7
 
 SHK_FLUX_RUSANOV, SHK_FLUX_LF, SHK_FLUX_ESWENO = 0, 1, 2
-SHK_REC_WENOJS53, SHK_REC_ESWENO32 = 0, 1
+SHK_REC_WENOJS53, SHK_REC_ESWENO32, SHK_REC_LEARNED = 0, 1, 2
 SHK_EQ_BURGERS, SHK_EQ_ADVECTION, SHK_EQ_LWR = 0, 1, 2
 SHK_F64, SHK_F32 = 0, 1
 
@@ -45,6 +45,9 @@ class ShkScheme(ctypes.Structure):
         ("delta", ctypes.c_double),
         ("nu", ctypes.c_double),
         ("speed", ctypes.c_double),
+        ("mlp", ctypes.c_void_p),
+        ("tau", ctypes.c_float),
+        ("band", ctypes.c_float),
     ]
 
 
@@ -89,6 +92,12 @@ SIGNATURES: dict[str, tuple] = {
     "shk_plan_adjoint": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _P]),
     "shk_apply_operator_lf_noalloc_f64": (ctypes.c_int, [_SCH, _P, _P, _I64, _I32, _D, _P]),
     "shk_apply_operator_lf_noalloc_max_cells": (ctypes.c_int64, []),
+    "shk_mlp_num_params": (ctypes.c_int, []),
+    "shk_mlp_workspace_bytes": (ctypes.c_int64, [_I64]),
+    "shk_mlp_loss_grad_f32": (ctypes.c_int, [_P, _P, _P, _P, _I64, _P, _P, _P, _I64, _P]),
+    "shk_mlp_adam_f32": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_float, ctypes.c_float,
+                                        ctypes.c_float, ctypes.c_float, _I32, _P]),
+    "shk_learned_faces_f32": (ctypes.c_int, [_SCH, _P, _P, _I64, _P]),
     "shk_measure_fp_peak": (ctypes.c_int, [_I32, _I32, ctypes.POINTER(_D)]),
 }
 

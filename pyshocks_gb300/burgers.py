@@ -62,6 +62,10 @@ class GpuConservationLawScheme(ConservationLawScheme):
         s.speed = float(self.speed)
         if s.rec < 0:
             raise NotImplementedError(f"reconstruction {rec.name!r} is not on the GB300 path")
+        if s.rec == L.SHK_REC_LEARNED:
+            from pyshocks_gb300.learned import c_scheme_fields
+
+            c_scheme_fields(rec, s)
         return s
 
 

@@ -120,14 +120,14 @@ __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1
     const T dl = fma(T(6), P2, fma(T(18), P0, m));
     T gR, gL, dR, dL, ie0, ie1, ie2;
     if constexpr (sizeof(T) == 8) {
-        const T r = T(1) / (dr * dl);
+        const T r = rcp_nr(dr * dl);
         const T rl = dl * r, rr = dr * r;  // 1/dr, 1/dl
         gR = urb * rl;
         gL = ulb * rr;
         dR = nr * rl;  // ur - v
         dL = nl * rr;  // ul - v
         const T e01 = e0 * e1;
-        const T q = T(1) / (e01 * e2);
+        const T q = rcp_nr(e01 * e2);
         ie0 = (e1 * e2) * q;
         ie1 = (e0 * e2) * q;
         ie2 = e01 * q;
@@ -416,6 +416,7 @@ OpParams<T> adj_params(const shk_scheme* s) {
     p.hnu = static_cast<T>(0.5 * s->nu);
     p.c = static_cast<T>(s->speed);
     p.hnu_amax = T(0);
+    p.lp = LearnedParams{nullptr, 0.0f, 0.0f, 0.0f};
     return p;
 }
 

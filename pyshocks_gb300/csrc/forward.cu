@@ -309,9 +309,10 @@ int cuda_check(cudaError_t e) {
 bool valid_scheme(const shk_scheme* s) {
     if (!s) return false;
     if (s->flux < 0 || s->flux > SHK_FLUX_ESWENO) return false;
-    if (s->rec < 0 || s->rec > SHK_REC_ESWENO32) return false;
+    if (s->rec < 0 || s->rec > SHK_REC_LEARNED) return false;
     if (s->equation < 0 || s->equation > SHK_EQ_LWR) return false;
     if ((s->flux == SHK_FLUX_ESWENO) != (s->rec == SHK_REC_ESWENO32)) return false;
+    if (s->rec == SHK_REC_LEARNED && (s->flux != SHK_FLUX_RUSANOV || !s->mlp)) return false;
     return true;
 }
 
@@ -323,6 +324,7 @@ OpParams<T> make_params(const shk_scheme* s) {
     p.hnu = static_cast<T>(0.5 * s->nu);
     p.c = static_cast<T>(s->speed);
     p.hnu_amax = T(0);
+    p.lp = LearnedParams{s->mlp, static_cast<float>(s->eps), s->tau, s->band};
     return p;
 }
 
@@ -343,6 +345,10 @@ int dispatch_scheme(const shk_scheme* s, F&& f) {
     switch (s->equation) {
 #define SHK_EQ_CASE(EQ)                                                                 \
     case EQ:                                                                            \
+        if (s->rec == SHK_REC_LEARNED) {                                                \
+            if constexpr (sizeof(T) == 4) return f.template operator()<T, EQ, SHK_REC_LEARNED, SHK_FLUX_RUSANOV>(); \
+            else return SHK_EUNSUPPORTED;                                               \
+        }                                                                               \
         if (s->rec == SHK_REC_ESWENO32) return f.template operator()<T, EQ, SHK_REC_ESWENO32, SHK_FLUX_ESWENO>(); \
         if (s->flux == SHK_FLUX_LF) return f.template operator()<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_LF>(); \
         return f.template operator()<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_RUSANOV>();

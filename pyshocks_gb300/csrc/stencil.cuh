@@ -9,6 +9,7 @@
 #include <cstdint>
 
 #include "device.cuh"
+#include "learned.cuh"
 
 namespace shk {
 
@@ -53,7 +54,45 @@ template <class T>
 struct OpParams {
     T eps, delta, hnu, c;  // WENO eps, ES-WENO delta, nu/2, advection speed
     T hnu_amax;            // LF: nu/2 * global max |f'|
+    LearnedParams lp;      // learned reconstruction (float32 state only)
 };
+
+// learned reconstruction of cells [clo, chi): two faces per cell, 16 faces per
+// warp-level tensor-core evaluation (row 2j: right face of cell clo+j, row
+// 2j+1: left face, mirrored stencil)
+__device__ __forceinline__ void learned_phase(const float* v, int clo, int chi, float* UL, float* UR,
+                                              const LearnedParams& lp) {
+    MlpFrags f;
+    mlp_load_frags(lp.mlp, f);
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int ncell = chi - clo, rows = 2 * ncell;
+    for (int q = warp; q * 16 < rows; q += nw) {
+        const int rg = q * 16 + g, rg8 = rg + 8;
+        const int side = g & 1;  // same parity for rows g and g+8
+        const int cg = clo + min(rg >> 1, ncell - 1), cg8 = clo + min(rg8 >> 1, ncell - 1);
+        float sg[5], sg8[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const int o = side ? 2 - k : k - 2;
+            sg[k] = v[cg + o];
+            sg8[k] = v[cg8 + o];
+        }
+        float xg[5], xg8[5];
+        mlp_normalise(sg, xg);
+        mlp_normalise(sg8, xg8);
+        float zr[3], zs[3];
+        mlp_mma_logits(f, xg, xg8, zr, zs);
+        if (t == 0 && rg < rows) {
+            const float val = learned_face(sg, zr[0], zr[1], zr[2], lp);
+            (side ? UL : UR)[cg] = val;
+        }
+        if (t == 1 && rg8 < rows) {
+            const float val = learned_face(sg8, zs[0], zs[1], zs[2], lp);
+            (side ? UL : UR)[cg8] = val;
+        }
+    }
+}
 
 // ---------------------------------------------------------------------------
 // one evaluation of the numerical fluxes F_j (face j+1/2) for j in [lo-1, hi)
@@ -75,6 +114,7 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
         }
         __syncthreads();
         // phase C: ul, ur of cells [lo-1, hi+1)
+#pragma unroll 2
         for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
             T ul, ur;
             weno53_cell<T>(v[c], sm.H[c - 2], sm.H[c - 1], sm.H[c], sm.H[c + 1], sm.D[c - 1],
@@ -83,6 +123,10 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
             sm.UL[c] = ul;
             sm.UR[c] = ur;
         }
+        __syncthreads();
+    } else if constexpr (REC == SHK_REC_LEARNED) {
+        static_assert(sizeof(T) == 4, "the learned reconstruction runs on float32 states");
+        learned_phase(v, lo - 1, hi + 1, sm.UL, sm.UR, p.lp);
         __syncthreads();
     } else {
         for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
