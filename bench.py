@@ -277,7 +277,14 @@ def bench_gpu(args, rank: int, world: int) -> None:
     rec = gb.reconstruction.make_reconstruction_from_name("wenojs53", eps=EPS)
     scheme = gb.burgers.make_scheme_from_name("rusanov", rec=rec)
     u0 = initial_state(sizes, params, dev)
-    solver = BatchedSolver(scheme, sizes, 2.0 / sizes.astype(np.float64), theta=THETA)
+    if args.scheme == "learned":
+        from pyshocks_gb300 import learned
+
+        lscheme = gb.burgers.Rusanov(rec=learned.LearnedWENO(params=learned.load_default_params()))
+        solver = BatchedSolver(lscheme, sizes, 2.0 / sizes.astype(np.float64), theta=THETA,
+                               dtype=torch.float32)
+    else:
+        solver = BatchedSolver(scheme, sizes, 2.0 / sizes.astype(np.float64), theta=THETA)
     stream = torch.cuda.Stream(device=dev)
     dist = None
     if world > 1:
@@ -493,6 +500,8 @@ def main() -> None:
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the float32 and adjoint measurements")
     ap.add_argument("--adjoint-steps", type=int, default=4000)
+    ap.add_argument("--scheme", choices=["plain", "learned"], default="plain",
+                    help="profiling aid: time the learned-weight float32 step instead")
     ap.add_argument("--profile", action="store_true",
                     help="timed region only (no e2e, CPU baseline or FP peak): for ncu")
     args = ap.parse_args()

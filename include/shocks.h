@@ -59,6 +59,8 @@ typedef struct {
     const float* mlp;  /* SHK_REC_LEARNED: 1347 float32 parameters (device)    */
     float tau;         /* SHK_REC_LEARNED: JS weight marking a non-smooth sub-stencil */
     float band;        /* SHK_REC_LEARNED: max network weight on such sub-stencils */
+    float dev;         /* SHK_REC_LEARNED: max |omega - omega_JS| per sub-stencil   */
+    float reserved2;
 } shk_scheme;
 
 const char* shk_strerror(int status);
@@ -133,6 +135,16 @@ int shk_plan_reset(shk_plan* plan, const void* u, const double* t0, const double
  * copied through unchanged; a non-finite dt sets SHK_ENONFINITE in the status
  * word and freezes that instance. */
 int shk_plan_step(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps, void* stream);
+
+/* prescribe the time steps: step k of instance b takes dt[k * B + b] (dt:
+ * nsteps x B doubles, device or host memory, copied into the plan on
+ * `stream`) instead of the CFL step, as a stepper whose predict_timestep
+ * returns a fixed step (timestepping.py:242-260, predict_timestep_from_maxit /
+ * predict_maxit_from_timestep). A step <= 0, and every step past the table,
+ * leaves the instance unchanged; tfinal is not consulted, so a recorded dt
+ * history (shk_plan_copy_dt_history) replays exactly. nsteps = 0 returns to
+ * CFL steps. Drops a captured step graph. */
+int shk_plan_set_fixed_dt(shk_plan* plan, const double* dt, int32_t nsteps, void* stream);
 
 /* capture two steps (u_a -> u_b -> u_a) into a CUDA graph and replay it
  * nsteps/2 times (nsteps must be even). */
@@ -211,11 +223,12 @@ int64_t shk_apply_operator_lf_noalloc_max_cells(void);
 int shk_mlp_num_params(void);
 int64_t shk_mlp_workspace_bytes(int64_t n);
 
-/* loss (1/n) sum_i w_i (face_i - target_i)^2 of the raw network over n
- * stencils (n x 5 float32) and its gradient w.r.t. the parameters (fp32
- * forward/backward, deterministic reduction). *loss is device memory (double). */
+/* loss (1/n) sum_i [w_i (face_i - target_i)^2 + reg |omega_i - d|^2] of the raw
+ * network over n stencils (n x 5 float32; d the WENO-JS5 ideal weights) and its
+ * gradient w.r.t. the parameters (fp32 forward/backward, deterministic
+ * reduction). *loss is device memory (double). */
 int shk_mlp_loss_grad_f32(const float* params, const float* stencils, const float* target,
-                          const float* weight, int64_t n, float* grad, double* loss,
+                          const float* weight, int64_t n, float reg, float* grad, double* loss,
                           void* workspace, int64_t workspace_bytes, void* stream);
 
 /* one Adam step on the parameters (step >= 1 for the bias corrections) */

@@ -11,7 +11,8 @@ of a face to the three nonlinear weights of the WENO-JS5 sub-stencils
 ``sum_k omega_k uhat_k`` of the sub-stencil values, so the flux stays
 conservative. Where the network puts more than ``band`` of its weight on
 sub-stencils that WENO-JS marks as crossing a discontinuity (JS weight below
-``tau``), the plain WENO-JS weights are used instead (per face).
+``tau``), or moves any weight more than ``dev`` from the JS weight, the plain
+WENO-JS weights are used instead (per face).
 
 Parameter vector (1347 float32): W1[32,5], b1[32], W2[32,32], b2[32],
 W3[3,32], b3[3], row-major.
@@ -52,15 +53,14 @@ def normalise(s: torch.Tensor) -> torch.Tensor:
 
 
 def mlp_weights(params, s, *, bf16: bool = False):
-    """Softmax weights of stencils ``s[..., 5]``. With ``bf16`` the inputs,
-    weights and hidden activations are rounded to bfloat16 (FP32
-    accumulation), as in the tensor-core inference kernel."""
+    """Softmax weights of stencils ``s[..., 5]``. With ``bf16`` the inputs and
+    weights are rounded to bfloat16 (FP32 accumulation) and each hidden layer
+    applies tanh to the bfloat16-rounded pre-activation with a bfloat16 result,
+    as the tensor-core inference kernel does (tanh.approx.bf16x2)."""
     W1, b1, W2, b2, W3, b3 = unpack(params)
     x = _bf16(normalise(s), bf16)
-    h1 = torch.tanh(x @ _bf16(W1, bf16).T + _bf16(b1, bf16))
-    h1 = _bf16(h1, bf16)
-    h2 = torch.tanh(h1 @ _bf16(W2, bf16).T + b2)
-    h2 = _bf16(h2, bf16)
+    h1 = _bf16(torch.tanh(_bf16(x @ _bf16(W1, bf16).T + _bf16(b1, bf16), bf16)), bf16)
+    h2 = _bf16(torch.tanh(_bf16(h1 @ _bf16(W2, bf16).T + b2, bf16)), bf16)
     z = h2 @ _bf16(W3, bf16).T + b3
     return torch.softmax(z, dim=-1)
 
@@ -85,13 +85,13 @@ def js_weights(s: torch.Tensor, eps: float) -> torch.Tensor:
     return a / a.sum(dim=-1, keepdim=True)
 
 
-def face_value(params, s, *, eps: float, tau: float, band: float, bf16: bool = False,
-               return_fallback: bool = False):
+def face_value(params, s, *, eps: float, tau: float, band: float, dev: float = 0.5,
+               bf16: bool = False, return_fallback: bool = False):
     """Learned face value of stencils ``s[..., 5]`` with the WENO-JS fallback."""
     w = mlp_weights(params, s, bf16=bf16)
     wjs = js_weights(s, eps)
     excess = torch.sum(w * (wjs < tau).to(w.dtype), dim=-1)
-    fb = excess > band
+    fb = (excess > band) | (torch.amax(torch.abs(w - wjs), dim=-1) > dev)
     w = torch.where(fb[..., None], wjs, w)
     v = torch.sum(w * substencils(s), dim=-1)
     return (v, fb) if return_fallback else v
@@ -111,16 +111,19 @@ def stencils_periodic(u: torch.Tensor):
 def learned_recon(u: torch.Tensor, weights: dict, eps: float):
     """``(ul, ur)`` of every cell for the torch oracle's ``face_flux``."""
     sl, sr = stencils_periodic(u)
-    kw = dict(eps=eps, tau=weights["tau"], band=weights["band"], bf16=weights.get("bf16", False))
+    kw = dict(eps=eps, tau=weights["tau"], band=weights["band"], dev=weights.get("dev", 0.5),
+              bf16=weights.get("bf16", False))
     return face_value(weights["params"], sl, **kw), face_value(weights["params"], sr, **kw)
 
 
-def training_loss(params, s, target, weight):
-    """Weighted squared face-value error of the raw network (no fallback):
-    ``sum_i w_i (sum_k omega_k uhat_k - target_i)^2 / n``."""
+def training_loss(params, s, target, weight, reg: float = 0.0):
+    """Weighted squared face-value error of the raw network (no fallback) plus
+    the pull toward the ideal weights:
+    ``sum_i [w_i (sum_k omega_k uhat_k - target_i)^2 + reg |omega_i - d|^2] / n``."""
     w = mlp_weights(params, s)
     v = torch.sum(w * substencils(s), dim=-1)
-    return torch.sum(weight * (v - target) ** 2) / s.shape[0]
+    d = torch.tensor(_D53, dtype=w.dtype)
+    return (torch.sum(weight * (v - target) ** 2) + reg * torch.sum((w - d) ** 2)) / s.shape[0]
 
 
 def init_params(seed: int = 0, dtype=torch.float32) -> torch.Tensor:

@@ -22,6 +22,23 @@ from pyshocks_gb300 import _lib as L
 _DTYPES = {torch.float64: L.SHK_F64, torch.float32: L.SHK_F32}
 
 
+def partition_instances(sizes: Sequence[int], world: int, work_per_cell: Sequence[float] | None = None):
+    """Longest-processing-time assignment of independent instances to *world*
+    ranks (instances never couple, so ranks need no data-path collective).
+    Returns one sorted index array per rank; the cost of an instance is its
+    cell count (times *work_per_cell*, e.g. its step count, when given)."""
+    sizes = np.asarray(sizes, dtype=np.float64)
+    cost = sizes * (np.asarray(work_per_cell, dtype=np.float64) if work_per_cell is not None else 1.0)
+    order = np.argsort(-cost, kind="stable")
+    load = np.zeros(world)
+    parts: list[list[int]] = [[] for _ in range(world)]
+    for i in order:
+        r = int(np.argmin(load))
+        parts[r].append(int(i))
+        load[r] += cost[i]
+    return [np.array(sorted(p), dtype=np.int64) for p in parts]
+
+
 def pack_offsets(sizes: Sequence[int]) -> np.ndarray:
     """``offsets[B+1]`` of a contiguous packing of instances of *sizes* cells."""
     off = np.zeros(len(sizes) + 1, dtype=np.int64)
@@ -151,6 +168,35 @@ class BatchedSolver:
             "plan_reset",
         )
         self._keep = (t0d, tfd)
+
+    def set_fixed_dt(self, dt=None, nsteps: int | None = None) -> None:
+        """Prescribe the time steps instead of the CFL step.
+
+        *dt* is a ``(nsteps, B)`` table (e.g. a recorded :meth:`dt_history`,
+        replayed exactly), a ``(nsteps,)`` sequence shared by all instances, or
+        a scalar repeated *nsteps* times (the fixed step of
+        :func:`~pyshocks_gb300.timestepping.predict_timestep_from_maxit`).
+        Steps past the table, and steps ``<= 0``, leave an instance unchanged;
+        the final time is not consulted. ``None`` returns to CFL steps.
+        """
+        if dt is None:
+            L.check(self.lib.shk_plan_set_fixed_dt(self._plan, None, 0, L.stream_handle()),
+                    "plan_set_fixed_dt")
+            self._dt_fixed = None
+            return
+        t = torch.as_tensor(dt, dtype=torch.float64, device=self.device)
+        if t.ndim == 0:
+            if nsteps is None:
+                raise ValueError("a scalar step needs nsteps")
+            t = t.expand(int(nsteps), self.B)
+        elif t.ndim == 1:
+            t = t[:, None].expand(t.shape[0], self.B)
+        if t.ndim != 2 or t.shape[1] != self.B:
+            raise ValueError(f"expected a (nsteps, {self.B}) table, got {tuple(t.shape)}")
+        t = t.contiguous()
+        L.check(self.lib.shk_plan_set_fixed_dt(self._plan, t.data_ptr(), int(t.shape[0]),
+                                               L.stream_handle()), "plan_set_fixed_dt")
+        self._dt_fixed = t  # kept alive until the stream-ordered copy has run
 
     def step(self, nsteps: int = 1, *, graph: bool = False) -> torch.Tensor:
         """Advance all active instances by *nsteps* SSPRK33 steps."""

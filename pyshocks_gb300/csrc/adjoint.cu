@@ -46,12 +46,17 @@ struct AdjSmem {
     T *GL, *GR, *GA;
     T *T0, *T1, *T2, *T3, *T4;
 
-    __host__ static size_t host_bytes(int W) { return size_t(kAdjArrays) * W * sizeof(T); }
+    float* Wr;  // learned reconstruction: bf16-rounded parameters
+
+    __host__ static size_t host_bytes(int W) {
+        return size_t(kAdjArrays) * W * sizeof(T) + sizeof(float) * ((kMlpParams + 3) & ~3);
+    }
     __device__ void carve(unsigned char* base, int W) {
         T* p = reinterpret_cast<T*>(base);
         T** slots[kAdjArrays] = {&U, &K1, &K2, &PB, &CB, &Z, &ACC, &H, &D, &Q,
                                  &UL, &UR, &GL, &GR, &GA, &T0, &T1, &T2, &T3, &T4};
         for (int i = 0; i < kAdjArrays; ++i) *slots[i] = p + size_t(i) * W;
+        Wr = reinterpret_cast<float*>(p + size_t(kAdjArrays) * W);
     }
     // forward-stage view (face_fluxes writes the face fluxes into D)
     __device__ Smem<T> fwd(T* state_out) const {
@@ -173,26 +178,31 @@ __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1
 
 // z_i = dt (J_L(v)^T w)_i for i in [lo, hi); v valid on [lo-6, hi+6), w on
 // [lo-3, hi+3). Rusanov flux, WENO-JS5 reconstruction.
-template <class T, int EQ>
+template <class T, int EQ, int REC>
 __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const AdjSmem<T>& a,
                           const OpParams<T>& p, T dtdx) {
     const int tid = threadIdx.x, nt = blockDim.x;
-    for (int c = lo - 5 + tid; c < hi + 4; c += nt) a.H[c] = T(0.5) * (v[c + 1] - v[c]);
-    __syncthreads();
-    for (int c = lo - 4 + tid; c < hi + 4; c += nt) {
-        const T d = a.H[c] - a.H[c - 1];
-        a.D[c] = d;
-        a.Q[c] = (T(13.0 / 3.0) * d) * d;
+    if constexpr (REC == SHK_REC_LEARNED) {
+        learned_phase<T>(v, lo - 3, hi + 3, a.UL, a.UR, reinterpret_cast<float*>(a.H), p.lp);
+        __syncthreads();
+    } else {
+        for (int c = lo - 5 + tid; c < hi + 4; c += nt) a.H[c] = T(0.5) * (v[c + 1] - v[c]);
+        __syncthreads();
+        for (int c = lo - 4 + tid; c < hi + 4; c += nt) {
+            const T d = a.H[c] - a.H[c - 1];
+            a.D[c] = d;
+            a.Q[c] = (T(13.0 / 3.0) * d) * d;
+        }
+        __syncthreads();
+        for (int c = lo - 3 + tid; c < hi + 3; c += nt) {
+            T ul, ur;
+            weno53_cell<T>(v[c], a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
+                           a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, ul, ur);
+            a.UL[c] = ul;
+            a.UR[c] = ur;
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    for (int c = lo - 3 + tid; c < hi + 3; c += nt) {
-        T ul, ur;
-        weno53_cell<T>(v[c], a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
-                       a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, ul, ur);
-        a.UL[c] = ul;
-        a.UR[c] = ur;
-    }
-    __syncthreads();
     // face j+1/2: F = 1/2 (f(L) + f(R)) - nu/2 a (L - R), L = ul_{j+1}, R = ur_j
     for (int j = lo - 3 + tid; j < hi + 2; j += nt) {
         const T fb = (w[j + 1] - w[j]) * dtdx;
@@ -205,9 +215,25 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
     __syncthreads();
     for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
         T t0, t1, t2, t3, t4;
-        weno53_cell_vjp<T>(a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
-                           a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, a.GR[c],
-                           a.GL[c - 1], t0, t1, t2, t3, t4);
+        if constexpr (REC == SHK_REC_LEARNED) {
+            // right face: stencil v_{c-2..c+2}; left face: mirrored v_{c+2..c-2};
+            // relative to v_c from the float cell differences, as the forward
+            // (learned_phase left them in H)
+            const float* db = reinterpret_cast<const float*>(a.H);
+            const float dm2 = db[c - 2], dm1 = db[c - 1], d0 = db[c], dp1 = db[c + 1];
+            const float lo2 = -(dm1 + dm2), lo1 = -dm1, hi1 = d0, hi2 = d0 + dp1;
+            float sR[5] = {lo2, lo1, 0.0f, hi1, hi2};
+            float sL[5] = {hi2, hi1, 0.0f, lo1, lo2};
+            float dR[5], dL[5];
+            learned_face_vjp(sR, a.GR[c], a.Wr, p.lp, dR);
+            learned_face_vjp(sL, a.GL[c - 1], a.Wr, p.lp, dL);
+            t0 = dR[0] + dL[4]; t1 = dR[1] + dL[3]; t2 = dR[2] + dL[2];
+            t3 = dR[3] + dL[1]; t4 = dR[4] + dL[0];
+        } else {
+            weno53_cell_vjp<T>(a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
+                               a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, a.GR[c],
+                               a.GL[c - 1], t0, t1, t2, t3, t4);
+        }
         a.T0[c] = t0; a.T1[c] = t1; a.T2[c] = t2; a.T3[c] = t3; a.T4[c] = t4;
     }
     __syncthreads();
@@ -223,22 +249,23 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
 
 // one adjoint step of a tile: p_out[s, s+te) from u_m (window, halo 20) and
 // p_next (window, halo 10/12). gout points at p_out + s.
-template <class T, int EQ>
+template <class T, int EQ, int REC>
 __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const OpParams<T>& p) {
     constexpr int HU = adj_uhalo<T>();
     const int tid = threadIdx.x, nt = blockDim.x;
+    const T fdt = dtdx * p.fscale;  // face fluxes are stored as F / fscale
     // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12)
     {
         const int lo = HU - 15, hi = HU + te + 15;
-        face_fluxes<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_RUSANOV>(a.U, lo, hi, a.fwd(a.K1), p);
-        for (int i = lo + tid; i < hi; i += nt) a.K1[i] = fma(dtdx, a.D[i - 1] - a.D[i], a.U[i]);
+        face_fluxes<T, EQ, REC, SHK_FLUX_RUSANOV>(a.U, lo, hi, a.fwd(a.K1), p);
+        for (int i = lo + tid; i < hi; i += nt) a.K1[i] = fma(fdt, a.D[i - 1] - a.D[i], a.U[i]);
         __syncthreads();
     }
     {
         const int lo = HU - 12, hi = HU + te + 12;
-        face_fluxes<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_RUSANOV>(a.K1, lo, hi, a.fwd(a.K2), p);
+        face_fluxes<T, EQ, REC, SHK_FLUX_RUSANOV>(a.K1, lo, hi, a.fwd(a.K2), p);
         for (int i = lo + tid; i < hi; i += nt) {
-            const T k = fma(dtdx, a.D[i - 1] - a.D[i], a.K1[i]);
+            const T k = fma(fdt, a.D[i - 1] - a.D[i], a.K1[i]);
             a.K2[i] = fma(T(1.0 / 4.0), k, T(3.0 / 4.0) * a.U[i]);
         }
         __syncthreads();
@@ -246,7 +273,7 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     // reverse stage 3: k2b = 2/3 (p + dt J(k2)^T p) on [HU-6, HU+te+6)
     {
         const int lo = HU - 6, hi = HU + te + 6;
-        vjp_stage<T, EQ>(a.K2, a.PB, a.Z, lo, hi, a, p, dtdx);
+        vjp_stage<T, EQ, REC>(a.K2, a.PB, a.Z, lo, hi, a, p, dtdx);
         for (int i = lo + tid; i < hi; i += nt) a.CB[i] = T(2.0 / 3.0) * (a.PB[i] + a.Z[i]);
         __syncthreads();
         for (int i = HU + tid; i < HU + te; i += nt)
@@ -256,14 +283,14 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     // reverse stage 2: k1b = 1/4 (k2b + dt J(k1)^T k2b) on [HU-3, HU+te+3)
     {
         const int lo = HU - 3, hi = HU + te + 3;
-        vjp_stage<T, EQ>(a.K1, a.CB, a.Z, lo, hi, a, p, dtdx);
+        vjp_stage<T, EQ, REC>(a.K1, a.CB, a.Z, lo, hi, a, p, dtdx);
         for (int i = lo + tid; i < hi; i += nt) a.CB[i] = T(1.0 / 4.0) * (a.CB[i] + a.Z[i]);
         __syncthreads();
     }
     // reverse stage 1: ub = 1/3 p + 3/4 k2b + k1b + dt J(u)^T k1b on the tile
     {
         const int lo = HU, hi = HU + te;
-        vjp_stage<T, EQ>(a.U, a.CB, a.Z, lo, hi, a, p, dtdx);
+        vjp_stage<T, EQ, REC>(a.U, a.CB, a.Z, lo, hi, a, p, dtdx);
         for (int i = lo + tid; i < hi; i += nt) gout[i - HU] = a.ACC[i] + (a.CB[i] + a.Z[i]);
     }
 }
@@ -277,7 +304,7 @@ __device__ __forceinline__ bool adjoint_load(const AdjSmem<T>& a, const T* um, c
     return load_window<T>(a.PB + (HU - HP), pn, n, s0 - HP, te + 2 * HP, bar, phase);
 }
 
-template <class T, int EQ>
+template <class T, int EQ, int REC>
 __global__ void __launch_bounds__(kThreads) batched_adjoint_kernel(PlanDev P, const T* __restrict__ um,
                                                                    const T* __restrict__ pnext,
                                                                    T* __restrict__ pout,
@@ -287,6 +314,7 @@ __global__ void __launch_bounds__(kThreads) batched_adjoint_kernel(PlanDev P, co
     __shared__ __align__(8) uint64_t bar;
     AdjSmem<T> a;
     a.carve(smem_raw, P.tile + 2 * adj_uhalo<T>());
+    if constexpr (REC == SHK_REC_LEARNED) learned_stage_params(p.lp.mlp, a.Wr);
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_mbar_init();
@@ -310,14 +338,14 @@ __global__ void __launch_bounds__(kThreads) batched_adjoint_kernel(PlanDev P, co
             return;
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
-        adjoint_tile<T, EQ>(a, pout + off + s0, te, dtdx, p);
+        adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p);
         __syncthreads();
     }
 }
 
 // forward step with a recorded dt (no CFL, no time update): recompute of the
 // states between checkpoints
-template <class T, int EQ>
+template <class T, int EQ, int REC>
 __global__ void __launch_bounds__(kThreads) replay_step_kernel(PlanDev P, const T* __restrict__ uin,
                                                                T* __restrict__ uout,
                                                                const double* __restrict__ dt_row,
@@ -350,7 +378,7 @@ __global__ void __launch_bounds__(kThreads) replay_step_kernel(PlanDev P, const 
             return;
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
-        step_tile<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_RUSANOV>(sm, uout + off + s0, te, dtdx, p);
+        step_tile<T, EQ, REC, SHK_FLUX_RUSANOV>(sm, uout + off + s0, te, dtdx, p);
         __syncthreads();
     }
 }
@@ -377,7 +405,7 @@ __global__ void __launch_bounds__(kThreads) single_vjp_kernel(const T* __restric
         if (threadIdx.x == 0 && err) atomicOr(err, ERR_TIMEOUT);
         return;
     }
-    adjoint_tile<T, EQ>(a, pout + g + s0, te, dtdx, p);
+    adjoint_tile<T, EQ, SHK_REC_WENOJS53>(a, pout + g + s0, te, dtdx, p);
     // ghost cotangents are zero (interior-only adjoint)
     if (blockIdx.x == 0)
         for (int i = threadIdx.x; i < g; i += blockDim.x) {
@@ -416,31 +444,46 @@ OpParams<T> adj_params(const shk_scheme* s) {
     p.hnu = static_cast<T>(0.5 * s->nu);
     p.c = static_cast<T>(s->speed);
     p.hnu_amax = T(0);
-    p.lp = LearnedParams{nullptr, 0.0f, 0.0f, 0.0f};
+    p.lp = LearnedParams{s->mlp, static_cast<float>(s->eps), s->tau, s->band, s->dev};
+    p.fscale = (sizeof(T) == 8 && s->flux == SHK_FLUX_RUSANOV && s->rec == SHK_REC_WENOJS53 &&
+                s->equation == SHK_EQ_BURGERS && s->nu == 1.0) ? T(0.25) : T(1);
     return p;
 }
 
 bool adjoint_supported(const shk_scheme* s) {
-    return s && s->flux == SHK_FLUX_RUSANOV && s->rec == SHK_REC_WENOJS53 && s->equation >= 0 &&
-           s->equation <= SHK_EQ_LWR;
+    return s && s->flux == SHK_FLUX_RUSANOV &&
+           (s->rec == SHK_REC_WENOJS53 || (s->rec == SHK_REC_LEARNED && s->mlp)) &&
+           s->equation >= 0 && s->equation <= SHK_EQ_LWR;
+}
+
+template <class T, int REC, class F>
+int by_equation_rec(int eq, F&& f) {
+    switch (eq) {
+        case SHK_EQ_BURGERS: return f.template operator()<T, SHK_EQ_BURGERS, REC>();
+        case SHK_EQ_ADVECTION: return f.template operator()<T, SHK_EQ_ADVECTION, REC>();
+        case SHK_EQ_LWR: return f.template operator()<T, SHK_EQ_LWR, REC>();
+    }
+    return SHK_EINVAL;
+}
+
+// WENO-JS53 for both precisions, the learned reconstruction for float32 states
+template <class T, class F>
+int by_scheme(const shk_scheme& sch, F&& f) {
+    if (sch.rec == SHK_REC_LEARNED) return by_equation_rec<T, SHK_REC_LEARNED>(sch.equation, f);
+    return by_equation_rec<T, SHK_REC_WENOJS53>(sch.equation, f);
 }
 
 template <class T, class F>
 int by_equation(int eq, F&& f) {
-    switch (eq) {
-        case SHK_EQ_BURGERS: return f.template operator()<T, SHK_EQ_BURGERS>();
-        case SHK_EQ_ADVECTION: return f.template operator()<T, SHK_EQ_ADVECTION>();
-        case SHK_EQ_LWR: return f.template operator()<T, SHK_EQ_LWR>();
-    }
-    return SHK_EINVAL;
+    return by_equation_rec<T, SHK_REC_WENOJS53>(eq, f);
 }
 
 template <class TS>
 struct AdjLaunch {
     PlanDev D; const void* um; const void* pn; void* po; const double* dt_row; OpParams<TS> p;
     size_t smem; int grid; cudaStream_t st;
-    template <class T, int EQ> int operator()() {
-        auto k = batched_adjoint_kernel<T, EQ>;
+    template <class T, int EQ, int REC> int operator()() {
+        auto k = batched_adjoint_kernel<T, EQ, REC>;
         ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(um), static_cast<const T*>(pn),
                                          static_cast<T*>(po), dt_row, p);
@@ -452,8 +495,8 @@ template <class TS>
 struct ReplayLaunch {
     PlanDev D; const void* uin; void* uout; const double* dt_row; OpParams<TS> p;
     size_t smem; int grid; cudaStream_t st;
-    template <class T, int EQ> int operator()() {
-        auto k = replay_step_kernel<T, EQ>;
+    template <class T, int EQ, int REC> int operator()() {
+        auto k = replay_step_kernel<T, EQ, REC>;
         ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(uin), static_cast<T*>(uout), dt_row, p);
         return acuda(cudaGetLastError());
@@ -463,7 +506,7 @@ struct ReplayLaunch {
 struct SingleVjpLaunch {
     const double* u; const double* pn; double* po; int64_t n; int g; int tile; double dtdx;
     OpParams<double> p; size_t smem; int blocks; cudaStream_t st;
-    template <class T, int EQ> int operator()() {
+    template <class T, int EQ, int REC> int operator()() {
         auto k = single_vjp_kernel<T, EQ>;
         ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<blocks, kThreads, smem, st>>>(u, pn, po, n, g, tile, dtdx, p, nullptr);
@@ -478,7 +521,7 @@ extern "C" {
 int shk_ssprk33_vjp_f64(const shk_scheme* scheme, const double* u, const double* p_next,
                         double* p_out, int64_t n, int32_t nghosts, double dx, double dt,
                         void* stream) {
-    if (!adjoint_supported(scheme) || !u || !p_next || !p_out || n < 3 || nghosts < 3 ||
+    if (!adjoint_supported(scheme) || scheme->rec != SHK_REC_WENOJS53 || !u || !p_next || !p_out || n < 3 || nghosts < 3 ||
         !(dx > 0) || !(dt >= 0))
         return SHK_EINVAL;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
@@ -556,10 +599,10 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
             const double* row = D.dt_hist + size_t(base + j - 1) * D.B;
             if (dtype == SHK_F64) {
                 ReplayLaunch<double> f{D, seg_at(j - 1), seg_at(j), row, adj_params<double>(&sch), fsmem, grid, st};
-                r = by_equation<double>(sch.equation, f);
+                r = by_scheme<double>(sch, f);
             } else {
                 ReplayLaunch<float> f{D, seg_at(j - 1), seg_at(j), row, adj_params<float>(&sch), fsmem, grid, st};
-                r = by_equation<float>(sch.equation, f);
+                r = by_scheme<float>(sch, f);
             }
             if (r != SHK_OK) return r;
         }
@@ -567,10 +610,10 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
             const double* row = D.dt_hist + size_t(base + j) * D.B;
             if (dtype == SHK_F64) {
                 AdjLaunch<double> f{D, seg_at(j), cur, nxt, row, adj_params<double>(&sch), asmem, agrid, st};
-                r = by_equation<double>(sch.equation, f);
+                r = by_scheme<double>(sch, f);
             } else {
                 AdjLaunch<float> f{D, seg_at(j), cur, nxt, row, adj_params<float>(&sch), asmem, agrid, st};
-                r = by_equation<float>(sch.equation, f);
+                r = by_scheme<float>(sch, f);
             }
             if (r != SHK_OK) return r;
             std::swap(cur, nxt);

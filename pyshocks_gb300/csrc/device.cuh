@@ -154,6 +154,47 @@ __device__ __forceinline__ void weno53_cell(T v, T Hm2, T Hm1, T H0, T Hp1, T Dm
     }
 }
 
+// Forward-path variant of weno53_cell on unscaled differences (fewer FP64
+// instructions): d_k = v_{k+1} - v_k, E_k = d_k - d_{k-1}, G_k = 13/3 E_k^2, and
+// 4 beta_j = G + h'^2 with h'_0 = E_{c-1} + 2 d_{c-1}, h'_1 = d_c + d_{c-1},
+// h'_2 = E_{c+1} - 2 d_c. With eps4 = 4 eps every s_j and P_j is scaled by a
+// common power of two, which cancels in the normalised weights. The
+// corrections 6 (uhat_k - v) (weights (1, 6, 3) folded as in weno53_cell) use
+// d_{c-2} = 3 d_{c-1} - h'_0 and d_{c+1} = h'_2 + 3 d_c:
+//   cr0 = 2 h'_0 - d_{c-1}      cr1 = 6 d_{c-1} + 12 d_c     cr2 = 3 (d_c - h'_2)
+//   cl0 = 2 h'_2 + d_c          cl1 = 6 E_c - cr1            cl2 = -3 (h'_0 + d_{c-1})
+__device__ __forceinline__ void weno53_cell_d(double v, double dm1, double d0, double Em1,
+                                              double E0, double Ep1, double Gm1, double G0,
+                                              double Gp1, double eps4, double& ul, double& ur) {
+    const double h0 = fma(2.0, dm1, Em1);
+    const double h1 = d0 + dm1;
+    const double h2 = fma(-2.0, d0, Ep1);
+    double s0 = eps4 + fma(h0, h0, Gm1); s0 = s0 * s0;
+    double s1 = eps4 + fma(h1, h1, G0); s1 = s1 * s1;
+    double s2 = eps4 + fma(h2, h2, Gp1); s2 = s2 * s2;
+    const double P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
+    const double cr0 = fma(2.0, h0, -dm1);
+    const double cr1 = fma(12.0, d0, 6.0 * dm1);
+    const double cr2 = 3.0 * (d0 - h2);
+    const double cl0 = fma(2.0, h2, d0);
+    const double cl1 = fma(6.0, E0, -cr1);
+    const double cl2 = -3.0 * (h0 + dm1);
+    const double nr = fma(P0, cr0, fma(P1, cr1, P2 * cr2));
+    const double nl = fma(P2, cl0, fma(P1, cl1, P0 * cl2));
+    const double m = 36.0 * P1;
+    const double dr = fma(6.0, P0, fma(18.0, P2, m));
+    const double dl = fma(6.0, P2, fma(18.0, P0, m));
+    const double r = rcp_nr(dr * dl);
+    ur = fma(nr * dl, r, v);
+    ul = fma(nl * dr, r, v);
+}
+
+// 2|x| from the bit pattern of |x| (integer exponent increment, exact for
+// normal numbers; zero and subnormals take the FP path)
+__device__ __forceinline__ double twice_abs_bits(unsigned long long b) {
+    return b >= (1ULL << 52) ? from_bits(b + (1ULL << 52)) : 2.0 * from_bits(b);
+}
+
 // ---- ES-WENO 3/2 reconstruction of one cell (weno.py:284-296) -----------------
 // d = (1/3, 2/3); beta_0 = (v_c - v_{c-1})^2, beta_1 = (v_{c+1} - v_c)^2,
 // tau = (v_{c+1} - 2 v_c + v_{c-1})^2; alpha_k = d_k (1 + tau / (eps + beta_k)).

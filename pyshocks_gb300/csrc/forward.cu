@@ -35,7 +35,7 @@ __device__ void finalize_step(const PlanDev& P, int64_t k) {
     const int cur = static_cast<int>(k & 1);
     for (int b = threadIdx.x; b < P.B; b += blockDim.x) {
         unsigned long long* am = P.amax + size_t(cur) * P.B + b;
-        const DtState s = compute_dt(from_bits(*am), P.cfl[b], P.theta, P.t[b], P.tfinal[b]);
+        const DtState s = plan_dt(P, k, b, from_bits(*am));
         double rec = 0.0;
         if (s.active) {
             if (s.finite) {
@@ -78,8 +78,7 @@ __global__ void __launch_bounds__(kThreads) batched_step_kernel(PlanDev P, const
         const int64_t n = P.offsets[b + 1] - off;
         const int64_t s0 = int64_t(P.item_tile[item]) * P.tile;
         const int te = static_cast<int>(imin64(P.tile, n - s0));
-        const DtState ds =
-            compute_dt(from_bits(P.amax[size_t(cur) * P.B + b]), P.cfl[b], P.theta, P.t[b], P.tfinal[b]);
+        const DtState ds = plan_dt(P, k, b, from_bits(P.amax[size_t(cur) * P.B + b]));
         B mx = 0;
         if (!(ds.active && ds.finite)) {
             // instance finished or frozen: copy the tile through
@@ -221,7 +220,7 @@ __global__ void __launch_bounds__(kThreads) apply_operator_kernel(const T* __res
     for (int i = threadIdx.x; i < te; i += blockDim.x) {
         const int w = HL + i;
         // -(f[1:] - f[:-1]) / dx  (schemes.py:346)
-        const T r = -(sm.D[w] - sm.D[w - 1]) / dx;
+        const T r = -((sm.D[w] - sm.D[w - 1]) * p.fscale) / dx;
         const int64_t gi = s0 + i;
         out[g + gi] = r;
         // ghost cells of the output: periodic image of the interior output
@@ -324,7 +323,10 @@ OpParams<T> make_params(const shk_scheme* s) {
     p.hnu = static_cast<T>(0.5 * s->nu);
     p.c = static_cast<T>(s->speed);
     p.hnu_amax = T(0);
-    p.lp = LearnedParams{s->mlp, static_cast<float>(s->eps), s->tau, s->band};
+    p.lp = LearnedParams{s->mlp, static_cast<float>(s->eps), s->tau, s->band, s->dev};
+    // FP64 Burgers-Rusanov with nu = 1 stores 4 F (see face_fluxes)
+    p.fscale = (sizeof(T) == 8 && s->flux == SHK_FLUX_RUSANOV && s->rec == SHK_REC_WENOJS53 &&
+                s->equation == SHK_EQ_BURGERS && s->nu == 1.0) ? T(0.25) : T(1);
     return p;
 }
 
@@ -345,10 +347,8 @@ int dispatch_scheme(const shk_scheme* s, F&& f) {
     switch (s->equation) {
 #define SHK_EQ_CASE(EQ)                                                                 \
     case EQ:                                                                            \
-        if (s->rec == SHK_REC_LEARNED) {                                                \
-            if constexpr (sizeof(T) == 4) return f.template operator()<T, EQ, SHK_REC_LEARNED, SHK_FLUX_RUSANOV>(); \
-            else return SHK_EUNSUPPORTED;                                               \
-        }                                                                               \
+        if (s->rec == SHK_REC_LEARNED)                                                  \
+            return f.template operator()<T, EQ, SHK_REC_LEARNED, SHK_FLUX_RUSANOV>();   \
         if (s->rec == SHK_REC_ESWENO32) return f.template operator()<T, EQ, SHK_REC_ESWENO32, SHK_FLUX_ESWENO>(); \
         if (s->flux == SHK_FLUX_LF) return f.template operator()<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_LF>(); \
         return f.template operator()<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_RUSANOV>();
@@ -426,6 +426,8 @@ struct shk_plan {
     unsigned int* done = nullptr;
     int32_t* status = nullptr;
     double* partial = nullptr;
+    double* dt_fixed = nullptr;  // prescribed steps [fixed_cap][B], active when fixed_steps > 0
+    int64_t fixed_cap = 0, fixed_steps = 0;
     // host mirror of the number of steps launched since reset
     int64_t host_steps = 0;
     // captured two-step graph
@@ -438,7 +440,8 @@ struct shk_plan {
         P.item_inst = item_inst; P.item_tile = item_tile; P.offsets = offsets; P.cfl = cfl;
         P.inv_dx = inv_dx; P.tfinal = tfinal; P.theta = theta; P.amax = amax; P.t = t;
         P.dt_hist = dt_hist; P.step = step; P.done = done; P.status = status;
-        P.partial = partial; P.B = B; P.nitems = nitems; P.tile = tile; P.max_steps = max_steps;
+        P.partial = partial; P.B = B;
+        P.dt_fixed = fixed_steps > 0 ? dt_fixed : nullptr; P.fixed_steps = fixed_steps; P.nitems = nitems; P.tile = tile; P.max_steps = max_steps;
         return P;
     }
 };
@@ -560,7 +563,7 @@ int shk_plan_destroy(shk_plan* plan) {
     if (plan->graph) cudaGraphExecDestroy(plan->graph);
     void* ptrs[] = {plan->item_inst, plan->item_tile, plan->item_first, plan->offsets, plan->cfl,
                     plan->inv_dx, plan->tfinal, plan->amax, plan->t, plan->dt_hist, plan->step,
-                    plan->done, plan->status, plan->partial};
+                    plan->done, plan->status, plan->partial, plan->dt_fixed};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete plan;
@@ -716,6 +719,30 @@ int shk_plan_step(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps, void* st
                                              : launch_step<float>(plan, in, out, st);
         if (r != SHK_OK) return r;
         plan->host_steps++;
+    }
+    return SHK_OK;
+}
+
+int shk_plan_set_fixed_dt(shk_plan* plan, const double* dt, int32_t nsteps, void* stream) {
+    if (!plan || nsteps < 0 || (nsteps > 0 && !dt)) return SHK_EINVAL;
+    cudaStream_t st = as_stream(stream);
+    if (nsteps > plan->fixed_cap) {
+        SHK_CUDA(cudaStreamSynchronize(st));
+        if (plan->dt_fixed) cudaFree(plan->dt_fixed);
+        plan->dt_fixed = nullptr;
+        plan->fixed_cap = plan->fixed_steps = 0;
+        if (cudaMalloc(&plan->dt_fixed, sizeof(double) * size_t(nsteps) * plan->B) != cudaSuccess)
+            return SHK_ENOMEM;
+        plan->fixed_cap = nsteps;
+    }
+    if (nsteps > 0)
+        SHK_CUDA(cudaMemcpyAsync(plan->dt_fixed, dt, sizeof(double) * size_t(nsteps) * plan->B,
+                                 cudaMemcpyDefault, st));
+    plan->fixed_steps = nsteps;
+    // the kernels take the plan's device view by value: a captured graph is stale now
+    if (plan->graph) {
+        cudaGraphExecDestroy(plan->graph);
+        plan->graph = nullptr;
     }
     return SHK_OK;
 }

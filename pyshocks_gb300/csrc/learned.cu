@@ -2,7 +2,12 @@
 // reconstruction (see learned.cuh for the method).
 //
 // Training loss over a batch of (stencil, target, weight) samples:
-//   L = (1/n) sum_i w_i (sum_k omega_k(x_i) uhat_k(s_i) - target_i)^2
+//   L = (1/n) sum_i [ w_i (sum_k omega_k(x_i) uhat_k(s_i) - target_i)^2
+//                     + reg sum_k (omega_k(x_i) - d_k)^2 ]
+// The second term pulls the weights toward the ideal weights d = (1, 6, 3)/10
+// of WENO-JS5 where the face error does not constrain them (on smooth data
+// every sub-stencil reconstructs well, and an arbitrary choice among them can
+// be unstable in time).
 // with x_i the normalised stencil. The forward and backward passes run one
 // sample per thread in fp32 (exact tanh/exp); per-block gradient sums are
 // formed from the per-sample activations staged in shared memory and written
@@ -23,7 +28,7 @@ constexpr int kStage = kMlpIn + kMlpH + kMlpH + kMlpH + kMlpH + kMlpOut;  // x, 
 
 __global__ void __launch_bounds__(kTrainThreads) mlp_loss_grad_kernel(
     const float* __restrict__ P, const float* __restrict__ stencils, const float* __restrict__ target,
-    const float* __restrict__ weight, int64_t n, float* __restrict__ block_grad,
+    const float* __restrict__ weight, int64_t n, float reg, float* __restrict__ block_grad,
     double* __restrict__ block_loss) {
     extern __shared__ __align__(16) float sm[];
     float* Ps = sm;                              // kMlpParams
@@ -92,10 +97,13 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_loss_grad_kernel(
         if (valid) {
             const float r = v - target[i];
             const float wi = weight[i];
-            lacc += static_cast<double>(wi) * r * r;
-            // dL/dv, dv/domega_k = uhat_k, softmax backward
+            const float g0 = w[0] - 0.1f, g1 = w[1] - 0.6f, g2 = w[2] - 0.3f;
+            lacc += static_cast<double>(wi) * r * r + static_cast<double>(reg) * (g0 * g0 + g1 * g1 + g2 * g2);
+            // dL/dv, dv/domega_k = uhat_k, plus the regulariser; softmax backward
             const float dv = 2.0f * wi * r * invn;
-            const float dw0 = dv * uh[0], dw1 = dv * uh[1], dw2 = dv * uh[2];
+            const float rg = 2.0f * reg * invn;
+            const float dw0 = fmaf(dv, uh[0], rg * g0), dw1 = fmaf(dv, uh[1], rg * g1),
+                        dw2 = fmaf(dv, uh[2], rg * g2);
             const float dot = w[0] * dw0 + w[1] * dw1 + w[2] * dw2;
             dz[0] = w[0] * (dw0 - dot);
             dz[1] = w[1] * (dw1 - dot);
@@ -201,21 +209,19 @@ __global__ void __launch_bounds__(256) learned_faces_kernel(LearnedParams lp, co
     MlpFrags f;
     mlp_load_frags(lp.mlp, f);
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int myrow = 16 * (t >> 1) + 8 * (t & 1) + g;
     const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
     const int64_t wid = int64_t(blockIdx.x) * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    for (int64_t tile = wid; tile * 16 < n; tile += warps) {
-        const int64_t rg = tile * 16 + g, rg8 = rg + 8;
-        float sg[5], sg8[5], xg[5], xg8[5];
-        for (int k = 0; k < 5; ++k) {
-            sg[k] = rg < n ? stencils[rg * 5 + k] : 0.0f;
-            sg8[k] = rg8 < n ? stencils[rg8 * 5 + k] : 0.0f;
-        }
-        mlp_normalise(sg, xg);
-        mlp_normalise(sg8, xg8);
-        float zr[3], zs[3];
-        mlp_mma_logits(f, xg, xg8, zr, zs);
-        if (t == 0 && rg < n) out[rg] = learned_face(sg, zr[0], zr[1], zr[2], lp);
-        if (t == 1 && rg8 < n) out[rg8] = learned_face(sg8, zs[0], zs[1], zs[2], lp);
+    for (int64_t blk = wid; blk * 32 < n; blk += warps) {
+        const int64_t r = blk * 32 + myrow;
+        const int64_t rr = r < n ? r : n - 1;
+        float s[5], ds[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s[k] = stencils[rr * 5 + k];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) ds[k] = s[k] - s[2];
+        const float d = learned_delta32(f, ds, lp);
+        if (r < n) out[r] = s[2] + d;
     }
 }
 
@@ -251,7 +257,7 @@ int64_t shk_mlp_workspace_bytes(int64_t n) {
 }
 
 int shk_mlp_loss_grad_f32(const float* params, const float* stencils, const float* target,
-                          const float* weight, int64_t n, float* grad, double* loss,
+                          const float* weight, int64_t n, float reg, float* grad, double* loss,
                           void* workspace, int64_t workspace_bytes, void* stream) {
     if (!params || !stencils || !target || !weight || !grad || n <= 0 || !workspace) return SHK_EINVAL;
     if (workspace_bytes < shk_mlp_workspace_bytes(n)) return SHK_EINVAL;
@@ -263,7 +269,7 @@ int shk_mlp_loss_grad_f32(const float* params, const float* stencils, const floa
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int r = lcheck(cudaFuncSetAttribute(mlp_loss_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (r) return r;
-    mlp_loss_grad_kernel<<<nb, kTrainThreads, smem, st>>>(params, stencils, target, weight, n, bg, bl);
+    mlp_loss_grad_kernel<<<nb, kTrainThreads, smem, st>>>(params, stencils, target, weight, n, reg, bg, bl);
     r = lcheck(cudaGetLastError());
     if (r) return r;
     mlp_reduce_kernel<<<(kMlpParams + 255) / 256, 256, 0, st>>>(bg, bl, nb, n, grad, loss);
@@ -283,8 +289,9 @@ int shk_mlp_adam_f32(float* params, const float* grad, float* m, float* v, float
 int shk_learned_faces_f32(const shk_scheme* scheme, const float* stencils, float* out, int64_t n,
                           void* stream) {
     if (!scheme || !scheme->mlp || !stencils || !out || n <= 0) return SHK_EINVAL;
-    LearnedParams lp{scheme->mlp, static_cast<float>(scheme->eps), scheme->tau, scheme->band};
-    const int64_t tiles = (n + 15) / 16;
+    LearnedParams lp{scheme->mlp, static_cast<float>(scheme->eps), scheme->tau, scheme->band,
+                     scheme->dev};
+    const int64_t tiles = (n + 31) / 32;
     const int blocks = static_cast<int>((tiles + 7) / 8 < 4096 ? (tiles + 7) / 8 : 4096);
     learned_faces_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(lp, stencils, out, n);
     return lcheck(cudaGetLastError());

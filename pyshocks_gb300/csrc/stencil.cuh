@@ -55,54 +55,79 @@ struct OpParams {
     T eps, delta, hnu, c;  // WENO eps, ES-WENO delta, nu/2, advection speed
     T hnu_amax;            // LF: nu/2 * global max |f'|
     LearnedParams lp;      // learned reconstruction (float32 state only)
+    T fscale;              // face values F are stored as F / fscale (see face_fluxes)
 };
 
-// learned reconstruction of cells [clo, chi): two faces per cell, 16 faces per
-// warp-level tensor-core evaluation (row 2j: right face of cell clo+j, row
-// 2j+1: left face, mirrored stencil)
-__device__ __forceinline__ void learned_phase(const float* v, int clo, int chi, float* UL, float* UR,
-                                              const LearnedParams& lp) {
+// learned reconstruction of cells [clo, chi): two faces per cell, one face per
+// lane, 32 faces per warp iteration (face 2j: right face of cell clo+j with
+// stencil v_{c-2..c+2}; face 2j+1: left face, mirrored stencil). The cell
+// differences d_k = v_{k+1} - v_k are formed once, in the state precision, and
+// stored as float in `dbuf`; a face's stencil relative to v_c is a float sum of
+// them, and the face value is v_c + correction in the state precision, so
+// double states spend two double operations per face here.
+template <class T>
+__device__ __forceinline__ void learned_phase(const T* v, int clo, int chi, T* UL, T* UR,
+                                              float* dbuf, const LearnedParams& lp) {
+    for (int c = clo - 2 + threadIdx.x; c < chi + 1; c += blockDim.x)
+        dbuf[c] = static_cast<float>(v[c + 1] - v[c]);
     MlpFrags f;
     mlp_load_frags(lp.mlp, f);
+    __syncthreads();
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int ncell = chi - clo, rows = 2 * ncell;
-    for (int q = warp; q * 16 < rows; q += nw) {
-        const int rg = q * 16 + g, rg8 = rg + 8;
-        const int side = g & 1;  // same parity for rows g and g+8
-        const int cg = clo + min(rg >> 1, ncell - 1), cg8 = clo + min(rg8 >> 1, ncell - 1);
-        float sg[5], sg8[5];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const int o = side ? 2 - k : k - 2;
-            sg[k] = v[cg + o];
-            sg8[k] = v[cg8 + o];
+    const int myrow = 16 * (t >> 1) + 8 * (t & 1) + g;  // within the 32-face block
+    for (int q = warp; q * 32 < rows; q += nw) {
+        const int r = q * 32 + myrow;
+        const bool valid = r < rows;
+        const int c = clo + min(r >> 1, ncell - 1);
+        const int side = r & 1;  // 0: right face (ur), 1: left face (ul)
+        const float dm2 = dbuf[c - 2], dm1 = dbuf[c - 1], d0 = dbuf[c], dp1 = dbuf[c + 1];
+        // v_{c+o} - v_c for o = -2..2, then mirrored for the left face
+        const float lo2 = -(dm1 + dm2), lo1 = -dm1, hi1 = d0, hi2 = d0 + dp1;
+        float ds[5];
+        if (side) {
+            ds[0] = hi2; ds[1] = hi1; ds[2] = 0.0f; ds[3] = lo1; ds[4] = lo2;
+        } else {
+            ds[0] = lo2; ds[1] = lo1; ds[2] = 0.0f; ds[3] = hi1; ds[4] = hi2;
         }
-        float xg[5], xg8[5];
-        mlp_normalise(sg, xg);
-        mlp_normalise(sg8, xg8);
-        float zr[3], zs[3];
-        mlp_mma_logits(f, xg, xg8, zr, zs);
-        if (t == 0 && rg < rows) {
-            const float val = learned_face(sg, zr[0], zr[1], zr[2], lp);
-            (side ? UL : UR)[cg] = val;
-        }
-        if (t == 1 && rg8 < rows) {
-            const float val = learned_face(sg8, zs[0], zs[1], zs[2], lp);
-            (side ? UL : UR)[cg8] = val;
-        }
+        const float d = learned_delta32(f, ds, lp);
+        if (valid) (side ? UL : UR)[c] = v[c] + static_cast<T>(d);
     }
 }
 
 // ---------------------------------------------------------------------------
 // one evaluation of the numerical fluxes F_j (face j+1/2) for j in [lo-1, hi)
-// from the stage input v (valid on [lo-3, hi+3)). Leaves F in sm.D.
+// from the stage input v (valid on [lo-3, hi+3)). Leaves F / p.fscale in sm.D
+// (fscale = 1/4 for the FP64 Burgers-Rusanov flux with nu = 1, else 1).
 // ---------------------------------------------------------------------------
 template <class T, int EQ, int REC, int FLUX>
 __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Smem<T>& sm,
                                             const OpParams<T>& p) {
     const int tid = threadIdx.x, nt = blockDim.x;
-    if constexpr (REC == SHK_REC_WENOJS53) {
+    if constexpr (REC == SHK_REC_WENOJS53 && sizeof(T) == 8) {
+        // FP64 (pipe-bound): unscaled differences, see weno53_cell_d.
+        // phase A: d_c = v_{c+1} - v_c, c in [lo-3, hi+2)
+        for (int c = lo - 3 + tid; c < hi + 2; c += nt) sm.H[c] = v[c + 1] - v[c];
+        __syncthreads();
+        // phase B: E_c = d_c - d_{c-1}, G_c = 13/3 E_c^2, c in [lo-2, hi+2)
+        for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
+            const T e = sm.H[c] - sm.H[c - 1];
+            sm.D[c] = e;
+            sm.Q[c] = (T(13.0 / 3.0) * e) * e;
+        }
+        __syncthreads();
+        const T eps4 = T(4) * p.eps;
+#pragma unroll 2
+        for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
+            T ul, ur;
+            weno53_cell_d(v[c], sm.H[c - 1], sm.H[c], sm.D[c - 1], sm.D[c], sm.D[c + 1],
+                          sm.Q[c - 1], sm.Q[c], sm.Q[c + 1], eps4, ul, ur);
+            sm.UL[c] = ul;
+            sm.UR[c] = ur;
+        }
+        __syncthreads();
+    } else if constexpr (REC == SHK_REC_WENOJS53) {
         // phase A: H_c = (v_{c+1} - v_c)/2, c in [lo-3, hi+2)
         for (int c = lo - 3 + tid; c < hi + 2; c += nt) sm.H[c] = T(0.5) * (v[c + 1] - v[c]);
         __syncthreads();
@@ -125,8 +150,7 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
         }
         __syncthreads();
     } else if constexpr (REC == SHK_REC_LEARNED) {
-        static_assert(sizeof(T) == 4, "the learned reconstruction runs on float32 states");
-        learned_phase(v, lo - 1, hi + 1, sm.UL, sm.UR, p.lp);
+        learned_phase<T>(v, lo - 1, hi + 1, sm.UL, sm.UR, reinterpret_cast<float*>(sm.H), p.lp);
         __syncthreads();
     } else {
         for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
@@ -141,7 +165,16 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
     // phase D: F_j, j in [lo-1, hi)
     for (int j = lo - 1 + tid; j < hi; j += nt) {
         T f;
-        if constexpr (FLUX == SHK_FLUX_RUSANOV) {
+        if constexpr (FLUX == SHK_FLUX_RUSANOV && EQ == SHK_EQ_BURGERS && sizeof(T) == 8) {
+            if (p.fscale != T(1)) {
+                // nu = 1: 4 F = L^2 + R^2 + 2a (R - L), stored with fscale = 1/4
+                const T L = sm.UL[j + 1], R = sm.UR[j];
+                const auto ab = abs_bits(v[j]) > abs_bits(v[j + 1]) ? abs_bits(v[j]) : abs_bits(v[j + 1]);
+                f = fma(L, L, fma(R, R, twice_abs_bits(ab) * (R - L)));
+            } else {
+                f = rusanov_face<EQ, T>(sm.UR[j], sm.UL[j + 1], v[j], v[j + 1], p.hnu, p.c);
+            }
+        } else if constexpr (FLUX == SHK_FLUX_RUSANOV) {
             f = rusanov_face<EQ, T>(sm.UR[j], sm.UL[j + 1], v[j], v[j + 1], p.hnu, p.c);
         } else if constexpr (FLUX == SHK_FLUX_LF) {
             f = lf_face<EQ, T>(sm.UR[j], sm.UL[j + 1], p.hnu_amax, p.c);
@@ -235,6 +268,7 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
                                             const OpParams<T>& p) {
     constexpr int HL = step_halo<T>();
     const int tid = threadIdx.x, nt = blockDim.x;
+    dtdx *= p.fscale;
     // stage 1: k1 = u + dt L(u) on [HL-6, HL+te+6)
     {
         const int lo = HL - 6, hi = HL + te + 6;
@@ -285,8 +319,24 @@ struct PlanDev {
     unsigned int* done;
     int32_t* status;
     double* partial;  // [nitems]
+    const double* dt_fixed;  // [fixed_steps][B] prescribed steps, or null (CFL steps)
+    int64_t fixed_steps;
     int32_t B, nitems, tile, max_steps;
 };
+
+// time step k of instance b: the prescribed step when the plan has a dt table
+// (a step <= 0 or past the table's end leaves the instance unchanged, a
+// non-finite one is an error), else the CFL step clipped at tfinal
+__device__ __forceinline__ DtState plan_dt(const PlanDev& P, int64_t k, int b, double smax) {
+    if (P.dt_fixed) {
+        DtState s;
+        s.dt = k < P.fixed_steps ? P.dt_fixed[size_t(k) * P.B + b] : 0.0;
+        s.active = !(s.dt <= 0.0);
+        s.finite = isfinite(s.dt);
+        return s;
+    }
+    return compute_dt(smax, P.cfl[b], P.theta, P.t[b], P.tfinal[b]);
+}
 
 template <class T>
 __device__ __forceinline__ unsigned long long to_double_bits(typename Bits<T>::type b) {

@@ -5,9 +5,9 @@ face to the three WENO-JS5 sub-stencil weights through a softmax, so the face
 value stays a convex combination of the sub-stencil values and the flux stays
 conservative. It plugs into the reference's reconstruction slot
 (``src/pyshocks/reconstruction.py:79-119``) as :class:`LearnedWENO`. Plain
-WENO-JS is the per-face fallback wherever the network leaves the trust band
-(more than ``band`` of its weight on sub-stencils whose JS weight is below
-``tau``).
+WENO-JS is the per-face fallback wherever the network leaves the trust band:
+more than ``band`` of its weight on sub-stencils whose JS weight is below
+``tau``, or any weight more than ``dev`` away from the JS weight.
 
 Training pairs come from the plain solver itself: fine-grid runs (N = 4096)
 restricted to the coarse grid (N = 256, 16-cell averages) give coarse stencils,
@@ -17,8 +17,8 @@ Training runs on the GPU with the hand-written loss/gradient and Adam kernels.
 
 from __future__ import annotations
 
-import ctypes
 import math
+import pathlib
 from dataclasses import dataclass, field
 from typing import Sequence
 
@@ -48,14 +48,29 @@ def init_params(seed: int = 0, device="cuda") -> torch.Tensor:
     return p.to(device=device, dtype=torch.float32)
 
 
+DEFAULT_PARAMS = pathlib.Path(__file__).resolve().parent / "data" / "mlp_weno_burgers_advection.npy"
+
+
+def load_default_params(device="cuda") -> torch.Tensor:
+    """The network trained by :func:`train_default` (committed with the package;
+    regenerate with ``python -m pyshocks_gb300.learned``). Falls back to the
+    untrained initialisation when the file is absent."""
+    if DEFAULT_PARAMS.exists():
+        return torch.tensor(np.load(DEFAULT_PARAMS), dtype=torch.float32, device=device)
+    return init_params(device=device)
+
+
 @dataclass(frozen=True, eq=False)
 class LearnedWENO(Reconstruction):
-    """Learned-weight WENO reconstruction (float32 states, batched solver)."""
+    """Learned-weight WENO reconstruction. With float64 states the stencil
+    differences and the network run in float32/bfloat16 and the face value is
+    assembled in float64 (``v_c + correction``)."""
 
     params: torch.Tensor = field(default_factory=lambda: init_params())
     eps: float = 1.0e-6
     tau: float = 1.0e-2
     band: float = 0.1
+    dev: float = 0.5
 
     code = L.SHK_REC_LEARNED
 
@@ -78,6 +93,7 @@ def c_scheme_fields(rec: LearnedWENO, s: L.ShkScheme) -> None:
     s.mlp = rec.params.data_ptr()
     s.tau = float(rec.tau)
     s.band = float(rec.band)
+    s.dev = float(rec.dev)
 
 
 def face_values(scheme, stencils: torch.Tensor) -> torch.Tensor:
@@ -203,7 +219,7 @@ class Trainer:
     """Adam on the MLP parameters with the CUDA loss/gradient kernel."""
 
     def __init__(self, params: torch.Tensor, *, lr: float = 2.0e-3, betas=(0.9, 0.999),
-                 eps: float = 1.0e-8, max_batch: int = 1 << 16):
+                 eps: float = 1.0e-8, max_batch: int = 1 << 16, reg: float = 1.0e-3):
         self.lib = L.lib()
         self.params = params
         self.m = torch.zeros_like(params)
@@ -215,6 +231,7 @@ class Trainer:
         self.ws = torch.empty(int(self.lib.shk_mlp_workspace_bytes(max_batch)), dtype=torch.uint8,
                               device=params.device)
         self.max_batch = max_batch
+        self.reg = float(reg)
 
     def loss_and_grad(self, s: torch.Tensor, t: torch.Tensor, w: torch.Tensor) -> torch.Tensor:
         n = s.shape[0]
@@ -222,7 +239,7 @@ class Trainer:
         if need > self.ws.numel():
             self.ws = torch.empty(need, dtype=torch.uint8, device=self.params.device)
         L.check(self.lib.shk_mlp_loss_grad_f32(
-            self.params.data_ptr(), s.data_ptr(), t.data_ptr(), w.data_ptr(), n,
+            self.params.data_ptr(), s.data_ptr(), t.data_ptr(), w.data_ptr(), n, self.reg,
             self.grad.data_ptr(), self.loss_dev.data_ptr(), self.ws.data_ptr(), self.ws.numel(),
             L.stream_handle()), "mlp_loss_grad")
         return self.loss_dev
@@ -261,3 +278,24 @@ class Trainer:
 
 
 # }}}
+
+
+def train_default(*, n_ics: int = 640, epochs: int = 8, reg: float = 1.0e-3, seed: int = 0,
+                  lr: float = 3.0e-3, batch: int = 32768):
+    """Train the default network: ~1e7 pairs (N = 256 restricted from N = 4096,
+    Burgers and linear advection, config-1-like and random-Fourier initial
+    conditions), Adam with cosine decay. Returns ``(params, loss history)``."""
+    s, t, w = generate_pairs(n_coarse=256, ratio=16, n_ics=n_ics, snapshots=16,
+                             steps_between=256, seed=seed)
+    params = init_params(seed=seed)
+    tr = Trainer(params, lr=lr, reg=reg)
+    hist = tr.fit(s, t, w, epochs=epochs, batch=batch, lr_final=1.0e-4, seed=seed)
+    return params, hist
+
+
+if __name__ == "__main__":
+    p, h = train_default()
+    DEFAULT_PARAMS.parent.mkdir(exist_ok=True)
+    np.save(DEFAULT_PARAMS, p.cpu().numpy())
+    print("losses", h)
+

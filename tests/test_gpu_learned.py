@@ -1,0 +1,141 @@
+"""Learned WENO weights on the GPU against the torch oracle (``oracle/learned_ref.py``).
+
+Tolerances:
+* tensor-core face values vs the oracle with the same bfloat16 roundings:
+  within 5e-3 of the stencil range for 99.5 % of the faces (tanh.approx vs
+  exact tanh can flip a bfloat16 rounding; faces at the edge of the trust
+  band can switch to the fallback);
+* the fp32 loss/gradient kernel vs torch float64 autograd: 1e-4 relative;
+* a learned batched step vs the oracle's learned step: 2e-3 of the range.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import learned_ref as LR
+from oracle import numpy_ref as R
+from oracle import torch_ref as T
+
+pytestmark = pytest.mark.gpu
+
+
+def _stencils(n, seed):
+    """Random smooth, kinked and discontinuous stencils."""
+    g = torch.Generator().manual_seed(seed)
+    x = torch.linspace(-2, 2, 5, dtype=torch.float64)
+    a = torch.randn(n, 1, generator=g, dtype=torch.float64)
+    b = torch.randn(n, 1, generator=g, dtype=torch.float64)
+    c = torch.randn(n, 1, generator=g, dtype=torch.float64)
+    smooth = a + b * x + 0.3 * c * x**2
+    jumpat = torch.randint(-2, 3, (n, 1), generator=g)
+    jump = torch.where(x[None, :] > jumpat, 1.0, 0.0) * torch.randn(n, 1, generator=g, dtype=torch.float64)
+    kind = torch.randint(0, 3, (n, 1), generator=g)
+    s = torch.where(kind == 0, smooth, torch.where(kind == 1, smooth + jump, smooth.abs()))
+    return s * torch.exp(torch.randn(n, 1, generator=g, dtype=torch.float64))
+
+
+def _scheme(params, tau=1.0e-2, band=0.1, dev=0.5):
+    from pyshocks_gb300 import burgers, learned
+
+    rec = learned.LearnedWENO(params=params, eps=1.0e-6, tau=tau, band=band, dev=dev)
+    return burgers.Rusanov(rec=rec)
+
+
+@pytest.mark.parametrize(("band", "dev"), [(0.1, 0.5), (2.0, 2.0)])
+def test_tensor_core_faces_match_oracle(band, dev):
+    from pyshocks_gb300 import learned
+
+    params = learned.init_params(seed=3)
+    s = _stencils(4099, 1)  # not a multiple of 16: ragged last warp tile
+    got = learned.face_values(_scheme(params, band=band, dev=dev), s.float().cuda()).double().cpu()
+    ref, fb = LR.face_value(params.double().cpu(), s.float().double(), eps=1.0e-6, tau=1.0e-2,
+                            band=band, dev=dev, bf16=True, return_fallback=True)
+    rng = (s.amax(-1) - s.amin(-1))
+    err = (got - ref).abs() / (rng + 1e-30)
+    # faces whose fallback decision sits on the edge of the band may flip
+    ok = err < 5.0e-3
+    assert ok.float().mean() > 0.995, float(err.max())
+    if band > 1.5:
+        assert not bool(fb.any())
+
+
+def test_loss_grad_kernel_matches_autograd():
+    from pyshocks_gb300 import learned
+
+    params = learned.init_params(seed=5)
+    s = _stencils(3001, 2)
+    t = s[:, 2] + 0.1 * torch.randn(3001, generator=torch.Generator().manual_seed(4), dtype=torch.float64)
+    w = 1.0 / (s.amax(-1) - s.amin(-1) + 1e-3) ** 2
+    tr = learned.Trainer(params.clone(), reg=0.3)
+    loss = float(tr.loss_and_grad(s.float().cuda(), t.float().cuda(), w.float().cuda()))
+    grad = tr.grad.double().cpu()
+    p64 = params.double().cpu().requires_grad_(True)
+    lref = LR.training_loss(p64, s.float().double(), t.float().double(), w.float().double(),
+                            reg=0.3)
+    (gref,) = torch.autograd.grad(lref, p64)
+    assert abs(loss - float(lref.detach())) < 1.0e-4 * abs(float(lref.detach()))
+    assert float((grad - gref).abs().max() / gref.abs().max()) < 1.0e-4
+
+
+def test_training_reduces_loss():
+    from pyshocks_gb300 import learned
+
+    s, t, w = learned.generate_pairs(n_coarse=64, ratio=8, n_ics=16, snapshots=4,
+                                     steps_between=64, seed=1)
+    params = learned.init_params(seed=0)
+    tr = learned.Trainer(params, lr=3e-3, reg=0.0)  # the face-error term alone
+    l0 = float(tr.loss_and_grad(s, t, w))
+    hist = tr.fit(s, t, w, epochs=20, batch=2048)
+    l1 = float(tr.loss_and_grad(s, t, w))
+    assert l1 < 0.7 * l0, (l0, l1, hist[-3:])
+
+
+def test_learned_batched_step_matches_oracle():
+    """A few float32 SSPRK33 steps of the learned scheme (Burgers, Rusanov)
+    against the oracle's learned reconstruction in float64 with the same
+    bfloat16 roundings and the same dt."""
+    from pyshocks_gb300 import learned
+    from pyshocks_gb300.batched import BatchedSolver
+
+    params = learned.init_params(seed=7)
+    n, nsteps = 256, 5
+    u0 = R.exact_cell_average_sine(R.make_uniform_cell_grid(-1.0, 1.0, n, 3))[3:-3]
+    solver = BatchedSolver(_scheme(params), [n], 2.0 / n, dtype=torch.float32, max_steps=nsteps)
+    solver.reset(torch.tensor(u0))
+    solver.step(nsteps)
+    got = solver.u.double().cpu()
+    dts = solver.dt_history().cpu()
+    wts = {"params": params.double().cpu(), "tau": 1.0e-2, "band": 0.1, "bf16": True}
+    ref, _ = T.forward(torch.tensor(u0, dtype=torch.float32).double()[None], 2.0 / n, nsteps,
+                       dts=dts, rec="learned", weights=wts)
+    err = float((got - ref[0]).abs().max())
+    assert err < 2.0e-3 * float(np.ptp(u0)), err
+    assert solver.status() == 0
+
+
+def test_learned_adjoint_matches_autograd():
+    """The hand-written adjoint of the learned scheme, MLP backward included
+    (float32 state, sqrt(n) checkpoints), against torch autograd through the
+    oracle's learned reconstruction with the same bfloat16 roundings and the
+    same frozen dt sequence. Tolerance 5e-3 relative (float32 state, tanh.approx)."""
+    from pyshocks_gb300 import learned
+    from pyshocks_gb300.adjoint import CheckpointedSolve
+    from pyshocks_gb300.batched import BatchedSolver
+
+    params = learned.init_params(seed=11)
+    n, nsteps = 128, 8
+    u0 = R.exact_cell_average_sine(R.make_uniform_cell_grid(-1.0, 1.0, n, 3))[3:-3]
+    tgt = u0 + 0.05 * np.sin(3 * np.pi * np.linspace(-1, 1, n, endpoint=False))
+    solver = BatchedSolver(_scheme(params), [n], 2.0 / n, dtype=torch.float32, max_steps=nsteps)
+    cs = CheckpointedSolve(solver, nsteps, stride=3)
+    uT = cs.forward(torch.tensor(u0))
+    g = cs.backward(uT - torch.tensor(tgt, device="cuda", dtype=torch.float32)).double().cpu()
+    wts = {"params": params.double().cpu(), "tau": 1.0e-2, "band": 0.1, "bf16": True}
+    u0t = torch.tensor(u0, dtype=torch.float32).double()[None]
+    ref, _, _ = T.adjoint_gradient(u0t, torch.tensor(tgt)[None], 2.0 / n, nsteps,
+                                   dts=solver.dt_history().cpu(), rec="learned", weights=wts)
+    err = float((g - ref[0]).abs().max() / ref.abs().max())
+    assert err < 5.0e-3, err
