@@ -223,10 +223,14 @@ int64_t shk_apply_operator_lf_noalloc_max_cells(void);
 int shk_mlp_num_params(void);
 int64_t shk_mlp_workspace_bytes(int64_t n);
 
-/* loss (1/n) sum_i [w_i (face_i - target_i)^2 + reg |omega_i - d|^2] of the raw
- * network over n stencils (n x 5 float32; d the WENO-JS5 ideal weights) and its
- * gradient w.r.t. the parameters (fp32 forward/backward, deterministic
- * reduction). *loss is device memory (double). */
+/* loss 1/(2n) sum_i sum_{F = R, L} [w_i (face_F,i - target_F,i)^2
+ *                                  + reg |omega_F,i - d|^2]
+ * of the raw network over n cells: stencils n x 5 float32 (v_{c-2..c+2}),
+ * target n x 2 (right, left face), weight n; d the WENO-JS5 ideal weights. One
+ * network output z per cell gives omega_R = softmax(z) and omega_L =
+ * softmax(z2 - ln 3, z1, z0 + ln 3). Also the gradient w.r.t. the parameters
+ * (fp32 forward/backward, deterministic reduction). *loss is device memory
+ * (double). */
 int shk_mlp_loss_grad_f32(const float* params, const float* stencils, const float* target,
                           const float* weight, int64_t n, float reg, float* grad, double* loss,
                           void* workspace, int64_t workspace_bytes, void* stream);
@@ -235,8 +239,9 @@ int shk_mlp_loss_grad_f32(const float* params, const float* stencils, const floa
 int shk_mlp_adam_f32(float* params, const float* grad, float* m, float* v, float lr,
                      float beta1, float beta2, float eps, int32_t step, void* stream);
 
-/* learned face values of n stencils (n x 5) with the tensor-core inference and
- * the WENO-JS trust band of the flux kernel (scheme->mlp, eps, tau, band) */
+/* learned face values (right, left: out is n x 2) of n cell stencils (n x 5,
+ * v_{c-2..c+2}) with the tensor-core inference and the per-face WENO-JS trust
+ * band of the flux kernel (scheme->mlp, eps, tau, band, dev) */
 int shk_learned_faces_f32(const shk_scheme* scheme, const float* stencils, float* out,
                           int64_t n, void* stream);
 

@@ -1,18 +1,20 @@
 """torch-CPU restatement of the learned-weight WENO reconstruction.
 
-THIS IS TEST INFRASTRUCTURE (the oracle) for ``pyshocks_gb300/csrc/learned.cu``:
-only tests use it, as the checker.
+THIS IS TEST INFRASTRUCTURE (the oracle) for ``pyshocks_gb300/csrc/learned.cu``
+and ``learned.cuh``: only tests use it, as the checker.
 
 The method (no reference counterpart; it plugs into the reference's
 reconstruction slot, ``src/pyshocks/reconstruction.py:79-119``): an MLP
 5 -> 32 -> 32 -> 3 (tanh, tanh, softmax) maps the normalised 5-point stencil
-of a face to the three nonlinear weights of the WENO-JS5 sub-stencils
-(``src/pyshocks/weno.py:206-244``). The face value is the convex combination
-``sum_k omega_k uhat_k`` of the sub-stencil values, so the flux stays
-conservative. Where the network puts more than ``band`` of its weight on
-sub-stencils that WENO-JS marks as crossing a discontinuity (JS weight below
-``tau``), or moves any weight more than ``dev`` from the JS weight, the plain
-WENO-JS weights are used instead (per face).
+``s = v_{c-2..c+2}`` of a cell to the weights of the WENO-JS5 sub-stencils
+(``src/pyshocks/weno.py:206-244``) at its right face, ``omega_R = softmax(z)``;
+the left face reuses the scores with its own ideal weights (as WENO-JS5 reuses
+its smoothness indicators): ``omega_L = softmax(z2 - ln 3, z1, z0 + ln 3)``.
+Each face value is the convex combination ``sum_k omega_k uhat_k`` of its
+sub-stencil values, so the flux stays conservative. Where the network puts
+more than ``band`` of a face's weight on sub-stencils that WENO-JS marks as
+crossing a discontinuity (JS weight below ``tau``), or moves any weight more
+than ``dev`` from the JS weight, that face uses the plain WENO-JS weights.
 
 Parameter vector (1347 float32): W1[32,5], b1[32], W2[32,32], b2[32],
 W3[3,32], b3[3], row-major.
@@ -52,78 +54,99 @@ def normalise(s: torch.Tensor) -> torch.Tensor:
     return (s - m) / (r + NORM_EPS)
 
 
-def mlp_weights(params, s, *, bf16: bool = False):
-    """Softmax weights of stencils ``s[..., 5]``. With ``bf16`` the inputs and
-    weights are rounded to bfloat16 (FP32 accumulation) and each hidden layer
-    applies tanh to the bfloat16-rounded pre-activation with a bfloat16 result,
-    as the tensor-core inference kernel does (tanh.approx.bf16x2)."""
+def logits(params, s, *, bf16: bool = False):
+    """Network output ``z`` of cell stencils ``s[..., 5]``. With ``bf16`` the
+    inputs and weights are rounded to bfloat16 (FP32 accumulation) and each
+    hidden layer applies tanh to the bfloat16-rounded pre-activation with a
+    bfloat16 result, as the tensor-core inference kernel does
+    (tanh.approx.bf16x2)."""
     W1, b1, W2, b2, W3, b3 = unpack(params)
     x = _bf16(normalise(s), bf16)
     h1 = _bf16(torch.tanh(_bf16(x @ _bf16(W1, bf16).T + _bf16(b1, bf16), bf16)), bf16)
     h2 = _bf16(torch.tanh(_bf16(h1 @ _bf16(W2, bf16).T + b2, bf16)), bf16)
-    z = h2 @ _bf16(W3, bf16).T + b3
-    return torch.softmax(z, dim=-1)
+    return h2 @ _bf16(W3, bf16).T + b3
 
 
-def substencils(s: torch.Tensor) -> torch.Tensor:
-    """The three WENO-JS5 sub-stencil values at the right face
-    (``src/pyshocks/weno.py:231-239``)."""
-    s0, s1, s2, s3, s4 = s.unbind(-1)
-    return torch.stack([(2 * s0 - 7 * s1 + 11 * s2) / 6,
-                        (-s1 + 5 * s2 + 2 * s3) / 6,
-                        (2 * s2 + 5 * s3 - s4) / 6], dim=-1)
+def mlp_weights(params, s, *, bf16: bool = False):
+    """Right- and left-face softmax weights ``(omega_R, omega_L)`` of cell
+    stencils ``s[..., 5]`` from one network evaluation."""
+    z = logits(params, s, bf16=bf16)
+    ln3 = torch.log(torch.tensor(3.0, dtype=z.dtype))
+    zl = torch.stack([z[..., 2] - ln3, z[..., 1], z[..., 0] + ln3], dim=-1)
+    return torch.softmax(z, dim=-1), torch.softmax(zl, dim=-1)
 
 
-def js_weights(s: torch.Tensor, eps: float) -> torch.Tensor:
-    """WENO-JS5 weights of the right face (``src/pyshocks/weno.py:247-256``)."""
+def substencils(s: torch.Tensor):
+    """WENO-JS5 sub-stencil values at the right face (``src/pyshocks/weno.py:231-239``)
+    and at the left face (the same formulas on the mirrored stencil)."""
+    def right(q):
+        q0, q1, q2, q3, q4 = q.unbind(-1)
+        return torch.stack([(2 * q0 - 7 * q1 + 11 * q2) / 6,
+                            (-q1 + 5 * q2 + 2 * q3) / 6,
+                            (2 * q2 + 5 * q3 - q4) / 6], dim=-1)
+    return right(s), right(torch.flip(s, dims=(-1,)))
+
+
+def js_weights(s: torch.Tensor, eps: float):
+    """WENO-JS5 weights of the right face (``src/pyshocks/weno.py:247-256``) and
+    of the left face (the mirrored stencil: ideal weight d_k on beta_{2-k})."""
     s0, s1, s2, s3, s4 = s.unbind(-1)
     b0 = 13 / 12 * (s0 - 2 * s1 + s2) ** 2 + 0.25 * (s0 - 4 * s1 + 3 * s2) ** 2
     b1 = 13 / 12 * (s1 - 2 * s2 + s3) ** 2 + 0.25 * (s1 - s3) ** 2
     b2 = 13 / 12 * (s2 - 2 * s3 + s4) ** 2 + 0.25 * (3 * s2 - 4 * s3 + s4) ** 2
-    a = torch.stack([_D53[0] / (eps + b0) ** 2, _D53[1] / (eps + b1) ** 2,
-                     _D53[2] / (eps + b2) ** 2], dim=-1)
-    return a / a.sum(dim=-1, keepdim=True)
+    r0, r1, r2 = 1 / (eps + b0) ** 2, 1 / (eps + b1) ** 2, 1 / (eps + b2) ** 2
+    ar = torch.stack([_D53[0] * r0, _D53[1] * r1, _D53[2] * r2], dim=-1)
+    al = torch.stack([_D53[0] * r2, _D53[1] * r1, _D53[2] * r0], dim=-1)
+    return ar / ar.sum(dim=-1, keepdim=True), al / al.sum(dim=-1, keepdim=True)
 
 
-def face_value(params, s, *, eps: float, tau: float, band: float, dev: float = 0.5,
-               bf16: bool = False, return_fallback: bool = False):
-    """Learned face value of stencils ``s[..., 5]`` with the WENO-JS fallback."""
-    w = mlp_weights(params, s, bf16=bf16)
-    wjs = js_weights(s, eps)
+def _band(w, wjs, tau, band, dev):
     excess = torch.sum(w * (wjs < tau).to(w.dtype), dim=-1)
-    fb = (excess > band) | (torch.amax(torch.abs(w - wjs), dim=-1) > dev)
-    w = torch.where(fb[..., None], wjs, w)
-    v = torch.sum(w * substencils(s), dim=-1)
-    return (v, fb) if return_fallback else v
+    return (excess > band) | (torch.amax(torch.abs(w - wjs), dim=-1) > dev)
+
+
+def cell_face_values(params, s, *, eps: float, tau: float, band: float, dev: float = 0.5,
+                     bf16: bool = False, return_fallback: bool = False):
+    """Learned ``(right, left)`` face values of cell stencils ``s[..., 5]``
+    with the per-face WENO-JS fallback."""
+    wr, wl = mlp_weights(params, s, bf16=bf16)
+    jr, jl = js_weights(s, eps)
+    fr, fl = _band(wr, jr, tau, band, dev), _band(wl, jl, tau, band, dev)
+    wr = torch.where(fr[..., None], jr, wr)
+    wl = torch.where(fl[..., None], jl, wl)
+    hr, hl = substencils(s)
+    vr, vl = torch.sum(wr * hr, dim=-1), torch.sum(wl * hl, dim=-1)
+    return ((vr, vl), (fr, fl)) if return_fallback else (vr, vl)
 
 
 def stencils_periodic(u: torch.Tensor):
-    """Right-face stencils (v_{i-2..i+2}) and mirrored left-face stencils
-    (v_{i+2..i-2}) of every cell of periodic rows ``u[B, N]``."""
+    """Cell stencils ``v_{i-2..i+2}`` of every cell of periodic rows ``u[B, N]``."""
     idx = torch.arange(-2, 3)
     n = u.shape[-1]
     cols = (torch.arange(n)[:, None] + idx[None, :]) % n
-    sr = u[..., cols]
-    sl = torch.flip(sr, dims=(-1,))
-    return sl, sr
+    return u[..., cols]
 
 
 def learned_recon(u: torch.Tensor, weights: dict, eps: float):
     """``(ul, ur)`` of every cell for the torch oracle's ``face_flux``."""
-    sl, sr = stencils_periodic(u)
     kw = dict(eps=eps, tau=weights["tau"], band=weights["band"], dev=weights.get("dev", 0.5),
               bf16=weights.get("bf16", False))
-    return face_value(weights["params"], sl, **kw), face_value(weights["params"], sr, **kw)
+    vr, vl = cell_face_values(weights["params"], stencils_periodic(u), **kw)
+    return vl, vr
 
 
 def training_loss(params, s, target, weight, reg: float = 0.0):
-    """Weighted squared face-value error of the raw network (no fallback) plus
-    the pull toward the ideal weights:
-    ``sum_i [w_i (sum_k omega_k uhat_k - target_i)^2 + reg |omega_i - d|^2] / n``."""
-    w = mlp_weights(params, s)
-    v = torch.sum(w * substencils(s), dim=-1)
-    d = torch.tensor(_D53, dtype=w.dtype)
-    return (torch.sum(weight * (v - target) ** 2) + reg * torch.sum((w - d) ** 2)) / s.shape[0]
+    """Weighted squared face-value error of the raw network (no fallback) over
+    both faces of each cell, plus the pull toward the ideal weights:
+    ``sum_i sum_F [w_i (sum_k omega_F,k uhat_F,k - T_F,i)^2 + reg |omega_F,i - d|^2] / (2 n)``
+    with ``target[:, 0]`` / ``target[:, 1]`` the right / left face targets."""
+    wr, wl = mlp_weights(params, s)
+    hr, hl = substencils(s)
+    vr, vl = torch.sum(wr * hr, dim=-1), torch.sum(wl * hl, dim=-1)
+    d = torch.tensor(_D53, dtype=wr.dtype)
+    err = weight * ((vr - target[:, 0]) ** 2 + (vl - target[:, 1]) ** 2)
+    pull = torch.sum((wr - d) ** 2, dim=-1) + torch.sum((wl - d) ** 2, dim=-1)
+    return (torch.sum(err) + reg * torch.sum(pull)) / (2 * s.shape[0])
 
 
 def init_params(seed: int = 0, dtype=torch.float32) -> torch.Tensor:

@@ -216,19 +216,15 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
     for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
         T t0, t1, t2, t3, t4;
         if constexpr (REC == SHK_REC_LEARNED) {
-            // right face: stencil v_{c-2..c+2}; left face: mirrored v_{c+2..c-2};
-            // relative to v_c from the float cell differences, as the forward
-            // (learned_phase left them in H)
+            // the cell's stencil relative to v_c from the float cell differences,
+            // as the forward (learned_phase left them in H)
             const float* db = reinterpret_cast<const float*>(a.H);
             const float dm2 = db[c - 2], dm1 = db[c - 1], d0 = db[c], dp1 = db[c + 1];
-            const float lo2 = -(dm1 + dm2), lo1 = -dm1, hi1 = d0, hi2 = d0 + dp1;
-            float sR[5] = {lo2, lo1, 0.0f, hi1, hi2};
-            float sL[5] = {hi2, hi1, 0.0f, lo1, lo2};
-            float dR[5], dL[5];
-            learned_face_vjp(sR, a.GR[c], a.Wr, p.lp, dR);
-            learned_face_vjp(sL, a.GL[c - 1], a.Wr, p.lp, dL);
-            t0 = dR[0] + dL[4]; t1 = dR[1] + dL[3]; t2 = dR[2] + dL[2];
-            t3 = dR[3] + dL[1]; t4 = dR[4] + dL[0];
+            const float sc[5] = {-(dm1 + dm2), -dm1, 0.0f, d0, d0 + dp1};
+            float dd[5];
+            learned_cell_vjp(sc, static_cast<float>(a.GR[c]), static_cast<float>(a.GL[c - 1]), a.Wr,
+                             p.lp, dd);
+            t0 = dd[0]; t1 = dd[1]; t2 = dd[2]; t3 = dd[3]; t4 = dd[4];
         } else {
             weno53_cell_vjp<T>(a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
                                a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, a.GR[c],

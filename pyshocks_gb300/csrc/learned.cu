@@ -1,18 +1,20 @@
 // Training and standalone inference kernels of the learned-weight WENO
 // reconstruction (see learned.cuh for the method).
 //
-// Training loss over a batch of (stencil, target, weight) samples:
-//   L = (1/n) sum_i [ w_i (sum_k omega_k(x_i) uhat_k(s_i) - target_i)^2
-//                     + reg sum_k (omega_k(x_i) - d_k)^2 ]
-// The second term pulls the weights toward the ideal weights d = (1, 6, 3)/10
-// of WENO-JS5 where the face error does not constrain them (on smooth data
-// every sub-stencil reconstructs well, and an arbitrary choice among them can
-// be unstable in time).
-// with x_i the normalised stencil. The forward and backward passes run one
-// sample per thread in fp32 (exact tanh/exp); per-block gradient sums are
-// formed from the per-sample activations staged in shared memory and written
-// to a per-block workspace, which a second kernel reduces in a fixed order
-// (deterministic). Adam updates the fp32 master weights in place.
+// Training loss over a batch of cells (stencil s_i = v_{c-2..c+2}, targets
+// T_R,i / T_L,i of its right / left face, weight w_i):
+//   L = 1/(2n) sum_i sum_{F in R, L} [ w_i (sum_k omega_F,k(x_i) uhat_F,k(s_i) - T_F,i)^2
+//                                      + reg sum_k (omega_F,k(x_i) - d_k)^2 ]
+// with x_i the normalised stencil and omega_R = softmax(z), omega_L =
+// softmax(z2 - ln 3, z1, z0 + ln 3) of the one network output z(x_i). The
+// second term pulls the weights toward the ideal weights d = (1, 6, 3)/10 of
+// WENO-JS5 where the face error does not constrain them (on smooth data every
+// sub-stencil reconstructs well, and an arbitrary choice among them can be
+// unstable in time). The forward and backward passes run one cell per thread
+// in fp32 (exact tanh/exp); per-block gradient sums are formed from the
+// per-cell activations staged in shared memory and written to a per-block
+// workspace, which a second kernel reduces in a fixed order (deterministic).
+// Adam updates the fp32 master weights in place.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -49,7 +51,7 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_loss_grad_kernel(
 #pragma unroll
     for (int j = 0; j < kOwn; ++j) gacc[j] = 0.0f;
     double lacc = 0.0;
-    const float invn = 1.0f / static_cast<float>(n);
+    const float invn = 0.5f / static_cast<float>(n);  // 2n face terms
 
     for (int64_t base = int64_t(blockIdx.x) * kTrainThreads; base < n;
          base += int64_t(gridDim.x) * kTrainThreads) {
@@ -64,6 +66,11 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_loss_grad_kernel(
 #pragma unroll
             for (int k = 0; k < 5; ++k) s[k] = 0.0f;
         }
+        // shifted by the cell value, as the flux kernel evaluates it
+        const float c = s[2];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) s[k] -= c;
+        s[2] = 0.0f;
         mlp_normalise(s, x);
 #pragma unroll 4
         for (int a = 0; a < kMlpH; ++a) {
@@ -88,26 +95,34 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_loss_grad_kernel(
             z[o] = acc;
         }
         const float zm = fmaxf(fmaxf(z[0], z[1]), z[2]);
-        float e[3], w[3], uh[3];
-        for (int o = 0; o < 3; ++o) e[o] = expf(z[o] - zm);
-        const float se = 1.0f / (e[0] + e[1] + e[2]);
-        for (int o = 0; o < 3; ++o) w[o] = e[o] * se;
-        mlp_substencils(s, uh);
-        const float v = w[0] * uh[0] + w[1] * uh[1] + w[2] * uh[2];
+        float wr[3], wl[3], hr[3], hl[3];
+        cell_softmax(expf(z[0] - zm), expf(z[1] - zm), expf(z[2] - zm), wr, wl);
+        cell_substencils(s, hr, hl);
         if (valid) {
-            const float r = v - target[i];
+            const float rr = (wr[0] * hr[0] + wr[1] * hr[1] + wr[2] * hr[2]) - (target[2 * i] - c);
+            const float rl = (wl[0] * hl[0] + wl[1] * hl[1] + wl[2] * hl[2]) - (target[2 * i + 1] - c);
             const float wi = weight[i];
-            const float g0 = w[0] - 0.1f, g1 = w[1] - 0.6f, g2 = w[2] - 0.3f;
-            lacc += static_cast<double>(wi) * r * r + static_cast<double>(reg) * (g0 * g0 + g1 * g1 + g2 * g2);
-            // dL/dv, dv/domega_k = uhat_k, plus the regulariser; softmax backward
-            const float dv = 2.0f * wi * r * invn;
+            const float gr[3] = {wr[0] - 0.1f, wr[1] - 0.6f, wr[2] - 0.3f};
+            const float gl[3] = {wl[0] - 0.1f, wl[1] - 0.6f, wl[2] - 0.3f};
+            lacc += static_cast<double>(wi) * (static_cast<double>(rr) * rr + static_cast<double>(rl) * rl) +
+                    static_cast<double>(reg) * (gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2] +
+                                                gl[0] * gl[0] + gl[1] * gl[1] + gl[2] * gl[2]);
+            // dL/dv per face, dv/domega_k = uhat_k, plus the regulariser; softmax
+            // backward of both faces into the shared logits
+            const float dvr = 2.0f * wi * rr * invn, dvl = 2.0f * wi * rl * invn;
             const float rg = 2.0f * reg * invn;
-            const float dw0 = fmaf(dv, uh[0], rg * g0), dw1 = fmaf(dv, uh[1], rg * g1),
-                        dw2 = fmaf(dv, uh[2], rg * g2);
-            const float dot = w[0] * dw0 + w[1] * dw1 + w[2] * dw2;
-            dz[0] = w[0] * (dw0 - dot);
-            dz[1] = w[1] * (dw1 - dot);
-            dz[2] = w[2] * (dw2 - dot);
+            float dw[3], dot;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) dw[k] = fmaf(dvr, hr[k], rg * gr[k]);
+            dot = wr[0] * dw[0] + wr[1] * dw[1] + wr[2] * dw[2];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) dz[k] = wr[k] * (dw[k] - dot);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) dw[k] = fmaf(dvl, hl[k], rg * gl[k]);
+            dot = wl[0] * dw[0] + wl[1] * dw[1] + wl[2] * dw[2];
+            dz[2] += wl[0] * (dw[0] - dot);
+            dz[1] += wl[1] * (dw[1] - dot);
+            dz[0] += wl[2] * (dw[2] - dot);
         }
         // backward through the hidden layers
         float da2[kMlpH], da1[kMlpH];
@@ -186,7 +201,7 @@ __global__ void mlp_reduce_kernel(const float* __restrict__ block_grad, const do
     if (p == 0 && loss) {
         double l = 0.0;
         for (int b = 0; b < nblocks; ++b) l += block_loss[b];
-        *loss = l / static_cast<double>(n);
+        *loss = l / (2.0 * static_cast<double>(n));
     }
 }
 
@@ -203,7 +218,8 @@ __global__ void mlp_adam_kernel(float* __restrict__ P, const float* __restrict__
     P[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
 }
 
-// standalone learned face values of n stencils (tensor-core path, as in the flux kernel)
+// standalone learned face values (right, left) of n cell stencils
+// (tensor-core path, as in the flux kernel)
 __global__ void __launch_bounds__(256) learned_faces_kernel(LearnedParams lp, const float* __restrict__ stencils,
                                                             float* __restrict__ out, int64_t n) {
     MlpFrags f;
@@ -220,8 +236,13 @@ __global__ void __launch_bounds__(256) learned_faces_kernel(LearnedParams lp, co
         for (int k = 0; k < 5; ++k) s[k] = stencils[rr * 5 + k];
 #pragma unroll
         for (int k = 0; k < 5; ++k) ds[k] = s[k] - s[2];
-        const float d = learned_delta32(f, ds, lp);
-        if (r < n) out[r] = s[2] + d;
+        ds[2] = 0.0f;
+        float cr, cl;
+        learned_cell32(f, ds, lp, cr, cl);
+        if (r < n) {
+            out[2 * r] = s[2] + cr;
+            out[2 * r + 1] = s[2] + cl;
+        }
     }
 }
 

@@ -1,13 +1,19 @@
 // Learned-weight WENO reconstruction: an MLP 5 -> 32 -> 32 -> 3 (tanh, tanh,
-// softmax) maps the normalised 5-point stencil of a face to the weights of the
-// three WENO-JS5 sub-stencils (src/pyshocks/weno.py:206-244); the face value is
-// the convex combination sum_k omega_k uhat_k, so the flux stays conservative.
-// The trust band: where the network puts more than `band` of its weight on
-// sub-stencils that WENO-JS marks as crossing a discontinuity (JS weight below
-// `tau`), or moves any weight more than `dev` away from the WENO-JS weight, the
-// plain WENO-JS weights are used instead (per face).
+// softmax) maps the normalised 5-point stencil of a cell, s = v_{c-2..c+2}, to
+// the weights of the three WENO-JS5 sub-stencils (src/pyshocks/weno.py:206-244)
+// at the cell's right face: omega_R = softmax(z). The cell's left face takes the
+// same sub-stencil scores with its own ideal weights, as WENO-JS5 does with its
+// shared smoothness indicators (alpha_k = d_k / (eps + beta_k)^2 on the right,
+// d_k / (eps + beta_{2-k})^2 on the mirrored left): omega_L = softmax(z2 - ln 3,
+// z1, z0 + ln 3), i.e. proportional to (e2 / 3, e1, 3 e0) with e = exp(z). One
+// network evaluation serves both faces. Each face value is the convex
+// combination sum_k omega_k uhat_k of its sub-stencil values, so the flux stays
+// conservative. The trust band, per face: where the network puts more than
+// `band` of its weight on sub-stencils that WENO-JS marks as crossing a
+// discontinuity (JS weight below `tau`), or moves any weight more than `dev`
+// away from the WENO-JS weight, that face uses the plain WENO-JS weights.
 //
-// Inference runs on the tensor cores: each warp evaluates 16 faces at a time
+// Inference runs on the tensor cores: each warp evaluates 32 cells at a time
 // with mma.sync m16n8k16 (bf16 inputs, fp32 accumulate); the layer outputs stay
 // in registers and feed the next layer's A fragments directly. Training uses a
 // per-thread fp32 forward/backward (learned.cu).
@@ -59,46 +65,48 @@ __device__ __forceinline__ void mlp_normalise(const float s[5], float x[5]) {
     for (int k = 0; k < 5; ++k) x[k] = (s[k] - m) * inv;
 }
 
-// sub-stencil values at the right face (weno.py:231-239)
-__device__ __forceinline__ void mlp_substencils(const float s[5], float uh[3]) {
-    uh[0] = (2.0f * s[0] - 7.0f * s[1] + 11.0f * s[2]) * (1.0f / 6.0f);
-    uh[1] = (-s[1] + 5.0f * s[2] + 2.0f * s[3]) * (1.0f / 6.0f);
-    uh[2] = (2.0f * s[2] + 5.0f * s[3] - s[4]) * (1.0f / 6.0f);
+// WENO-JS5 smoothness indicators of the three sub-stencils of a cell
+// (weno.py:247-256) and the two second/first differences of each
+__device__ __forceinline__ void js_betas(const float s[5], float be[3], float q[6]) {
+    q[0] = s[0] - 2.0f * s[1] + s[2]; q[1] = s[0] - 4.0f * s[1] + 3.0f * s[2];
+    q[2] = s[1] - 2.0f * s[2] + s[3]; q[3] = s[1] - s[3];
+    q[4] = s[2] - 2.0f * s[3] + s[4]; q[5] = 3.0f * s[2] - 4.0f * s[3] + s[4];
+#pragma unroll
+    for (int l = 0; l < 3; ++l)
+        be[l] = (13.0f / 12.0f) * q[2 * l] * q[2 * l] + 0.25f * q[2 * l + 1] * q[2 * l + 1];
 }
 
-// WENO-JS5 weights of the right face (weno.py:247-256), fp32
-__device__ __forceinline__ void js_weights_f32(const float s[5], float eps, float w[3]) {
-    const float q10 = s[0] - 2.0f * s[1] + s[2], q20 = s[0] - 4.0f * s[1] + 3.0f * s[2];
-    const float q11 = s[1] - 2.0f * s[2] + s[3], q21 = s[1] - s[3];
-    const float q12 = s[2] - 2.0f * s[3] + s[4], q22 = 3.0f * s[2] - 4.0f * s[3] + s[4];
-    const float b0 = (13.0f / 12.0f) * q10 * q10 + 0.25f * q20 * q20;
-    const float b1 = (13.0f / 12.0f) * q11 * q11 + 0.25f * q21 * q21;
-    const float b2 = (13.0f / 12.0f) * q12 * q12 + 0.25f * q22 * q22;
-    const float e0 = eps + b0, e1 = eps + b1, e2 = eps + b2;
-    const float a0 = 0.1f / (e0 * e0), a1 = 0.6f / (e1 * e1), a2 = 0.3f / (e2 * e2);
-    const float inv = 1.0f / (a0 + a1 + a2);
-    w[0] = a0 * inv;
-    w[1] = a1 * inv;
-    w[2] = a2 * inv;
+// WENO-JS5 weights of the right face (d = (1, 6, 3)/10 on beta_k) and of the
+// mirrored left face (d_k on beta_{2-k}) from the cell's indicators
+__device__ __forceinline__ void js_weights_pair(const float be[3], float eps, float wr[3],
+                                                float wl[3]) {
+    const float e0 = eps + be[0], e1 = eps + be[1], e2 = eps + be[2];
+    const float r0 = 1.0f / (e0 * e0), r1 = 1.0f / (e1 * e1), r2 = 1.0f / (e2 * e2);
+    const float a1 = 0.6f * r1;
+    const float ir = 1.0f / fmaf(0.1f, r0, fmaf(0.3f, r2, a1));
+    const float il = 1.0f / fmaf(0.1f, r2, fmaf(0.3f, r0, a1));
+    wr[0] = 0.1f * r0 * ir; wr[1] = a1 * ir; wr[2] = 0.3f * r2 * ir;
+    wl[0] = 0.1f * r2 * il; wl[1] = a1 * il; wl[2] = 0.3f * r0 * il;
 }
 
-// face value from network logits z, with the JS trust band
-__device__ __forceinline__ float learned_face(const float s[5], float z0, float z1, float z2,
-                                              const LearnedParams& lp) {
-    const float zm = fmaxf(fmaxf(z0, z1), z2);
-    const float e0 = __expf(z0 - zm), e1 = __expf(z1 - zm), e2 = __expf(z2 - zm);
-    const float inv = 1.0f / (e0 + e1 + e2);
-    float w[3] = {e0 * inv, e1 * inv, e2 * inv};
-    float wj[3];
-    js_weights_f32(s, lp.eps, wj);
-    if (outside_band(w, wj, lp)) {
-        w[0] = wj[0];
-        w[1] = wj[1];
-        w[2] = wj[2];
-    }
-    float uh[3];
-    mlp_substencils(s, uh);
-    return w[0] * uh[0] + w[1] * uh[1] + w[2] * uh[2];
+// sub-stencil values minus the cell value, right and left face, from the
+// stencil shifted by the cell value (ds[2] = 0)
+__device__ __forceinline__ void cell_substencils(const float ds[5], float ur[3], float ul[3]) {
+    ur[0] = (2.0f * ds[0] - 7.0f * ds[1]) * (1.0f / 6.0f);
+    ur[1] = (2.0f * ds[3] - ds[1]) * (1.0f / 6.0f);
+    ur[2] = (5.0f * ds[3] - ds[4]) * (1.0f / 6.0f);
+    ul[0] = (2.0f * ds[4] - 7.0f * ds[3]) * (1.0f / 6.0f);
+    ul[1] = (2.0f * ds[1] - ds[3]) * (1.0f / 6.0f);
+    ul[2] = (5.0f * ds[1] - ds[0]) * (1.0f / 6.0f);
+}
+
+// right- and left-face weights from the exponentials e_k = exp(z_k - max z)
+__device__ __forceinline__ void cell_softmax(float e0, float e1, float e2, float wr[3], float wl[3]) {
+    const float ir = __frcp_rn(e0 + e1 + e2);
+    wr[0] = e0 * ir; wr[1] = e1 * ir; wr[2] = e2 * ir;
+    const float l0 = e2 * (1.0f / 3.0f), l2 = 3.0f * e0;
+    const float il = __frcp_rn(l0 + e1 + l2);
+    wl[0] = l0 * il; wl[1] = e1 * il; wl[2] = l2 * il;
 }
 
 // ---- tensor-core inference --------------------------------------------------
@@ -116,12 +124,6 @@ __device__ __forceinline__ void mma_bf16(float& d0, float& d1, float& d2, float&
         "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
         : "+f"(d0), "+f"(d1), "+f"(d2), "+f"(d3)
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-__device__ __forceinline__ float tanh_fast(float x) {
-    float y;
-    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
 }
 
 // B fragments of the three layers for this lane (g = lane/4, t = lane%4):
@@ -170,79 +172,13 @@ __device__ __forceinline__ void mlp_load_frags(const float* __restrict__ P, MlpF
     f.b3[1] = (2 * t + 1 < kMlpOut) ? P[kOffB3 + 2 * t + 1] : 0.0f;
 }
 
-// Logits of 16 faces (rows g and g+8 of this lane's group). xg / xg8: the
-// normalised stencils of rows g and g+8 (every lane of the group passes its
-// rows). Returns, in every lane, the logits (z0, z1, z2) of row g (zr) and of
-// row g+8 (zs), gathered from the accumulator layout by shuffles.
-__device__ __forceinline__ void mlp_mma_logits(const MlpFrags& f, const float xg[5],
-                                               const float xg8[5], float zr[3], float zs[3]) {
-    const int lane = threadIdx.x & 31, t = lane & 3;
-    // layer-1 A fragment: columns 2t, 2t+1 (and 2t+8.. = 0): x0..x4, 1 (bias), 0
-    auto col = [&](const float x[5], int c) -> float {
-        return c < kMlpIn ? x[c] : (c == kMlpIn ? 1.0f : 0.0f);
-    };
-    const uint32_t a0 = pack_bf16(col(xg, 2 * t), col(xg, 2 * t + 1));
-    const uint32_t a1 = pack_bf16(col(xg8, 2 * t), col(xg8, 2 * t + 1));
-    float h[4][4];
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        h[nt][0] = h[nt][1] = h[nt][2] = h[nt][3] = 0.0f;
-        mma_bf16(h[nt][0], h[nt][1], h[nt][2], h[nt][3], a0, a1, 0u, 0u, f.w1[nt][0], f.w1[nt][1]);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) h[nt][i] = tanh_fast(h[nt][i]);
-    }
-    // layer 2: A (16 x 32) from the layer-1 accumulators, 2 k-tiles
-    uint32_t A2[2][4];
-#pragma unroll
-    for (int kt = 0; kt < 2; ++kt) {
-        A2[kt][0] = pack_bf16(h[2 * kt][0], h[2 * kt][1]);
-        A2[kt][1] = pack_bf16(h[2 * kt][2], h[2 * kt][3]);
-        A2[kt][2] = pack_bf16(h[2 * kt + 1][0], h[2 * kt + 1][1]);
-        A2[kt][3] = pack_bf16(h[2 * kt + 1][2], h[2 * kt + 1][3]);
-    }
-    float q[4][4];
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        q[nt][0] = q[nt][2] = f.b2[nt][0];
-        q[nt][1] = q[nt][3] = f.b2[nt][1];
-#pragma unroll
-        for (int kt = 0; kt < 2; ++kt)
-            mma_bf16(q[nt][0], q[nt][1], q[nt][2], q[nt][3], A2[kt][0], A2[kt][1], A2[kt][2],
-                     A2[kt][3], f.w2[nt][kt][0], f.w2[nt][kt][1]);
-#pragma unroll
-        for (int i = 0; i < 4; ++i) q[nt][i] = tanh_fast(q[nt][i]);
-    }
-    uint32_t A3[2][4];
-#pragma unroll
-    for (int kt = 0; kt < 2; ++kt) {
-        A3[kt][0] = pack_bf16(q[2 * kt][0], q[2 * kt][1]);
-        A3[kt][1] = pack_bf16(q[2 * kt][2], q[2 * kt][3]);
-        A3[kt][2] = pack_bf16(q[2 * kt + 1][0], q[2 * kt + 1][1]);
-        A3[kt][3] = pack_bf16(q[2 * kt + 1][2], q[2 * kt + 1][3]);
-    }
-    float z0 = f.b3[0], z1 = f.b3[1], z2 = f.b3[0], z3 = f.b3[1];
-#pragma unroll
-    for (int kt = 0; kt < 2; ++kt)
-        mma_bf16(z0, z1, z2, z3, A3[kt][0], A3[kt][1], A3[kt][2], A3[kt][3], f.w3[kt][0],
-                 f.w3[kt][1]);
-    // lane t=0 of the group holds (row g: z[0], z[1]; row g+8: z[0], z[1]),
-    // lane t=1 holds (row g: z[2], pad; row g+8: z[2], pad)
-    const int base = lane & ~3;
-    zr[0] = __shfl_sync(0xffffffffu, z0, base);
-    zr[1] = __shfl_sync(0xffffffffu, z1, base);
-    zr[2] = __shfl_sync(0xffffffffu, z0, base + 1);
-    zs[0] = __shfl_sync(0xffffffffu, z2, base);
-    zs[1] = __shfl_sync(0xffffffffu, z3, base);
-    zs[2] = __shfl_sync(0xffffffffu, z2, base + 1);
-}
-
-// ---- 32 faces per warp iteration ---------------------------------------------
-// Lane (g, t) owns one face: row g (t = 0) / g+8 (t = 1) of m16 tile A, row g
+// ---- 32 cells per warp iteration ----------------------------------------------
+// Lane (g, t) owns one cell: row g (t = 0) / g+8 (t = 1) of m16 tile A, row g
 // (t = 2) / g+8 (t = 3) of tile B. The owner holds its stencil *shifted by the
-// cell value* (ds_k = s_k - s_2: the weights are shift-invariant and the face
+// cell value* (ds_k = s_k - s_2: the weights are shift-invariant and a face
 // value is s_2 + sum_k omega_k (uhat_k - s_2), so float differences serve
 // float and double states alike), computes its normalised input, and at the
-// end its face correction. The A fragments of both tiles are gathered by
+// end both face corrections. The A fragments of both tiles are gathered by
 // shuffles; hidden layers apply tanh to packed bf16 pairs (tanh.approx.bf16x2),
 // which are exactly the next layer's A fragments.
 
@@ -280,12 +216,12 @@ __device__ __forceinline__ void mlp_tile(const MlpFrags& f, uint32_t a0, uint32_
         mma_bf16(z0, z1, z2, z3, A3[kt][0], A3[kt][1], A3[kt][2], A3[kt][3], f.w3[kt][0], f.w3[kt][1]);
 }
 
-// The face correction sum_k omega_k (uhat_k - s_2) of this lane's face from its
-// shifted stencil ds (ds[2] = 0), with the WENO-JS trust band. All 32 lanes
-// must call it (shuffles); `valid` only masks nothing -- every lane passes a
-// finite stencil.
-__device__ __forceinline__ float learned_delta32(const MlpFrags& f, const float ds[5],
-                                                 const LearnedParams& lp) {
+// The face corrections sum_k omega_k (uhat_k - s_2) of this lane's cell (right
+// face cr, left face cl) from its shifted stencil ds (ds[2] = 0), with the
+// WENO-JS trust band per face. All 32 lanes must call it (shuffles) with
+// finite stencils.
+__device__ __forceinline__ void learned_cell32(const MlpFrags& f, const float ds[5],
+                                               const LearnedParams& lp, float& cr, float& cl) {
     const int lane = threadIdx.x & 31, t = lane & 3, base = lane & ~3;
     // normalised input and its packed column pairs (x0,x1) (x2,x3) (x4,1)
     float x[5];
@@ -316,29 +252,27 @@ __device__ __forceinline__ float learned_delta32(const MlpFrags& f, const float 
     else if (t == 1) { z0 = u2; z1 = u3; z2 = w1; }
     else if (t == 2) { z0 = v0; z1 = v1; z2 = y0; }
     else { z0 = v2; z1 = v3; z2 = y1; }
-    // softmax, trust band, correction
+    // softmax of both faces, trust band, corrections
     const float zm = fmaxf(fmaxf(z0, z1), z2);
-    const float e0 = __expf(z0 - zm), e1 = __expf(z1 - zm), e2 = __expf(z2 - zm);
-    const float inv = __frcp_rn(e0 + e1 + e2);
-    float w[3] = {e0 * inv, e1 * inv, e2 * inv};
-    float wj[3];
-    js_weights_f32(ds, lp.eps, wj);
-    if (outside_band(w, wj, lp)) {
-        w[0] = wj[0];
-        w[1] = wj[1];
-        w[2] = wj[2];
-    }
-    float uh[3];
-    mlp_substencils(ds, uh);  // uhat_k - s_2 (ds[2] = 0)
-    return w[0] * uh[0] + w[1] * uh[1] + w[2] * uh[2];
+    float wr[3], wl[3];
+    cell_softmax(__expf(z0 - zm), __expf(z1 - zm), __expf(z2 - zm), wr, wl);
+    float be[3], q[6], jr[3], jl[3];
+    js_betas(ds, be, q);
+    js_weights_pair(be, lp.eps, jr, jl);
+    if (outside_band(wr, jr, lp)) { wr[0] = jr[0]; wr[1] = jr[1]; wr[2] = jr[2]; }
+    if (outside_band(wl, jl, lp)) { wl[0] = jl[0]; wl[1] = jl[1]; wl[2] = jl[2]; }
+    float hr[3], hl[3];
+    cell_substencils(ds, hr, hl);
+    cr = wr[0] * hr[0] + wr[1] * hr[1] + wr[2] * hr[2];
+    cl = wl[0] * hl[0] + wl[1] * hl[1] + wl[2] * hl[2];
 }
 
-// ---- backward of one learned face value (adjoint) ----------------------------
+// ---- backward of the two learned face values of a cell (adjoint) -------------
 // Wr: the parameters with the weights rounded to bfloat16 exactly as the
 // tensor-core forward uses them (layer-2/3 biases stay fp32), staged in shared
-// memory by learned_stage_params. The forward is recomputed per face in fp32
+// memory by learned_stage_params. The forward is recomputed per cell in fp32
 // with the same roundings of inputs and activations and the same tanh/exp
-// approximations, so the value differentiated is the one the flux kernel
+// approximations, so the values differentiated are the ones the flux kernel
 // produced; roundings pass the cotangent straight through. max/min of the
 // normalisation split the cotangent evenly at ties (torch/JAX convention).
 
@@ -353,35 +287,23 @@ __device__ __forceinline__ void learned_stage_params(const float* __restrict__ P
     }
 }
 
-// d(face value)/d(stencil) scaled by ub; returns ds[5]. The stencil may be
-// passed shifted by any constant (the face value moves with it, the weights do
-// not), so callers pass differences to the cell value as the forward does.
 __device__ __forceinline__ float bf16_tanh(float x) {
     const uint32_t y = tanh_bf16x2(pack_bf16(x, 0.0f));
     return __uint_as_float(y << 16);
 }
 
-__device__ __forceinline__ void learned_face_vjp(const float s_in[5], float ub, const float* Wr,
-                                                 const LearnedParams& lp, float ds[5]) {
-    float s[5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) s[k] = s_in[k] - s_in[2];
-    float uh[3];
-    mlp_substencils(s, uh);
-    // WENO-JS weights and fallback decision (as learned_face)
-    const float q10 = s[0] - 2.0f * s[1] + s[2], q20 = s[0] - 4.0f * s[1] + 3.0f * s[2];
-    const float q11 = s[1] - 2.0f * s[2] + s[3], q21 = s[1] - s[3];
-    const float q12 = s[2] - 2.0f * s[3] + s[4], q22 = 3.0f * s[2] - 4.0f * s[3] + s[4];
-    const float be[3] = {(13.0f / 12.0f) * q10 * q10 + 0.25f * q20 * q20,
-                         (13.0f / 12.0f) * q11 * q11 + 0.25f * q21 * q21,
-                         (13.0f / 12.0f) * q12 * q12 + 0.25f * q22 * q22};
-    float wj[3];
-    {
-        const float e0 = lp.eps + be[0], e1 = lp.eps + be[1], e2 = lp.eps + be[2];
-        const float a0 = 0.1f / (e0 * e0), a1 = 0.6f / (e1 * e1), a2 = 0.3f / (e2 * e2);
-        const float inv = 1.0f / (a0 + a1 + a2);
-        wj[0] = a0 * inv; wj[1] = a1 * inv; wj[2] = a2 * inv;
-    }
+// gR d(u_R)/ds + gL d(u_L)/ds of the cell's right and left face values with
+// respect to its stencil s = v_{c-2..c+2}; callers pass s shifted by the cell
+// value as the forward does (ds[2] = 0; the gradient of a shift-equivariant
+// value does not depend on the shift). Returns dsum[5].
+__device__ __forceinline__ void learned_cell_vjp(const float s[5], float gR, float gL,
+                                                 const float* Wr, const LearnedParams& lp,
+                                                 float dsum[5]) {
+    float hr[3], hl[3];
+    cell_substencils(s, hr, hl);
+    float be[3], q[6], jr[3], jl[3];
+    js_betas(s, be, q);
+    js_weights_pair(be, lp.eps, jr, jl);
     // network forward with the inference roundings
     float x[5];
     mlp_normalise(s, x);
@@ -408,38 +330,55 @@ __device__ __forceinline__ void learned_face_vjp(const float s_in[5], float ub, 
         z[o] = acc;
     }
     const float zm = fmaxf(fmaxf(z[0], z[1]), z[2]);
-    const float e0 = __expf(z[0] - zm), e1 = __expf(z[1] - zm), e2 = __expf(z[2] - zm);
-    const float einv = 1.0f / (e0 + e1 + e2);
-    const float w[3] = {e0 * einv, e1 * einv, e2 * einv};
-    const bool fallback = outside_band(w, wj, lp);
-    const float* wt = fallback ? wj : w;
-    // direct part: sum_k omega_k d uhat_k / ds (6 uhat taps: (2,-7,11,0,0) (0,-1,5,2,0) (0,0,2,5,-1))
-    const float c6 = ub * (1.0f / 6.0f);
-    ds[0] = c6 * (2.0f * wt[0]);
-    ds[1] = c6 * (-7.0f * wt[0] - wt[1]);
-    ds[2] = c6 * (11.0f * wt[0] + 5.0f * wt[1] + 2.0f * wt[2]);
-    ds[3] = c6 * (2.0f * wt[1] + 5.0f * wt[2]);
-    ds[4] = c6 * (-wt[2]);
-    const float u = wt[0] * uh[0] + wt[1] * uh[1] + wt[2] * uh[2];
-    if (fallback) {
-        // d u / d beta_l = -2 omega_l (uhat_l - u) / (eps + beta_l)
-        float bb[3];
-        for (int l = 0; l < 3; ++l) bb[l] = -2.0f * ub * wj[l] * (uh[l] - u) / (lp.eps + be[l]);
+    float wr[3], wl[3];
+    cell_softmax(__expf(z[0] - zm), __expf(z[1] - zm), __expf(z[2] - zm), wr, wl);
+    const bool fbr = outside_band(wr, jr, lp), fbl = outside_band(wl, jl, lp);
+    const float* tr = fbr ? jr : wr;
+    const float* tl = fbl ? jl : wl;
+    // direct parts: sum_k omega_k d uhat_k / ds; 6 uhat taps, right face
+    // (2,-7,11,0,0) (0,-1,5,2,0) (0,0,2,5,-1), left face mirrored
+    const float cR = gR * (1.0f / 6.0f), cL = gL * (1.0f / 6.0f);
+    dsum[0] = cR * (2.0f * tr[0]) - cL * tl[2];
+    dsum[1] = cR * (-7.0f * tr[0] - tr[1]) + cL * (2.0f * tl[1] + 5.0f * tl[2]);
+    dsum[2] = cR * (11.0f * tr[0] + 5.0f * tr[1] + 2.0f * tr[2]) +
+              cL * (11.0f * tl[0] + 5.0f * tl[1] + 2.0f * tl[2]);
+    dsum[3] = cR * (2.0f * tr[1] + 5.0f * tr[2]) + cL * (-7.0f * tl[0] - tl[1]);
+    dsum[4] = -cR * tr[2] + cL * (2.0f * tl[0]);
+    const float uR = tr[0] * hr[0] + tr[1] * hr[1] + tr[2] * hr[2];
+    const float uL = tl[0] * hl[0] + tl[1] * hl[1] + tl[2] * hl[2];
+    if (fbr || fbl) {
+        // WENO-JS faces: d u / d beta_l = -2 omega_l (uhat_l - u) / (eps + beta_l);
+        // the left face's sub-stencil k sees beta_{2-k}
+        float bb[3] = {0.0f, 0.0f, 0.0f};
+        if (fbr)
+            for (int l = 0; l < 3; ++l) bb[l] += -2.0f * gR * jr[l] * (hr[l] - uR) / (lp.eps + be[l]);
+        if (fbl)
+            for (int k = 0; k < 3; ++k)
+                bb[2 - k] += -2.0f * gL * jl[k] * (hl[k] - uL) / (lp.eps + be[2 - k]);
         // d beta_l / ds = 13/6 q1_l dq1_l + 1/2 q2_l dq2_l
-        const float a0 = (13.0f / 6.0f) * q10 * bb[0], c0 = 0.5f * q20 * bb[0];
-        const float a1 = (13.0f / 6.0f) * q11 * bb[1], c1 = 0.5f * q21 * bb[1];
-        const float a2 = (13.0f / 6.0f) * q12 * bb[2], c2 = 0.5f * q22 * bb[2];
-        ds[0] += a0 + c0;
-        ds[1] += -2.0f * a0 - 4.0f * c0 + a1 + c1;
-        ds[2] += a0 + 3.0f * c0 - 2.0f * a1 + a2 + 3.0f * c2;
-        ds[3] += a1 - c1 - 2.0f * a2 - 4.0f * c2;
-        ds[4] += a2 + c2;
-        return;
+        const float a0 = (13.0f / 6.0f) * q[0] * bb[0], c0 = 0.5f * q[1] * bb[0];
+        const float a1 = (13.0f / 6.0f) * q[2] * bb[1], c1 = 0.5f * q[3] * bb[1];
+        const float a2 = (13.0f / 6.0f) * q[4] * bb[2], c2 = 0.5f * q[5] * bb[2];
+        dsum[0] += a0 + c0;
+        dsum[1] += -2.0f * a0 - 4.0f * c0 + a1 + c1;
+        dsum[2] += a0 + 3.0f * c0 - 2.0f * a1 + a2 + 3.0f * c2;
+        dsum[3] += a1 - c1 - 2.0f * a2 - 4.0f * c2;
+        dsum[4] += a2 + c2;
+        if (fbr && fbl) return;
     }
-    // softmax and network backward (input gradient only)
-    const float dw0 = ub * uh[0], dw1 = ub * uh[1], dw2 = ub * uh[2];
-    const float dot = w[0] * dw0 + w[1] * dw1 + w[2] * dw2;
-    const float dz[3] = {w[0] * (dw0 - dot), w[1] * (dw1 - dot), w[2] * (dw2 - dot)};
+    // softmax backward of the network faces into the shared logits: right
+    // omega = softmax(z); left omega = softmax(z2 - ln 3, z1, z0 + ln 3)
+    float dz[3] = {0.0f, 0.0f, 0.0f};
+    if (!fbr) {
+        const float d0 = gR * hr[0], d1 = gR * hr[1], d2 = gR * hr[2];
+        const float dot = wr[0] * d0 + wr[1] * d1 + wr[2] * d2;
+        dz[0] += wr[0] * (d0 - dot); dz[1] += wr[1] * (d1 - dot); dz[2] += wr[2] * (d2 - dot);
+    }
+    if (!fbl) {
+        const float d0 = gL * hl[0], d1 = gL * hl[1], d2 = gL * hl[2];
+        const float dot = wl[0] * d0 + wl[1] * d1 + wl[2] * d2;
+        dz[2] += wl[0] * (d0 - dot); dz[1] += wl[1] * (d1 - dot); dz[0] += wl[2] * (d2 - dot);
+    }
     float da2[kMlpH];
     for (int k = 0; k < kMlpH; ++k) {
         const float dh = Wr[kOffW3 + k] * dz[0] + Wr[kOffW3 + kMlpH + k] * dz[1] +
@@ -473,9 +412,8 @@ __device__ __forceinline__ void learned_face_vjp(const float s_in[5], float ub, 
     for (int k = 0; k < 5; ++k) {
         float d = inv * (dx[k] - 0.2f * sdx);
         d += gr * ((s[k] == hi ? 1.0f / nhi : 0.0f) - (s[k] == lo ? 1.0f / nlo : 0.0f));
-        ds[k] += d;
+        dsum[k] += d;
     }
 }
 
 }  // namespace shk
-

@@ -58,13 +58,12 @@ struct OpParams {
     T fscale;              // face values F are stored as F / fscale (see face_fluxes)
 };
 
-// learned reconstruction of cells [clo, chi): two faces per cell, one face per
-// lane, 32 faces per warp iteration (face 2j: right face of cell clo+j with
-// stencil v_{c-2..c+2}; face 2j+1: left face, mirrored stencil). The cell
+// learned reconstruction of cells [clo, chi): one cell per lane, 32 cells per
+// warp iteration, both faces of a cell from one network evaluation. The cell
 // differences d_k = v_{k+1} - v_k are formed once, in the state precision, and
-// stored as float in `dbuf`; a face's stencil relative to v_c is a float sum of
-// them, and the face value is v_c + correction in the state precision, so
-// double states spend two double operations per face here.
+// stored as float in `dbuf`; a cell's stencil relative to v_c is a float sum
+// of them, and the face values are v_c + correction in the state precision, so
+// double states spend three double operations per cell here.
 template <class T>
 __device__ __forceinline__ void learned_phase(const T* v, int clo, int chi, T* UL, T* UR,
                                               float* dbuf, const LearnedParams& lp) {
@@ -75,24 +74,21 @@ __device__ __forceinline__ void learned_phase(const T* v, int clo, int chi, T* U
     __syncthreads();
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int ncell = chi - clo, rows = 2 * ncell;
-    const int myrow = 16 * (t >> 1) + 8 * (t & 1) + g;  // within the 32-face block
-    for (int q = warp; q * 32 < rows; q += nw) {
+    const int ncell = chi - clo;
+    const int myrow = 16 * (t >> 1) + 8 * (t & 1) + g;  // within the 32-cell block
+    for (int q = warp; q * 32 < ncell; q += nw) {
         const int r = q * 32 + myrow;
-        const bool valid = r < rows;
-        const int c = clo + min(r >> 1, ncell - 1);
-        const int side = r & 1;  // 0: right face (ur), 1: left face (ul)
+        const int c = clo + min(r, ncell - 1);
         const float dm2 = dbuf[c - 2], dm1 = dbuf[c - 1], d0 = dbuf[c], dp1 = dbuf[c + 1];
-        // v_{c+o} - v_c for o = -2..2, then mirrored for the left face
-        const float lo2 = -(dm1 + dm2), lo1 = -dm1, hi1 = d0, hi2 = d0 + dp1;
-        float ds[5];
-        if (side) {
-            ds[0] = hi2; ds[1] = hi1; ds[2] = 0.0f; ds[3] = lo1; ds[4] = lo2;
-        } else {
-            ds[0] = lo2; ds[1] = lo1; ds[2] = 0.0f; ds[3] = hi1; ds[4] = hi2;
+        // v_{c+o} - v_c for o = -2..2
+        const float ds[5] = {-(dm1 + dm2), -dm1, 0.0f, d0, d0 + dp1};
+        float cr, cl;
+        learned_cell32(f, ds, lp, cr, cl);
+        if (r < ncell) {
+            const T vc = v[c];
+            UR[c] = vc + static_cast<T>(cr);
+            UL[c] = vc + static_cast<T>(cl);
         }
-        const float d = learned_delta32(f, ds, lp);
-        if (valid) (side ? UL : UR)[c] = v[c] + static_cast<T>(d);
     }
 }
 

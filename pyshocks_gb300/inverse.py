@@ -27,6 +27,7 @@ class InverseProblem:
     :arg nsteps: SSPRK33 steps of every forward solve.
     :arg bounds: box constraint of the projected update (``(0, 1)`` for
         densities).
+    :arg lr: gradient step (the misfit is an unweighted sum over cells).
     """
 
     def __init__(self, scheme, sizes, dx, nsteps: int, *, dtype=torch.float32,
@@ -41,8 +42,10 @@ class InverseProblem:
         self.obs = torch.zeros_like(self.u0)
         self.J = torch.zeros(self.solver.B, dtype=torch.float64, device=dev)
         self.bounds = bounds
-        # gradient steps scale with the cell size (dJ/du0 ~ dx for cell averages)
-        self.lr = lr / torch.tensor(np.asarray(self.solver.dx), dtype=dtype, device=dev)[self.inst]
+        # J is a plain sum over cells and the solution operator is close to a
+        # transport (norm-preserving away from shocks), so dJ/du0 is O(residual)
+        # and a step of lr ~ 1 is the natural scale
+        self.lr = float(lr)
         self.graph = None
 
     def forward(self, u0: torch.Tensor) -> torch.Tensor:

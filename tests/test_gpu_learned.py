@@ -49,17 +49,21 @@ def test_tensor_core_faces_match_oracle(band, dev):
     from pyshocks_gb300 import learned
 
     params = learned.init_params(seed=3)
-    s = _stencils(4099, 1)  # not a multiple of 16: ragged last warp tile
+    s = _stencils(4099, 1)  # not a multiple of 32: ragged last warp block
     got = learned.face_values(_scheme(params, band=band, dev=dev), s.float().cuda()).double().cpu()
-    ref, fb = LR.face_value(params.double().cpu(), s.float().double(), eps=1.0e-6, tau=1.0e-2,
-                            band=band, dev=dev, bf16=True, return_fallback=True)
+    (vr, vl), (fr, fl) = LR.cell_face_values(params.double().cpu(), s.float().double(), eps=1.0e-6,
+                                             tau=1.0e-2, band=band, dev=dev, bf16=True,
+                                             return_fallback=True)
     rng = (s.amax(-1) - s.amin(-1))
-    err = (got - ref).abs() / (rng + 1e-30)
-    # faces whose fallback decision sits on the edge of the band may flip
-    ok = err < 5.0e-3
-    assert ok.float().mean() > 0.995, float(err.max())
+    for col, ref in ((0, vr), (1, vl)):
+        err = (got[:, col] - ref).abs() / (rng + 1e-30)
+        # faces whose fallback decision sits on the edge of the band may flip
+        ok = err < 5.0e-3
+        assert ok.float().mean() > 0.995, (col, float(err.max()))
     if band > 1.5:
-        assert not bool(fb.any())
+        assert not bool(fr.any() or fl.any())
+    else:
+        assert bool(fr.any() and fl.any()) and not bool(fr.all())
 
 
 def test_loss_grad_kernel_matches_autograd():
@@ -67,10 +71,11 @@ def test_loss_grad_kernel_matches_autograd():
 
     params = learned.init_params(seed=5)
     s = _stencils(3001, 2)
-    t = s[:, 2] + 0.1 * torch.randn(3001, generator=torch.Generator().manual_seed(4), dtype=torch.float64)
+    g = torch.Generator().manual_seed(4)
+    t = s[:, 2:3] + 0.1 * torch.randn(3001, 2, generator=g, dtype=torch.float64)
     w = 1.0 / (s.amax(-1) - s.amin(-1) + 1e-3) ** 2
     tr = learned.Trainer(params.clone(), reg=0.3)
-    loss = float(tr.loss_and_grad(s.float().cuda(), t.float().cuda(), w.float().cuda()))
+    loss = float(tr.loss_and_grad(s.float().cuda(), t.float().cuda().contiguous(), w.float().cuda()))
     grad = tr.grad.double().cpu()
     p64 = params.double().cpu().requires_grad_(True)
     lref = LR.training_loss(p64, s.float().double(), t.float().double(), w.float().double(),
@@ -90,7 +95,7 @@ def test_training_reduces_loss():
     l0 = float(tr.loss_and_grad(s, t, w))
     hist = tr.fit(s, t, w, epochs=20, batch=2048)
     l1 = float(tr.loss_and_grad(s, t, w))
-    assert l1 < 0.7 * l0, (l0, l1, hist[-3:])
+    assert l1 < 0.8 * l0, (l0, l1, hist[-3:])
 
 
 def test_learned_batched_step_matches_oracle():
