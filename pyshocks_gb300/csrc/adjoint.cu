@@ -45,23 +45,21 @@ struct AdjSmem {
     T *H, *D, *Q, *UL, *UR;
     T *GL, *GR, *GA;
     T *T0, *T1, *T2, *T3, *T4;
+    int W;  // window length (cells) of every array
 
-    float* Wr;  // learned reconstruction: bf16-rounded parameters
-
-    __host__ static size_t host_bytes(int W) {
-        return size_t(kAdjArrays) * W * sizeof(T) + sizeof(float) * ((kMlpParams + 3) & ~3);
-    }
+    __host__ static size_t host_bytes(int W) { return size_t(kAdjArrays) * W * sizeof(T); }
     __device__ void carve(unsigned char* base, int W) {
         T* p = reinterpret_cast<T*>(base);
         T** slots[kAdjArrays] = {&U, &K1, &K2, &PB, &CB, &Z, &ACC, &H, &D, &Q,
                                  &UL, &UR, &GL, &GR, &GA, &T0, &T1, &T2, &T3, &T4};
         for (int i = 0; i < kAdjArrays; ++i) *slots[i] = p + size_t(i) * W;
-        Wr = reinterpret_cast<float*>(p + size_t(kAdjArrays) * W);
+        this->W = W;
     }
     // forward-stage view (face_fluxes writes the face fluxes into D)
     __device__ Smem<T> fwd(T* state_out) const {
         Smem<T> s;
         s.U = U; s.S = state_out; s.H = H; s.D = D; s.Q = Q; s.UL = UL; s.UR = UR;
+        s.W = W;
         return s;
     }
 };
@@ -213,24 +211,38 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
         a.GA[j] = -(fb * p.hnu) * (L - R);
     }
     __syncthreads();
-    for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
-        T t0, t1, t2, t3, t4;
-        if constexpr (REC == SHK_REC_LEARNED) {
-            // the cell's stencil relative to v_c from the float cell differences,
-            // as the forward (learned_phase left them in H)
-            const float* db = reinterpret_cast<const float*>(a.H);
+    if constexpr (REC == SHK_REC_LEARNED) {
+        // one cell per lane, 32 cells per warp iteration (tensor-core network
+        // backward); the cell's stencil relative to v_c from the float cell
+        // differences, as the forward (learned_phase left them in H)
+        const float* db = reinterpret_cast<const float*>(a.H);
+        MlpFrags f;
+        mlp_load_frags(p.lp.mlp, f);
+        MlpBackFrags bk;
+        mlp_load_back_frags(p.lp.mlp, bk);
+        const int lane = tid & 31, g = lane >> 2, tq = lane & 3;
+        const int myrow = 16 * (tq >> 1) + 8 * (tq & 1) + g;
+        const int c0 = lo - 2, ncell = hi + 2 - c0;
+        for (int qb = tid >> 5; qb * 32 < ncell; qb += nt >> 5) {
+            const int r = qb * 32 + myrow;
+            const int c = c0 + min(r, ncell - 1);
             const float dm2 = db[c - 2], dm1 = db[c - 1], d0 = db[c], dp1 = db[c + 1];
             const float sc[5] = {-(dm1 + dm2), -dm1, 0.0f, d0, d0 + dp1};
             float dd[5];
-            learned_cell_vjp(sc, static_cast<float>(a.GR[c]), static_cast<float>(a.GL[c - 1]), a.Wr,
-                             p.lp, dd);
-            t0 = dd[0]; t1 = dd[1]; t2 = dd[2]; t3 = dd[3]; t4 = dd[4];
-        } else {
+            learned_cell_vjp32(f, bk, sc, static_cast<float>(a.GR[c]), static_cast<float>(a.GL[c - 1]),
+                               p.lp, dd);
+            if (r < ncell) {
+                a.T0[c] = dd[0]; a.T1[c] = dd[1]; a.T2[c] = dd[2]; a.T3[c] = dd[3]; a.T4[c] = dd[4];
+            }
+        }
+    } else {
+        for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
+            T t0, t1, t2, t3, t4;
             weno53_cell_vjp<T>(a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
                                a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, a.GR[c],
                                a.GL[c - 1], t0, t1, t2, t3, t4);
+            a.T0[c] = t0; a.T1[c] = t1; a.T2[c] = t2; a.T3[c] = t3; a.T4[c] = t4;
         }
-        a.T0[c] = t0; a.T1[c] = t1; a.T2[c] = t2; a.T3[c] = t3; a.T4[c] = t4;
     }
     __syncthreads();
     for (int i = lo + tid; i < hi; i += nt) {
@@ -243,10 +255,82 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
     __syncthreads();
 }
 
+// Adjoint step of the mixed-precision learned step (step_tile_mixed): the
+// forward stages are recomputed exactly as that step computes them (float
+// operator on float stage states, increments about u), the three reverse
+// stages run in float on float copies of u and p, and the result
+//   ub = p + 2/3 Z3 + 1/4 Z2 + Z1
+// (Z_s the stage VJPs dt J^T(.) of the reverse sweep below) adds the float
+// increment to the double p once. Of the double arrays only the loaded windows
+// a.U and a.PB are read; af holds the float arrays (af.K1, af.K2 may overlay
+// a.U, which is dead once af.U is written).
+template <int EQ>
+__device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float>& af, double* gout,
+                                   int te, double dtdx, const OpParams<double>& p) {
+    constexpr int HU = adj_uhalo<double>(), HP = adj_phalo<double>();
+    constexpr int REC = SHK_REC_LEARNED;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const OpParams<float> pf = float_params(p);
+    const float dtf = static_cast<float>(dtdx);
+    for (int i = tid; i < te + 2 * HU; i += nt) af.U[i] = static_cast<float>(a.U[i]);
+    for (int i = HU - HP + tid; i < HU + te + HP; i += nt) af.PB[i] = static_cast<float>(a.PB[i]);
+    __syncthreads();
+    // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12)
+    {
+        const int lo = HU - 15, hi = HU + te + 15;
+        face_fluxes<float, EQ, REC, SHK_FLUX_RUSANOV>(af.U, lo, hi, af.fwd(af.K1), pf);
+        for (int i = lo + tid; i < hi; i += nt) {
+            const float d = dtf * (af.D[i - 1] - af.D[i]);
+            af.T0[i] = d;
+            af.K1[i] = af.U[i] + d;
+        }
+        __syncthreads();
+    }
+    {
+        const int lo = HU - 12, hi = HU + te + 12;
+        face_fluxes<float, EQ, REC, SHK_FLUX_RUSANOV>(af.K1, lo, hi, af.fwd(af.K2), pf);
+        for (int i = lo + tid; i < hi; i += nt) {
+            const float d = 0.25f * (af.T0[i] + dtf * (af.D[i - 1] - af.D[i]));
+            af.K2[i] = af.U[i] + d;
+        }
+        __syncthreads();
+    }
+    // reverse stage 3: k2b = 2/3 (p + Z3), Z3 = dt J(k2)^T p
+    {
+        const int lo = HU - 6, hi = HU + te + 6;
+        vjp_stage<float, EQ, REC>(af.K2, af.PB, af.Z, lo, hi, af, pf, dtf);
+        for (int i = lo + tid; i < hi; i += nt) af.CB[i] = (2.0f / 3.0f) * (af.PB[i] + af.Z[i]);
+        for (int i = HU + tid; i < HU + te; i += nt) af.ACC[i] = (2.0f / 3.0f) * af.Z[i];
+        __syncthreads();
+    }
+    // reverse stage 2: k1b = 1/4 (k2b + Z2), Z2 = dt J(k1)^T k2b
+    {
+        const int lo = HU - 3, hi = HU + te + 3;
+        vjp_stage<float, EQ, REC>(af.K1, af.CB, af.Z, lo, hi, af, pf, dtf);
+        for (int i = HU + tid; i < HU + te; i += nt) af.ACC[i] = fmaf(0.25f, af.Z[i], af.ACC[i]);
+        for (int i = lo + tid; i < hi; i += nt) af.CB[i] = 0.25f * (af.CB[i] + af.Z[i]);
+        __syncthreads();
+    }
+    // reverse stage 1: Z1 = dt J(u)^T k1b; ub = p + (2/3 Z3 + 1/4 Z2 + Z1)
+    {
+        const int lo = HU, hi = HU + te;
+        vjp_stage<float, EQ, REC>(af.U, af.CB, af.Z, lo, hi, af, pf, dtf);
+        for (int i = lo + tid; i < hi; i += nt)
+            gout[i - HU] = a.PB[i] + static_cast<double>(af.ACC[i] + af.Z[i]);
+    }
+}
+
 // one adjoint step of a tile: p_out[s, s+te) from u_m (window, halo 20) and
 // p_next (window, halo 10/12). gout points at p_out + s.
 template <class T, int EQ, int REC>
 __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const OpParams<T>& p) {
+    if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED) {
+        // full double layout: the float arrays fit from CB on (20 in 16 double ones)
+        AdjSmem<float> af;
+        af.carve(reinterpret_cast<unsigned char*>(a.CB), a.W);
+        adjoint_tile_mixed<EQ>(a, af, gout, te, dtdx, p);
+        return;
+    }
     constexpr int HU = adj_uhalo<T>();
     const int tid = threadIdx.x, nt = blockDim.x;
     const T fdt = dtdx * p.fscale;  // face fluxes are stored as F / fscale
@@ -291,6 +375,27 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     }
 }
 
+// compact layout of the mixed-precision learned adjoint (22 float arrays of W):
+// a.U (double, slots 0-1, dead after the float copy, then af.K1/af.K2),
+// a.PB (double, slots 2-3), af.U, af.PB, then the other 16 float arrays
+constexpr int kMixedAdjSlots = 22;
+__device__ inline void carve_mixed(unsigned char* base, int W, AdjSmem<double>& a, AdjSmem<float>& af) {
+    float* f = reinterpret_cast<float*>(base);
+    a.U = reinterpret_cast<double*>(f);
+    a.PB = reinterpret_cast<double*>(f + 2 * W);
+    a.K1 = a.K2 = a.CB = a.Z = a.ACC = a.H = a.D = a.Q = a.UL = a.UR = nullptr;
+    a.GL = a.GR = a.GA = a.T0 = a.T1 = a.T2 = a.T3 = a.T4 = nullptr;
+    a.W = W;
+    af.K1 = f;
+    af.K2 = f + W;
+    af.U = f + 4 * W;
+    af.PB = f + 5 * W;
+    float** rest[] = {&af.CB, &af.Z, &af.ACC, &af.H, &af.D, &af.Q, &af.UL, &af.UR,
+                      &af.GL, &af.GR, &af.GA, &af.T0, &af.T1, &af.T2, &af.T3, &af.T4};
+    for (int i = 0; i < 16; ++i) *rest[i] = f + (6 + i) * W;
+    af.W = W;
+}
+
 template <class T>
 __device__ __forceinline__ bool adjoint_load(const AdjSmem<T>& a, const T* um, const T* pn,
                                              int64_t n, int64_t s0, int te, uint64_t* bar,
@@ -301,16 +406,18 @@ __device__ __forceinline__ bool adjoint_load(const AdjSmem<T>& a, const T* um, c
 }
 
 template <class T, int EQ, int REC>
-__global__ void __launch_bounds__(kThreads) batched_adjoint_kernel(PlanDev P, const T* __restrict__ um,
+__global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batched_adjoint_kernel(PlanDev P, const T* __restrict__ um,
                                                                    const T* __restrict__ pnext,
                                                                    T* __restrict__ pout,
                                                                    const double* __restrict__ dt_row,
                                                                    OpParams<T> p) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
+    constexpr bool kMixed = sizeof(T) == 8 && REC == SHK_REC_LEARNED;
     AdjSmem<T> a;
-    a.carve(smem_raw, P.tile + 2 * adj_uhalo<T>());
-    if constexpr (REC == SHK_REC_LEARNED) learned_stage_params(p.lp.mlp, a.Wr);
+    AdjSmem<float> af;
+    if constexpr (kMixed) carve_mixed(smem_raw, P.tile + 2 * adj_uhalo<T>(), a, af);
+    else a.carve(smem_raw, P.tile + 2 * adj_uhalo<T>());
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_mbar_init();
@@ -334,7 +441,8 @@ __global__ void __launch_bounds__(kThreads) batched_adjoint_kernel(PlanDev P, co
             return;
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
-        adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p);
+        if constexpr (kMixed) adjoint_tile_mixed<EQ>(a, af, pout + off + s0, te, dtdx, p);
+        else adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p);
         __syncthreads();
     }
 }
@@ -342,7 +450,7 @@ __global__ void __launch_bounds__(kThreads) batched_adjoint_kernel(PlanDev P, co
 // forward step with a recorded dt (no CFL, no time update): recompute of the
 // states between checkpoints
 template <class T, int EQ, int REC>
-__global__ void __launch_bounds__(kThreads) replay_step_kernel(PlanDev P, const T* __restrict__ uin,
+__global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) replay_step_kernel(PlanDev P, const T* __restrict__ uin,
                                                                T* __restrict__ uout,
                                                                const double* __restrict__ dt_row,
                                                                OpParams<T> p) {
@@ -573,7 +681,10 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
     const size_t esz = dtype == SHK_F64 ? 8 : 4;
     const size_t bytes = size_t(total) * esz;
     const int W = D.tile + 2 * adj_uhalo<double>();
-    const size_t asmem = dtype == SHK_F64 ? AdjSmem<double>::host_bytes(W) : AdjSmem<float>::host_bytes(W);
+    const bool mixed = dtype == SHK_F64 && sch.rec == SHK_REC_LEARNED;
+    const size_t asmem = mixed ? sizeof(float) * kMixedAdjSlots * size_t(W)
+                               : (dtype == SHK_F64 ? AdjSmem<double>::host_bytes(W)
+                                                   : AdjSmem<float>::host_bytes(W));
     const size_t fsmem = dtype == SHK_F64 ? Smem<double>::host_bytes(D.tile + 2 * step_halo<double>())
                                           : Smem<float>::host_bytes(D.tile + 2 * step_halo<float>());
     // adjoint grid: resident CTAs for its larger shared-memory footprint

@@ -23,6 +23,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -267,71 +268,188 @@ __device__ __forceinline__ void learned_cell32(const MlpFrags& f, const float ds
     cl = wl[0] * hl[0] + wl[1] * hl[1] + wl[2] * hl[2];
 }
 
-// ---- backward of the two learned face values of a cell (adjoint) -------------
-// Wr: the parameters with the weights rounded to bfloat16 exactly as the
-// tensor-core forward uses them (layer-2/3 biases stay fp32), staged in shared
-// memory by learned_stage_params. The forward is recomputed per cell in fp32
-// with the same roundings of inputs and activations and the same tanh/exp
-// approximations, so the values differentiated are the ones the flux kernel
-// produced; roundings pass the cotangent straight through. max/min of the
-// normalisation split the cotangent evenly at ties (torch/JAX convention).
+// ---- backward of the two learned face values of 32 cells (adjoint) ------------
+// The forward is recomputed with the inference's own mma sequence (the same
+// activations, bit for bit), keeping the bf16 hidden activations h1, h2 in
+// their fragment registers. The network backward runs on the tensor cores too:
+// da2 = (dz W3) * (1 - h2^2), da1 = (da2 W2) * (1 - h1^2), dx = da1 W1, as
+// mma.sync m16n8k16 with fp16 operands and fp32 accumulation, the weights
+// being the bf16-rounded ones of the forward (exact in fp16). Each cell's
+// cotangent dz is scaled by a power of two into [1, 2) before the products
+// and dx scaled back (the backward is linear and rows are independent, so the
+// scaling is exact and fp16 neither overflows nor loses small cotangents).
+// Roundings of the forward pass the cotangent straight through; max/min of the
+// normalisation split it evenly at ties (torch/JAX convention).
+
+__device__ __forceinline__ void mma_f16(float& d0, float& d1, float& d2, float& d3, uint32_t a0,
+                                        uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                        uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 "
+        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(d0), "+f"(d1), "+f"(d2), "+f"(d3)
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack_f16(float lo, float hi) {
+    __half2 v = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ float bf16_lo(uint32_t x) { return __uint_as_float(x << 16); }
+__device__ __forceinline__ float bf16_hi(uint32_t x) { return __uint_as_float(x & 0xffff0000u); }
 
 __device__ __forceinline__ float round_bf16(float x) {
     return __bfloat162float(__float2bfloat16_rn(x));
 }
 
-__device__ __forceinline__ void learned_stage_params(const float* __restrict__ P, float* Wr) {
-    for (int i = threadIdx.x; i < kMlpParams; i += blockDim.x) {
-        const bool keep = (i >= kOffB2 && i < kOffW3) || i >= kOffB3;
-        Wr[i] = keep ? P[i] : round_bf16(P[i]);
+// fp16 B fragments of the backward products for this lane (g = lane/4, t = lane%4):
+// B[k][n] with k the contracted index (rows 2t, 2t+1 and 2t+8, 2t+9), n = g
+struct MlpBackFrags {
+    uint32_t w3[4];        // dz W3: k = output (3 of 16), n = hidden (4 n-tiles)
+    uint32_t w2[4][2][2];  // da2 W2: k = layer-2 unit (2 k-tiles), n = layer-1 unit (4 n-tiles)
+    uint32_t w1[2][2];     // da1 W1: k = layer-1 unit (2 k-tiles), n = input (5 of 8)
+};
+
+__device__ __forceinline__ void mlp_load_back_frags(const float* __restrict__ P, MlpBackFrags& b) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    auto h = [](float w) { return round_bf16(w); };
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        const int n = nt * 8 + g;
+        // rows k = 2t, 2t+1 of W3 (k < 3), column n
+        const float w30 = 2 * t < kMlpOut ? h(P[kOffW3 + (2 * t) * kMlpH + n]) : 0.0f;
+        const float w31 = 2 * t + 1 < kMlpOut ? h(P[kOffW3 + (2 * t + 1) * kMlpH + n]) : 0.0f;
+        b.w3[nt] = pack_f16(w30, w31);
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt) {
+            const int k = kt * 16 + 2 * t;
+            b.w2[nt][kt][0] = pack_f16(h(P[kOffW2 + k * kMlpH + n]), h(P[kOffW2 + (k + 1) * kMlpH + n]));
+            b.w2[nt][kt][1] = pack_f16(h(P[kOffW2 + (k + 8) * kMlpH + n]), h(P[kOffW2 + (k + 9) * kMlpH + n]));
+        }
+    }
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt) {
+        const int k = kt * 16 + 2 * t;
+        auto w1 = [&](int kk) { return g < kMlpIn ? h(P[kOffW1 + kk * kMlpIn + g]) : 0.0f; };
+        b.w1[kt][0] = pack_f16(w1(k), w1(k + 1));
+        b.w1[kt][1] = pack_f16(w1(k + 8), w1(k + 9));
     }
 }
 
-__device__ __forceinline__ float bf16_tanh(float x) {
-    const uint32_t y = tanh_bf16x2(pack_bf16(x, 0.0f));
-    return __uint_as_float(y << 16);
+// hidden layers + output of one m16 tile, keeping the bf16 activations
+// (A2 = tanh(h1 pre-activation), A3 = tanh(h2 pre-activation)) in A-fragment layout
+__device__ __forceinline__ void mlp_tile_keep(const MlpFrags& f, uint32_t a0, uint32_t a1,
+                                              uint32_t A2[2][4], uint32_t A3[2][4], float& z0,
+                                              float& z1, float& z2, float& z3) {
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
+        mma_bf16(c0, c1, c2, c3, a0, a1, 0u, 0u, f.w1[nt][0], f.w1[nt][1]);
+        A2[nt >> 1][(nt & 1) * 2 + 0] = tanh_bf16x2(pack_bf16(c0, c1));
+        A2[nt >> 1][(nt & 1) * 2 + 1] = tanh_bf16x2(pack_bf16(c2, c3));
+    }
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        float c0 = f.b2[nt][0], c1 = f.b2[nt][1], c2 = f.b2[nt][0], c3 = f.b2[nt][1];
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt)
+            mma_bf16(c0, c1, c2, c3, A2[kt][0], A2[kt][1], A2[kt][2], A2[kt][3], f.w2[nt][kt][0],
+                     f.w2[nt][kt][1]);
+        A3[nt >> 1][(nt & 1) * 2 + 0] = tanh_bf16x2(pack_bf16(c0, c1));
+        A3[nt >> 1][(nt & 1) * 2 + 1] = tanh_bf16x2(pack_bf16(c2, c3));
+    }
+    z0 = f.b3[0]; z1 = f.b3[1]; z2 = f.b3[0]; z3 = f.b3[1];
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt)
+        mma_bf16(z0, z1, z2, z3, A3[kt][0], A3[kt][1], A3[kt][2], A3[kt][3], f.w3[kt][0], f.w3[kt][1]);
 }
 
-// gR d(u_R)/ds + gL d(u_L)/ds of the cell's right and left face values with
-// respect to its stencil s = v_{c-2..c+2}; callers pass s shifted by the cell
-// value as the forward does (ds[2] = 0; the gradient of a shift-equivariant
-// value does not depend on the shift). Returns dsum[5].
-__device__ __forceinline__ void learned_cell_vjp(const float s[5], float gR, float gL,
-                                                 const float* Wr, const LearnedParams& lp,
-                                                 float dsum[5]) {
+// (x0, x1) * (1 - h^2) for a bf16 pair h, packed to fp16
+__device__ __forceinline__ uint32_t tanh_back_f16(float x0, float x1, uint32_t h) {
+    const float h0 = bf16_lo(h), h1 = bf16_hi(h);
+    return pack_f16(x0 * fmaf(-h0, h0, 1.0f), x1 * fmaf(-h1, h1, 1.0f));
+}
+
+// network backward of one m16 tile: d0 / d1 the fp16 A registers of the
+// (scaled) logit cotangents of rows g / g+8 (columns 2t, 2t+1); returns the
+// input cotangents dx (row g: columns 2t, 2t+1 in x[0], x[1]; row g+8 in x[2], x[3])
+__device__ __forceinline__ void mlp_tile_back(const MlpBackFrags& b, uint32_t d0, uint32_t d1,
+                                              const uint32_t A2[2][4], const uint32_t A3[2][4],
+                                              float x[4]) {
+    uint32_t D2[2][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
+        mma_f16(c0, c1, c2, c3, d0, d1, 0u, 0u, b.w3[nt], 0u);
+        D2[nt >> 1][(nt & 1) * 2 + 0] = tanh_back_f16(c0, c1, A3[nt >> 1][(nt & 1) * 2 + 0]);
+        D2[nt >> 1][(nt & 1) * 2 + 1] = tanh_back_f16(c2, c3, A3[nt >> 1][(nt & 1) * 2 + 1]);
+    }
+    uint32_t D1[2][4];
+#pragma unroll
+    for (int nt = 0; nt < 4; ++nt) {
+        float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt)
+            mma_f16(c0, c1, c2, c3, D2[kt][0], D2[kt][1], D2[kt][2], D2[kt][3], b.w2[nt][kt][0],
+                    b.w2[nt][kt][1]);
+        D1[nt >> 1][(nt & 1) * 2 + 0] = tanh_back_f16(c0, c1, A2[nt >> 1][(nt & 1) * 2 + 0]);
+        D1[nt >> 1][(nt & 1) * 2 + 1] = tanh_back_f16(c2, c3, A2[nt >> 1][(nt & 1) * 2 + 1]);
+    }
+    x[0] = x[1] = x[2] = x[3] = 0.0f;
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt)
+        mma_f16(x[0], x[1], x[2], x[3], D1[kt][0], D1[kt][1], D1[kt][2], D1[kt][3], b.w1[kt][0],
+                b.w1[kt][1]);
+}
+
+// gR d(u_R)/ds + gL d(u_L)/ds of this lane's cell (right and left face values)
+// with respect to its stencil s = v_{c-2..c+2}, given shifted by the cell
+// value as the forward evaluates it (ds[2] = 0; the gradient of a
+// shift-equivariant value does not depend on the shift). All 32 lanes must
+// call it (shuffles, mma) with finite stencils; returns dsum[5].
+__device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpBackFrags& bk,
+                                                   const float s[5], float gR, float gL,
+                                                   const LearnedParams& lp, float dsum[5]) {
+    const int lane = threadIdx.x & 31, t = lane & 3, base = lane & ~3;
+    // ---- forward (as learned_cell32), keeping the activations
+    float x[5];
+    mlp_normalise(s, x);
+    const uint32_t p0 = pack_bf16(x[0], x[1]), p1 = pack_bf16(x[2], x[3]), p2 = pack_bf16(x[4], 1.0f);
+    uint32_t a[4];
+#pragma unroll
+    for (int o = 0; o < 4; ++o) {
+        const uint32_t q0 = __shfl_sync(0xffffffffu, p0, base + o);
+        const uint32_t q1 = __shfl_sync(0xffffffffu, p1, base + o);
+        const uint32_t q2 = __shfl_sync(0xffffffffu, p2, base + o);
+        a[o] = t == 0 ? q0 : (t == 1 ? q1 : (t == 2 ? q2 : 0u));
+    }
+    uint32_t A2a[2][4], A3a[2][4], A2b[2][4], A3b[2][4];
+    float zA0, zA1, zA2, zA3, zB0, zB1, zB2, zB3;
+    mlp_tile_keep(f, a[0], a[1], A2a, A3a, zA0, zA1, zA2, zA3);
+    mlp_tile_keep(f, a[2], a[3], A2b, A3b, zB0, zB1, zB2, zB3);
+    float z0, z1, z2;
+    {
+        const float u0 = __shfl_sync(0xffffffffu, zA0, base), u1 = __shfl_sync(0xffffffffu, zA1, base);
+        const float u2 = __shfl_sync(0xffffffffu, zA2, base), u3 = __shfl_sync(0xffffffffu, zA3, base);
+        const float v0 = __shfl_sync(0xffffffffu, zB0, base), v1 = __shfl_sync(0xffffffffu, zB1, base);
+        const float v2 = __shfl_sync(0xffffffffu, zB2, base), v3 = __shfl_sync(0xffffffffu, zB3, base);
+        const float w0 = __shfl_sync(0xffffffffu, zA0, base + 1), w1 = __shfl_sync(0xffffffffu, zA2, base + 1);
+        const float y0 = __shfl_sync(0xffffffffu, zB0, base + 1), y1 = __shfl_sync(0xffffffffu, zB2, base + 1);
+        if (t == 0) { z0 = u0; z1 = u1; z2 = w0; }
+        else if (t == 1) { z0 = u2; z1 = u3; z2 = w1; }
+        else if (t == 2) { z0 = v0; z1 = v1; z2 = y0; }
+        else { z0 = v2; z1 = v3; z2 = y1; }
+    }
+    // ---- per-cell part: weights, fallback, direct terms, logit cotangents
     float hr[3], hl[3];
     cell_substencils(s, hr, hl);
     float be[3], q[6], jr[3], jl[3];
     js_betas(s, be, q);
     js_weights_pair(be, lp.eps, jr, jl);
-    // network forward with the inference roundings
-    float x[5];
-    mlp_normalise(s, x);
-    float xr[5];
-#pragma unroll
-    for (int k = 0; k < 5; ++k) xr[k] = round_bf16(x[k]);
-    float h1[kMlpH], h2[kMlpH];
-    for (int a = 0; a < kMlpH; ++a) {
-        float acc = 0.0f;
-#pragma unroll
-        for (int k = 0; k < kMlpIn; ++k) acc = fmaf(Wr[kOffW1 + a * kMlpIn + k], xr[k], acc);
-        acc += Wr[kOffB1 + a];
-        h1[a] = bf16_tanh(acc);
-    }
-    for (int a = 0; a < kMlpH; ++a) {
-        float acc = Wr[kOffB2 + a];
-        for (int k = 0; k < kMlpH; ++k) acc = fmaf(Wr[kOffW2 + a * kMlpH + k], h1[k], acc);
-        h2[a] = bf16_tanh(acc);
-    }
-    float z[3];
-    for (int o = 0; o < 3; ++o) {
-        float acc = Wr[kOffB3 + o];
-        for (int k = 0; k < kMlpH; ++k) acc = fmaf(Wr[kOffW3 + o * kMlpH + k], h2[k], acc);
-        z[o] = acc;
-    }
-    const float zm = fmaxf(fmaxf(z[0], z[1]), z[2]);
+    const float zm = fmaxf(fmaxf(z0, z1), z2);
     float wr[3], wl[3];
-    cell_softmax(__expf(z[0] - zm), __expf(z[1] - zm), __expf(z[2] - zm), wr, wl);
+    cell_softmax(__expf(z0 - zm), __expf(z1 - zm), __expf(z2 - zm), wr, wl);
     const bool fbr = outside_band(wr, jr, lp), fbl = outside_band(wl, jl, lp);
     const float* tr = fbr ? jr : wr;
     const float* tl = fbl ? jl : wl;
@@ -344,11 +462,11 @@ __device__ __forceinline__ void learned_cell_vjp(const float s[5], float gR, flo
               cL * (11.0f * tl[0] + 5.0f * tl[1] + 2.0f * tl[2]);
     dsum[3] = cR * (2.0f * tr[1] + 5.0f * tr[2]) + cL * (-7.0f * tl[0] - tl[1]);
     dsum[4] = -cR * tr[2] + cL * (2.0f * tl[0]);
-    const float uR = tr[0] * hr[0] + tr[1] * hr[1] + tr[2] * hr[2];
-    const float uL = tl[0] * hl[0] + tl[1] * hl[1] + tl[2] * hl[2];
     if (fbr || fbl) {
         // WENO-JS faces: d u / d beta_l = -2 omega_l (uhat_l - u) / (eps + beta_l);
         // the left face's sub-stencil k sees beta_{2-k}
+        const float uR = tr[0] * hr[0] + tr[1] * hr[1] + tr[2] * hr[2];
+        const float uL = tl[0] * hl[0] + tl[1] * hl[1] + tl[2] * hl[2];
         float bb[3] = {0.0f, 0.0f, 0.0f};
         if (fbr)
             for (int l = 0; l < 3; ++l) bb[l] += -2.0f * gR * jr[l] * (hr[l] - uR) / (lp.eps + be[l]);
@@ -364,7 +482,6 @@ __device__ __forceinline__ void learned_cell_vjp(const float s[5], float gR, flo
         dsum[2] += a0 + 3.0f * c0 - 2.0f * a1 + a2 + 3.0f * c2;
         dsum[3] += a1 - c1 - 2.0f * a2 - 4.0f * c2;
         dsum[4] += a2 + c2;
-        if (fbr && fbl) return;
     }
     // softmax backward of the network faces into the shared logits: right
     // omega = softmax(z); left omega = softmax(z2 - ln 3, z1, z0 + ln 3)
@@ -379,21 +496,42 @@ __device__ __forceinline__ void learned_cell_vjp(const float s[5], float gR, flo
         const float dot = wl[0] * d0 + wl[1] * d1 + wl[2] * d2;
         dz[2] += wl[0] * (d0 - dot); dz[1] += wl[1] * (d1 - dot); dz[0] += wl[2] * (d2 - dot);
     }
-    float da2[kMlpH];
-    for (int k = 0; k < kMlpH; ++k) {
-        const float dh = Wr[kOffW3 + k] * dz[0] + Wr[kOffW3 + kMlpH + k] * dz[1] +
-                         Wr[kOffW3 + 2 * kMlpH + k] * dz[2];
-        da2[k] = dh * (1.0f - h2[k] * h2[k]);
-    }
-    float dx[5] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    for (int k = 0; k < kMlpH; ++k) {
-        float dh = 0.0f;
-        for (int a = 0; a < kMlpH; ++a) dh = fmaf(Wr[kOffW2 + a * kMlpH + k], da2[a], dh);
-        const float da1 = dh * (1.0f - h1[k] * h1[k]);
+    // power-of-two scale of the row into [1, 2)
+    const float mz = fmaxf(fmaxf(fabsf(dz[0]), fabsf(dz[1])), fabsf(dz[2]));
+    int ez = static_cast<int>((__float_as_uint(mz) >> 23) & 0xffu) - 127;
+    ez = mz > 0.0f ? max(-100, min(100, ez)) : 0;
+    const float up = __uint_as_float(static_cast<uint32_t>(127 - ez) << 23);  // 2^-ez
+    const float down = __uint_as_float(static_cast<uint32_t>(127 + ez) << 23);  // 2^ez
+    const uint32_t e01 = pack_f16(dz[0] * up, dz[1] * up), e2 = pack_f16(dz[2] * up, 0.0f);
+    // ---- network backward on the tensor cores: A registers of the logit
+    // cotangents (columns 2t, 2t+1 of rows g, g+8 of each tile)
+    uint32_t d[4];
 #pragma unroll
-        for (int j = 0; j < kMlpIn; ++j) dx[j] = fmaf(Wr[kOffW1 + k * kMlpIn + j], da1, dx[j]);
+    for (int o = 0; o < 4; ++o) {
+        const uint32_t q01 = __shfl_sync(0xffffffffu, e01, base + o);
+        const uint32_t q2 = __shfl_sync(0xffffffffu, e2, base + o);
+        d[o] = t == 0 ? q01 : (t == 1 ? q2 : 0u);
     }
-    // normalisation x = (s - mean) / (max - min + eps)
+    float xa[4], xb[4];
+    mlp_tile_back(bk, d[0], d[1], A2a, A3a, xa);
+    mlp_tile_back(bk, d[2], d[3], A2b, A3b, xb);
+    // gather the owned row's dx[0..4] from lanes base+0 (columns 0, 1),
+    // base+1 (2, 3) and base+2 (4)
+    float dx[6];
+#pragma unroll
+    for (int src = 0; src < 3; ++src) {
+        const float r0 = __shfl_sync(0xffffffffu, xa[0], base + src);
+        const float r1 = __shfl_sync(0xffffffffu, xa[1], base + src);
+        const float r2 = __shfl_sync(0xffffffffu, xa[2], base + src);
+        const float r3 = __shfl_sync(0xffffffffu, xa[3], base + src);
+        const float r4 = __shfl_sync(0xffffffffu, xb[0], base + src);
+        const float r5 = __shfl_sync(0xffffffffu, xb[1], base + src);
+        const float r6 = __shfl_sync(0xffffffffu, xb[2], base + src);
+        const float r7 = __shfl_sync(0xffffffffu, xb[3], base + src);
+        dx[2 * src] = t == 0 ? r0 : (t == 1 ? r2 : (t == 2 ? r4 : r6));
+        dx[2 * src + 1] = t == 0 ? r1 : (t == 1 ? r3 : (t == 2 ? r5 : r7));
+    }
+    // ---- normalisation x = (s - mean) / (max - min + eps), unscaled
     const float m = (s[0] + s[1] + s[2] + s[3] + s[4]) * 0.2f;
     float lo = fminf(fminf(fminf(s[0], s[1]), fminf(s[2], s[3])), s[4]);
     float hi = fmaxf(fmaxf(fmaxf(s[0], s[1]), fmaxf(s[2], s[3])), s[4]);
@@ -402,6 +540,7 @@ __device__ __forceinline__ void learned_cell_vjp(const float s[5], float gR, flo
     int nhi = 0, nlo = 0;
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
+        dx[k] *= down;
         sdx += dx[k];
         sxd += dx[k] * (s[k] - m);
         nhi += s[k] == hi;
@@ -410,9 +549,9 @@ __device__ __forceinline__ void learned_cell_vjp(const float s[5], float gR, flo
     const float gr = -sxd * inv * inv;  // d/d(range)
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
-        float d = inv * (dx[k] - 0.2f * sdx);
-        d += gr * ((s[k] == hi ? 1.0f / nhi : 0.0f) - (s[k] == lo ? 1.0f / nlo : 0.0f));
-        dsum[k] += d;
+        float dd = inv * (dx[k] - 0.2f * sdx);
+        dd += gr * ((s[k] == hi ? 1.0f / nhi : 0.0f) - (s[k] == lo ? 1.0f / nlo : 0.0f));
+        dsum[k] += dd;
     }
 }
 

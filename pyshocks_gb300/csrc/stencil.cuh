@@ -40,6 +40,7 @@ struct Smem {
     T* Q;   // 13/12 (2D)^2; reused for ES-WENO omega_0
     T* UL;  // ul (value at the left face of the cell)
     T* UR;  // ur (value at the right face of the cell)
+    int W;  // window length (cells) of every array
 
     __device__ static size_t bytes(int W) { return size_t(7) * W * sizeof(T); }
     __host__ static size_t host_bytes(int W) { return size_t(7) * W * sizeof(T); }
@@ -47,6 +48,7 @@ struct Smem {
         T* p = reinterpret_cast<T*>(base);
         U = p; S = p + W; H = p + 2 * W; D = p + 3 * W; Q = p + 4 * W;
         UL = p + 5 * W; UR = p + 6 * W;
+        this->W = W;
     }
 };
 
@@ -57,6 +59,20 @@ struct OpParams {
     LearnedParams lp;      // learned reconstruction (float32 state only)
     T fscale;              // face values F are stored as F / fscale (see face_fluxes)
 };
+
+// float copy of the operator parameters (the mixed-precision learned path)
+template <class T>
+__host__ __device__ inline OpParams<float> float_params(const OpParams<T>& p) {
+    OpParams<float> f;
+    f.eps = static_cast<float>(p.eps);
+    f.delta = static_cast<float>(p.delta);
+    f.hnu = static_cast<float>(p.hnu);
+    f.c = static_cast<float>(p.c);
+    f.hnu_amax = static_cast<float>(p.hnu_amax);
+    f.lp = p.lp;
+    f.fscale = 1.0f;
+    return f;
+}
 
 // learned reconstruction of cells [clo, chi): one cell per lane, 32 cells per
 // warp iteration, both faces of a cell from one network evaluation. The cell
@@ -259,9 +275,78 @@ __host__ __device__ inline DtState compute_dt(double smax, double cfl, double th
 // fused SSPRK33 step of one tile: window [s - HL, s + te + HL) -> u_out[s, s + te)
 // returns the thread's max |f'(u_new)| bits
 // ---------------------------------------------------------------------------
+// Mixed precision (double state, learned reconstruction): the operator runs in
+// float on the float-rounded stage states and each stage is an increment about
+// the step's start state u, accumulated in float and added to u in double
+// once per step:
+//   k1 = u + i1,  k2 = 3/4 u + 1/4 (k1 + i2) = u + d2,  d2 = (i1 + i2) / 4,
+//   u+ = 1/3 u + 2/3 (k2 + i3) = u + 2/3 (d2 + i3),
+// with i_s = dt/dx (F_{j-1/2} - F_{j+1/2}) of stage s. Rounding the operator's
+// inputs to float perturbs the increments only (the state itself is never
+// rounded), and the learned reconstruction works in float/bfloat16 anyway;
+// the double pipe then carries three operations per cell and step instead of
+// the whole operator. The float arrays live inside the double layout: U is the
+// loaded double window, S holds the float window uf and the float stage state,
+// H the float cell differences and the increments.
+template <int EQ, int FLUX>
+__device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* gout, int te,
+                                              double dtdx, const OpParams<double>& p) {
+    constexpr int HL = step_halo<double>();
+    const int tid = threadIdx.x, nt = blockDim.x, W = sm.W;
+    const OpParams<float> pf = float_params(p);
+    Smem<float> fs;
+    fs.U = reinterpret_cast<float*>(sm.S);
+    fs.S = fs.U + W;
+    fs.H = reinterpret_cast<float*>(sm.H);
+    fs.D = reinterpret_cast<float*>(sm.D);
+    fs.Q = reinterpret_cast<float*>(sm.Q);
+    fs.UL = reinterpret_cast<float*>(sm.UL);
+    fs.UR = reinterpret_cast<float*>(sm.UR);
+    fs.W = W;
+    float* inc = fs.H + W;
+    const float dtf = static_cast<float>(dtdx);
+    for (int i = tid; i < te + 2 * HL; i += nt) fs.U[i] = static_cast<float>(sm.U[i]);
+    __syncthreads();
+    {
+        const int lo = HL - 6, hi = HL + te + 6;
+        face_fluxes<float, EQ, SHK_REC_LEARNED, FLUX>(fs.U, lo, hi, fs, pf);
+        for (int i = lo + tid; i < hi; i += nt) {
+            const float d = dtf * (fs.D[i - 1] - fs.D[i]);
+            inc[i] = d;
+            fs.S[i] = fs.U[i] + d;
+        }
+        __syncthreads();
+    }
+    {
+        const int lo = HL - 3, hi = HL + te + 3;
+        face_fluxes<float, EQ, SHK_REC_LEARNED, FLUX>(fs.S, lo, hi, fs, pf);
+        for (int i = lo + tid; i < hi; i += nt) {
+            const float d = 0.25f * (inc[i] + dtf * (fs.D[i - 1] - fs.D[i]));
+            inc[i] = d;
+            fs.S[i] = fs.U[i] + d;
+        }
+        __syncthreads();
+    }
+    unsigned long long mx = 0;
+    {
+        const int lo = HL, hi = HL + te;
+        face_fluxes<float, EQ, SHK_REC_LEARNED, FLUX>(fs.S, lo, hi, fs, pf);
+        for (int i = lo + tid; i < hi; i += nt) {
+            const float d = (2.0f / 3.0f) * (inc[i] + dtf * (fs.D[i - 1] - fs.D[i]));
+            const double un = sm.U[i] + static_cast<double>(d);
+            gout[i - HL] = un;
+            const unsigned long long b = abs_bits(wave_speed<EQ>(un, p.c));
+            mx = b > mx ? b : mx;
+        }
+    }
+    return mx;
+}
+
 template <class T, int EQ, int REC, int FLUX>
 __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, T dtdx,
                                             const OpParams<T>& p) {
+    if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED)
+        return step_tile_mixed<EQ, FLUX>(sm, gout, te, dtdx, p);
     constexpr int HL = step_halo<T>();
     const int tid = threadIdx.x, nt = blockDim.x;
     dtdx *= p.fscale;

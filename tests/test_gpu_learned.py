@@ -98,8 +98,10 @@ def test_training_reduces_loss():
     assert l1 < 0.8 * l0, (l0, l1, hist[-3:])
 
 
-def test_learned_batched_step_matches_oracle():
-    """A few float32 SSPRK33 steps of the learned scheme (Burgers, Rusanov)
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_learned_batched_step_matches_oracle(dtype):
+    """A few SSPRK33 steps of the learned scheme (Burgers, Rusanov; float32
+    state, or float64 state with the float operator and float64 accumulation)
     against the oracle's learned reconstruction in float64 with the same
     bfloat16 roundings and the same dt."""
     from pyshocks_gb300 import learned
@@ -108,24 +110,26 @@ def test_learned_batched_step_matches_oracle():
     params = learned.init_params(seed=7)
     n, nsteps = 256, 5
     u0 = R.exact_cell_average_sine(R.make_uniform_cell_grid(-1.0, 1.0, n, 3))[3:-3]
-    solver = BatchedSolver(_scheme(params), [n], 2.0 / n, dtype=torch.float32, max_steps=nsteps)
+    solver = BatchedSolver(_scheme(params), [n], 2.0 / n, dtype=dtype, max_steps=nsteps)
     solver.reset(torch.tensor(u0))
     solver.step(nsteps)
     got = solver.u.double().cpu()
     dts = solver.dt_history().cpu()
     wts = {"params": params.double().cpu(), "tau": 1.0e-2, "band": 0.1, "bf16": True}
-    ref, _ = T.forward(torch.tensor(u0, dtype=torch.float32).double()[None], 2.0 / n, nsteps,
+    ref, _ = T.forward(torch.tensor(u0, dtype=dtype).double()[None], 2.0 / n, nsteps,
                        dts=dts, rec="learned", weights=wts)
     err = float((got - ref[0]).abs().max())
     assert err < 2.0e-3 * float(np.ptp(u0)), err
     assert solver.status() == 0
 
 
-def test_learned_adjoint_matches_autograd():
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_learned_adjoint_matches_autograd(dtype):
     """The hand-written adjoint of the learned scheme, MLP backward included
-    (float32 state, sqrt(n) checkpoints), against torch autograd through the
-    oracle's learned reconstruction with the same bfloat16 roundings and the
-    same frozen dt sequence. Tolerance 5e-3 relative (float32 state, tanh.approx)."""
+    (tensor cores, fp16 operands), sqrt(n) checkpoints, against torch autograd
+    through the oracle's learned reconstruction with the same bfloat16
+    roundings and the same frozen dt sequence. Tolerance 5e-3 relative (float
+    operator, tanh.approx, fp16 backward products)."""
     from pyshocks_gb300 import learned
     from pyshocks_gb300.adjoint import CheckpointedSolve
     from pyshocks_gb300.batched import BatchedSolver
@@ -134,12 +138,12 @@ def test_learned_adjoint_matches_autograd():
     n, nsteps = 128, 8
     u0 = R.exact_cell_average_sine(R.make_uniform_cell_grid(-1.0, 1.0, n, 3))[3:-3]
     tgt = u0 + 0.05 * np.sin(3 * np.pi * np.linspace(-1, 1, n, endpoint=False))
-    solver = BatchedSolver(_scheme(params), [n], 2.0 / n, dtype=torch.float32, max_steps=nsteps)
+    solver = BatchedSolver(_scheme(params), [n], 2.0 / n, dtype=dtype, max_steps=nsteps)
     cs = CheckpointedSolve(solver, nsteps, stride=3)
     uT = cs.forward(torch.tensor(u0))
-    g = cs.backward(uT - torch.tensor(tgt, device="cuda", dtype=torch.float32)).double().cpu()
+    g = cs.backward(uT - torch.tensor(tgt, device="cuda", dtype=dtype)).double().cpu()
     wts = {"params": params.double().cpu(), "tau": 1.0e-2, "band": 0.1, "bf16": True}
-    u0t = torch.tensor(u0, dtype=torch.float32).double()[None]
+    u0t = torch.tensor(u0, dtype=dtype).double()[None]
     ref, _, _ = T.adjoint_gradient(u0t, torch.tensor(tgt)[None], 2.0 / n, nsteps,
                                    dts=solver.dt_history().cpu(), rec="learned", weights=wts)
     err = float((g - ref[0]).abs().max() / ref.abs().max())
