@@ -382,8 +382,11 @@ def bench_gpu(args, rank: int, world: int) -> None:
 
     extra = None
     if rank == 0 and not args.profile and not args.no_extra:
+        adj = bench_adjoint(scheme, dev, args)
         extra = {"fp32_forward": bench_fp32(scheme, sizes, u0, stream, args),
-                 "adjoint": bench_adjoint(scheme, dev, args)}
+                 "adjoint": adj,
+                 "learned": bench_learned(scheme, dev, stream, args, adj),
+                 "inverse_lwr": bench_inverse(dev, args)}
 
     cpu = None
     if rank == 0 and not args.no_cpu and not args.profile:
@@ -421,49 +424,77 @@ def bench_gpu(args, rank: int, world: int) -> None:
         print(json.dumps(line), flush=True)
 
 
-def bench_fp32(scheme, sizes, u0, stream, args) -> dict:
-    """Same batch and steps with float32 state (FP64 dt and reductions)."""
+def _timed_steps(solver, u0, k, stream) -> float:
+    """ms per step of *k* graph-captured steps after a warm-up."""
     import torch
 
-    from pyshocks_gb300.batched import BatchedSolver
-
-    s32 = BatchedSolver(scheme, sizes, 2.0 / sizes.astype(np.float64), dtype=torch.float32)
-    k = args.steps + (args.steps % 2)
     with torch.cuda.stream(stream):
-        s32.reset(u0)
-        s32.step(4, graph=True)
+        solver.reset(u0)
+        solver.step(4, graph=True)
         stream.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        s32.step(k, graph=True)
+        solver.step(k, graph=True)
         e1.record(stream)
         e1.synchronize()
-    ms = e0.elapsed_time(e1)
+    if solver.status():
+        raise RuntimeError(f"step kernel reported status {solver.status()}")
+    return e0.elapsed_time(e1) / k
+
+
+def bench_fp32(scheme, sizes, u0, stream, args) -> dict:
+    """Same batch and steps with float32 state (float64 dt and reductions): rate,
+    error against the float64 run of the same steps, conservation drift."""
+    import torch
+
+    from pyshocks_gb300.batched import BatchedSolver
+
+    dx = 2.0 / sizes.astype(np.float64)
+    k = args.steps + (args.steps % 2)
+    s32 = BatchedSolver(scheme, sizes, dx, dtype=torch.float32)
+    ms = _timed_steps(s32, u0, k, stream)
     cells = int(np.sum(sizes))
     rate = cells * k / (ms * 1e-3)
+    # error and drift after 4 + k steps from u0 (the timed run's state)
+    s64 = BatchedSolver(scheme, sizes, dx)
+    with torch.cuda.stream(stream):
+        s64.reset(u0)
+        m0 = s64.reduce(0)
+        s64.step(4 + k, graph=True)
+        diff = (s32.u.double() - s64.u).abs()
+        inst = torch.repeat_interleave(torch.arange(len(sizes), device=diff.device),
+                                       torch.tensor(sizes, device=diff.device))
+        l1 = torch.zeros(len(sizes), dtype=torch.float64, device=diff.device).index_add_(0, inst, diff)
+        l1 = l1 * torch.tensor(dx, device=diff.device)
+        drift64 = ((s64.reduce(0) - m0).abs() / torch.tensor(sizes, device=diff.device)).max()
+        drift32 = ((s32.reduce(0) - m0).abs() / torch.tensor(sizes, device=diff.device)).max()
+        stream.synchronize()
     return {"metric": "WENO5 cell-steps/s (float32 state)", "value": rate, "unit": "cell-steps/s",
-            "ms_per_step": ms / k, "algo_gb_per_s": 8 * rate / 1e9}
+            "ms_per_step": ms, "algo_gb_per_s": 8 * rate / 1e9,
+            "vs_float64_after_steps": 4 + k,
+            "l1_mean": float(l1.mean()), "linf": float(diff.max()),
+            "mass_drift_per_cell_max": {"float64": float(drift64), "float32": float(drift32)}}
 
 
-def bench_adjoint(scheme, dev, args) -> dict:
-    """The adjoint configuration: B=256 Burgers instances, N=4096, config-1 initial
-    condition, J = 1/2 |u(T) - u_target|^2, sqrt(n)-checkpointed reverse sweep,
-    float64. One gradient = one instance's full dJ/du0."""
+def _adjoint_rate(scheme, dev, nsteps, dtype, B=256, n=4096) -> dict:
+    """B Burgers instances, N=4096, config-1 initial condition,
+    J = 1/2 |u(T) - u_target|^2, sqrt(n)-checkpointed reverse sweep. One
+    gradient = one instance's full dJ/du0."""
     import torch
 
     from pyshocks_gb300.adjoint import CheckpointedSolve
     from pyshocks_gb300.batched import BatchedSolver
 
-    n, B, nsteps = 4096, 256, args.adjoint_steps
     # exact cell averages of 0.5 + sin(pi x) on [-1, 1]
     f = np.linspace(-1.0, 1.0, n + 1)
     u1 = 0.5 + (np.cos(np.pi * f[:-1]) - np.cos(np.pi * f[1:])) / (np.pi * (2.0 / n))
-    u0 = torch.tensor(np.tile(u1, B), device=dev)
-    solver = BatchedSolver(scheme, [n] * B, 2.0 / n, max_steps=nsteps)
+    u0 = torch.tensor(np.tile(u1, B), device=dev, dtype=dtype)
+    solver = BatchedSolver(scheme, [n] * B, 2.0 / n, max_steps=nsteps, dtype=dtype)
     cs = CheckpointedSolve(solver, nsteps)
     rng = np.random.default_rng(SEED + 3)
-    target = (u0 + 0.05 * torch.tensor(rng.standard_normal(u0.numel()), device=dev)).contiguous()
+    pert = torch.tensor(rng.standard_normal(u0.numel()), device=dev, dtype=dtype)
+    target = cs.forward((u0 + 0.05 * pert).contiguous()).clone()
     cs.forward(u0)  # warm-up
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -476,9 +507,124 @@ def bench_adjoint(scheme, dev, args) -> dict:
     if solver.status() or not torch.isfinite(g).all():
         raise RuntimeError("adjoint run failed")
     return {"metric": "adjoint grads/s", "value": B / (t2 - t0), "unit": "gradients/s",
-            "config": {"batch": B, "n": n, "steps": nsteps, "checkpoint_stride": cs.stride},
+            "config": {"batch": B, "n": n, "steps": nsteps, "checkpoint_stride": cs.stride,
+                       "dtype": str(dtype).replace("torch.", "")},
             "forward_s": t1 - t0, "reverse_s": t2 - t1,
             "adjoint_cell_steps_per_s": n * B * nsteps / (t2 - t1)}
+
+
+def bench_adjoint(scheme, dev, args) -> dict:
+    """The adjoint configuration in float64 (B=256, N=4096, 4000 steps)."""
+    import torch
+
+    return _adjoint_rate(scheme, dev, args.adjoint_steps, torch.float64)
+
+
+def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
+    """Learned-weight WENO against the plain float64 kernel: forward rate on
+    B=4096 x N=4096, adjoint rate on the adjoint configuration, and L1 error
+    at t=0.4 against the plain float64 solution on a 4x finer grid (restricted
+    by averaging) for B=64 instances of the same initial-condition family."""
+    import torch
+
+    from pyshocks_gb300 import burgers, learned
+    from pyshocks_gb300.batched import BatchedSolver
+
+    params = learned.load_default_params(device=dev)
+    lrec = learned.LearnedWENO(params=params)
+    lscheme = burgers.Rusanov(rec=lrec)
+    uscheme = burgers.Rusanov(rec=learned.LearnedWENO(params=learned.init_params(device=dev)))
+    n = 4096
+    k = args.steps + (args.steps % 2)
+    B = 4096
+    u0 = initial_state(np.full(B, n), workload_params(SEED + 4, batch=B)[1], dev)
+    rates = {}
+    for name, sch, dt in (("plain_f64", plain, torch.float64),
+                          ("learned_f64", lscheme, torch.float64),
+                          ("learned_f32", lscheme, torch.float32)):
+        s = BatchedSolver(sch, [n] * B, 2.0 / n, dtype=dt)
+        rates[name] = B * n / (_timed_steps(s, u0, k, stream) * 1e-3)
+        del s
+    # accuracy
+    Bl, r, T = 64, 4, 0.4
+    prm = workload_params(SEED + 5, batch=Bl)[1]
+
+    def run(sch, nn, dt):
+        s = BatchedSolver(sch, [nn] * Bl, 2.0 / nn, dtype=dt)
+        with torch.cuda.stream(stream):
+            s.reset(initial_state(np.full(Bl, nn), prm, dev), tfinal=T)
+            while float(s.time().min()) < T:
+                s.step(256, graph=True)
+            stream.synchronize()
+        if s.status():
+            raise RuntimeError("accuracy run failed")
+        return s.u.double().reshape(Bl, nn)
+
+    ref = run(plain, n * r, torch.float64).reshape(Bl, n, r).mean(-1)
+
+    def l1(u):
+        return float((u - ref).abs().sum(-1).mean() * 2.0 / n)
+
+    err = {"plain_f64": l1(run(plain, n, torch.float64)),
+           "plain_f32": l1(run(plain, n, torch.float32)),
+           "learned_f64": l1(run(lscheme, n, torch.float64)),
+           "learned_f32": l1(run(lscheme, n, torch.float32)),
+           "untrained_f64": l1(run(uscheme, n, torch.float64))}
+    adj = {"learned_f64": _adjoint_rate(lscheme, dev, args.adjoint_steps, torch.float64),
+           "learned_f32": _adjoint_rate(lscheme, dev, args.adjoint_steps, torch.float32)}
+    return {
+        "forward": {"unit": "cell-steps/s", "config": {"batch": B, "n": n, "steps": k}, **rates,
+                    "speedup_learned_f64": rates["learned_f64"] / rates["plain_f64"],
+                    "speedup_learned_f32": rates["learned_f32"] / rates["plain_f64"]},
+        "adjoint": {"unit": "gradients/s", "plain_f64": adjoint_plain["value"],
+                    "learned_f64": adj["learned_f64"]["value"],
+                    "learned_f32": adj["learned_f32"]["value"],
+                    "speedup_learned_f64": adj["learned_f64"]["value"] / adjoint_plain["value"],
+                    "speedup_learned_f32": adj["learned_f32"]["value"] / adjoint_plain["value"]},
+        "l1_vs_fine_plain": {"config": {"batch": Bl, "n": n, "t_final": T, "fine": n * r}, **err},
+        "note": ("learned_f64 keeps the state and its accumulation in float64 and runs the "
+                 "operator in float32 (bfloat16 tensor-core network); learned_f32 also "
+                 "stores the state in float32. untrained_f64: the network at initialisation "
+                 "(softmax at the ideal weights) with the same trust band"),
+    }
+
+
+def bench_inverse(dev, args) -> dict:
+    """The batched LWR inverse problem (learned scheme, float32 state, float64
+    misfits, whole iteration in a CUDA graph): B=1024 instances with N from
+    {4096..65536}; ``--inverse-steps`` SSPRK33 steps per solve (the full
+    configuration has 3000) and a few timed gradient-descent iterations."""
+    import torch
+
+    from pyshocks_gb300 import burgers, learned
+    from pyshocks_gb300.inverse import InverseProblem, lwr_initial_states
+
+    rng = np.random.default_rng(SEED + 6)
+    B = 1024
+    sizes = rng.choice(np.array([4096, 8192, 16384, 32768, 65536]), size=B)
+    rec = learned.LearnedWENO(params=learned.load_default_params(device=dev))
+    prob = InverseProblem(burgers.LWRRusanov(rec=rec), sizes, 2.0 / sizes.astype(np.float64),
+                          args.inverse_steps, lr=0.5)
+    truth = lwr_initial_states(rng, sizes, device=dev)
+    prob.observe(truth)
+    guess = torch.cat([torch.full((int(m),), float(x.mean()), dtype=torch.float64, device=dev)
+                       for m, x in zip(sizes, torch.split(truth, list(sizes)))])
+    prob.run(guess, 1, graph=True)  # capture + warm-up
+    torch.cuda.synchronize()
+    iters = 3
+    t0 = time.perf_counter()
+    hist = prob.run(guess, iters, graph=True)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / iters
+    j = torch.stack(hist).sum(-1).cpu().numpy()
+    cells = int(sizes.sum())
+    return {"config": {"batch": B, "cells": cells, "steps": args.inverse_steps,
+                       "full_steps": 3000, "iterations_timed": iters},
+            "s_per_iteration": dt,
+            "cell_steps_per_s": 2 * cells * args.inverse_steps / dt,
+            "est_s_per_iteration_full": dt * 3000 / args.inverse_steps,
+            "misfit_sum": [float(x) for x in j],
+            "note": "cell_steps_per_s counts the forward and the reverse sweep of each iteration"}
 
 
 def ctypes_fp_peak(L):
@@ -500,6 +646,8 @@ def main() -> None:
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the float32 and adjoint measurements")
     ap.add_argument("--adjoint-steps", type=int, default=4000)
+    ap.add_argument("--inverse-steps", type=int, default=300,
+                    help="SSPRK33 steps per solve of the inverse-problem leg (full: 3000)")
     ap.add_argument("--scheme", choices=["plain", "learned"], default="plain",
                     help="profiling aid: time the learned-weight float32 step instead")
     ap.add_argument("--profile", action="store_true",

@@ -60,7 +60,9 @@ typedef struct {
     float tau;         /* SHK_REC_LEARNED: JS weight marking a non-smooth sub-stencil */
     float band;        /* SHK_REC_LEARNED: max network weight on such sub-stencils */
     float dev;         /* SHK_REC_LEARNED: max |omega - omega_JS| per sub-stencil   */
-    float reserved2;
+    float norm_eps;    /* SHK_REC_LEARNED: floor of the stencil range in the network's
+                        * input normalisation (s - mean) / (range + norm_eps); <= 0
+                        * means 1e-12 */
 } shk_scheme;
 
 const char* shk_strerror(int status);
@@ -229,11 +231,12 @@ int64_t shk_mlp_workspace_bytes(int64_t n);
  * target n x 2 (right, left face), weight n; d the WENO-JS5 ideal weights. One
  * network output z per cell gives omega_R = softmax(z) and omega_L =
  * softmax(z2 - ln 3, z1, z0 + ln 3). Also the gradient w.r.t. the parameters
- * (fp32 forward/backward, deterministic reduction). *loss is device memory
- * (double). */
+ * (fp32 forward/backward, deterministic reduction); norm_eps as in
+ * shk_scheme. *loss is device memory (double). */
 int shk_mlp_loss_grad_f32(const float* params, const float* stencils, const float* target,
-                          const float* weight, int64_t n, float reg, float* grad, double* loss,
-                          void* workspace, int64_t workspace_bytes, void* stream);
+                          const float* weight, int64_t n, float reg, float norm_eps,
+                          float* grad, double* loss, void* workspace, int64_t workspace_bytes,
+                          void* stream);
 
 /* one Adam step on the parameters (step >= 1 for the bias corrections) */
 int shk_mlp_adam_f32(float* params, const float* grad, float* m, float* v, float lr,

@@ -26,7 +26,7 @@ import torch
 
 N_IN, N_H, N_OUT = 5, 32, 3
 N_PARAMS = N_H * N_IN + N_H + N_H * N_H + N_H + N_OUT * N_H + N_OUT
-NORM_EPS = 1.0e-12
+NORM_EPS = 1.0e-5
 _D53 = (0.1, 0.6, 0.3)
 
 
@@ -47,30 +47,30 @@ def _bf16(x: torch.Tensor, on: bool) -> torch.Tensor:
     return x.to(torch.bfloat16).to(x.dtype) if on else x
 
 
-def normalise(s: torch.Tensor) -> torch.Tensor:
-    """``(s - mean) / (max - min + 1e-12)`` of stencils ``s[..., 5]``."""
+def normalise(s: torch.Tensor, norm_eps: float = NORM_EPS) -> torch.Tensor:
+    """``(s - mean) / (max - min + norm_eps)`` of stencils ``s[..., 5]``."""
     m = s.mean(dim=-1, keepdim=True)
     r = s.amax(dim=-1, keepdim=True) - s.amin(dim=-1, keepdim=True)
-    return (s - m) / (r + NORM_EPS)
+    return (s - m) / (r + norm_eps)
 
 
-def logits(params, s, *, bf16: bool = False):
+def logits(params, s, *, bf16: bool = False, norm_eps: float = NORM_EPS):
     """Network output ``z`` of cell stencils ``s[..., 5]``. With ``bf16`` the
     inputs and weights are rounded to bfloat16 (FP32 accumulation) and each
     hidden layer applies tanh to the bfloat16-rounded pre-activation with a
     bfloat16 result, as the tensor-core inference kernel does
     (tanh.approx.bf16x2)."""
     W1, b1, W2, b2, W3, b3 = unpack(params)
-    x = _bf16(normalise(s), bf16)
+    x = _bf16(normalise(s, norm_eps), bf16)
     h1 = _bf16(torch.tanh(_bf16(x @ _bf16(W1, bf16).T + _bf16(b1, bf16), bf16)), bf16)
     h2 = _bf16(torch.tanh(_bf16(h1 @ _bf16(W2, bf16).T + b2, bf16)), bf16)
     return h2 @ _bf16(W3, bf16).T + b3
 
 
-def mlp_weights(params, s, *, bf16: bool = False):
+def mlp_weights(params, s, *, bf16: bool = False, norm_eps: float = NORM_EPS):
     """Right- and left-face softmax weights ``(omega_R, omega_L)`` of cell
     stencils ``s[..., 5]`` from one network evaluation."""
-    z = logits(params, s, bf16=bf16)
+    z = logits(params, s, bf16=bf16, norm_eps=norm_eps)
     ln3 = torch.log(torch.tensor(3.0, dtype=z.dtype))
     zl = torch.stack([z[..., 2] - ln3, z[..., 1], z[..., 0] + ln3], dim=-1)
     return torch.softmax(z, dim=-1), torch.softmax(zl, dim=-1)
@@ -106,10 +106,11 @@ def _band(w, wjs, tau, band, dev):
 
 
 def cell_face_values(params, s, *, eps: float, tau: float, band: float, dev: float = 0.5,
-                     bf16: bool = False, return_fallback: bool = False):
+                     bf16: bool = False, return_fallback: bool = False,
+                     norm_eps: float = NORM_EPS):
     """Learned ``(right, left)`` face values of cell stencils ``s[..., 5]``
     with the per-face WENO-JS fallback."""
-    wr, wl = mlp_weights(params, s, bf16=bf16)
+    wr, wl = mlp_weights(params, s, bf16=bf16, norm_eps=norm_eps)
     jr, jl = js_weights(s, eps)
     fr, fl = _band(wr, jr, tau, band, dev), _band(wl, jl, tau, band, dev)
     wr = torch.where(fr[..., None], jr, wr)
@@ -130,17 +131,17 @@ def stencils_periodic(u: torch.Tensor):
 def learned_recon(u: torch.Tensor, weights: dict, eps: float):
     """``(ul, ur)`` of every cell for the torch oracle's ``face_flux``."""
     kw = dict(eps=eps, tau=weights["tau"], band=weights["band"], dev=weights.get("dev", 0.5),
-              bf16=weights.get("bf16", False))
+              bf16=weights.get("bf16", False), norm_eps=weights.get("norm_eps", NORM_EPS))
     vr, vl = cell_face_values(weights["params"], stencils_periodic(u), **kw)
     return vl, vr
 
 
-def training_loss(params, s, target, weight, reg: float = 0.0):
+def training_loss(params, s, target, weight, reg: float = 0.0, norm_eps: float = NORM_EPS):
     """Weighted squared face-value error of the raw network (no fallback) over
     both faces of each cell, plus the pull toward the ideal weights:
     ``sum_i sum_F [w_i (sum_k omega_F,k uhat_F,k - T_F,i)^2 + reg |omega_F,i - d|^2] / (2 n)``
     with ``target[:, 0]`` / ``target[:, 1]`` the right / left face targets."""
-    wr, wl = mlp_weights(params, s)
+    wr, wl = mlp_weights(params, s, norm_eps=norm_eps)
     hr, hl = substencils(s)
     vr, vl = torch.sum(wr * hr, dim=-1), torch.sum(wl * hl, dim=-1)
     d = torch.tensor(_D53, dtype=wr.dtype)

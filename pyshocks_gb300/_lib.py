@@ -49,7 +49,7 @@ class ShkScheme(ctypes.Structure):
         ("tau", ctypes.c_float),
         ("band", ctypes.c_float),
         ("dev", ctypes.c_float),
-        ("reserved2", ctypes.c_float),
+        ("norm_eps", ctypes.c_float),
     ]
 
 
@@ -97,8 +97,8 @@ SIGNATURES: dict[str, tuple] = {
     "shk_apply_operator_lf_noalloc_max_cells": (ctypes.c_int64, []),
     "shk_mlp_num_params": (ctypes.c_int, []),
     "shk_mlp_workspace_bytes": (ctypes.c_int64, [_I64]),
-    "shk_mlp_loss_grad_f32": (ctypes.c_int, [_P, _P, _P, _P, _I64, ctypes.c_float, _P, _P, _P,
-                                             _I64, _P]),
+    "shk_mlp_loss_grad_f32": (ctypes.c_int, [_P, _P, _P, _P, _I64, ctypes.c_float, ctypes.c_float,
+                                             _P, _P, _P, _I64, _P]),
     "shk_mlp_adam_f32": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_float, ctypes.c_float,
                                         ctypes.c_float, ctypes.c_float, _I32, _P]),
     "shk_learned_faces_f32": (ctypes.c_int, [_SCH, _P, _P, _I64, _P]),

@@ -334,19 +334,32 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     constexpr int HU = adj_uhalo<T>();
     const int tid = threadIdx.x, nt = blockDim.x;
     const T fdt = dtdx * p.fscale;  // face fluxes are stored as F / fscale
-    // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12)
+    // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12),
+    // with the forward step's own formulas (increments about u for float)
     {
         const int lo = HU - 15, hi = HU + te + 15;
         face_fluxes<T, EQ, REC, SHK_FLUX_RUSANOV>(a.U, lo, hi, a.fwd(a.K1), p);
-        for (int i = lo + tid; i < hi; i += nt) a.K1[i] = fma(fdt, a.D[i - 1] - a.D[i], a.U[i]);
+        for (int i = lo + tid; i < hi; i += nt) {
+            if constexpr (sizeof(T) == 4) {
+                const T d = fdt * (a.D[i - 1] - a.D[i]);
+                a.T0[i] = d;
+                a.K1[i] = a.U[i] + d;
+            } else {
+                a.K1[i] = fma(fdt, a.D[i - 1] - a.D[i], a.U[i]);
+            }
+        }
         __syncthreads();
     }
     {
         const int lo = HU - 12, hi = HU + te + 12;
         face_fluxes<T, EQ, REC, SHK_FLUX_RUSANOV>(a.K1, lo, hi, a.fwd(a.K2), p);
         for (int i = lo + tid; i < hi; i += nt) {
-            const T k = fma(fdt, a.D[i - 1] - a.D[i], a.K1[i]);
-            a.K2[i] = fma(T(1.0 / 4.0), k, T(3.0 / 4.0) * a.U[i]);
+            if constexpr (sizeof(T) == 4) {
+                a.K2[i] = a.U[i] + T(0.25) * (a.T0[i] + fdt * (a.D[i - 1] - a.D[i]));
+            } else {
+                const T k = fma(fdt, a.D[i - 1] - a.D[i], a.K1[i]);
+                a.K2[i] = fma(T(1.0 / 4.0), k, T(3.0 / 4.0) * a.U[i]);
+            }
         }
         __syncthreads();
     }
@@ -548,7 +561,8 @@ OpParams<T> adj_params(const shk_scheme* s) {
     p.hnu = static_cast<T>(0.5 * s->nu);
     p.c = static_cast<T>(s->speed);
     p.hnu_amax = T(0);
-    p.lp = LearnedParams{s->mlp, static_cast<float>(s->eps), s->tau, s->band, s->dev};
+    p.lp = LearnedParams{s->mlp, static_cast<float>(s->eps), s->tau, s->band, s->dev,
+                         norm_floor(s->norm_eps)};
     p.fscale = (sizeof(T) == 8 && s->flux == SHK_FLUX_RUSANOV && s->rec == SHK_REC_WENOJS53 &&
                 s->equation == SHK_EQ_BURGERS && s->nu == 1.0) ? T(0.25) : T(1);
     return p;

@@ -323,7 +323,8 @@ OpParams<T> make_params(const shk_scheme* s) {
     p.hnu = static_cast<T>(0.5 * s->nu);
     p.c = static_cast<T>(s->speed);
     p.hnu_amax = T(0);
-    p.lp = LearnedParams{s->mlp, static_cast<float>(s->eps), s->tau, s->band, s->dev};
+    p.lp = LearnedParams{s->mlp, static_cast<float>(s->eps), s->tau, s->band, s->dev,
+                         norm_floor(s->norm_eps)};
     // FP64 Burgers-Rusanov with nu = 1 stores 4 F (see face_fluxes)
     p.fscale = (sizeof(T) == 8 && s->flux == SHK_FLUX_RUSANOV && s->rec == SHK_REC_WENOJS53 &&
                 s->equation == SHK_EQ_BURGERS && s->nu == 1.0) ? T(0.25) : T(1);

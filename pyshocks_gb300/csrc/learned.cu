@@ -30,7 +30,7 @@ constexpr int kStage = kMlpIn + kMlpH + kMlpH + kMlpH + kMlpH + kMlpOut;  // x, 
 
 __global__ void __launch_bounds__(kTrainThreads) mlp_loss_grad_kernel(
     const float* __restrict__ P, const float* __restrict__ stencils, const float* __restrict__ target,
-    const float* __restrict__ weight, int64_t n, float reg, float* __restrict__ block_grad,
+    const float* __restrict__ weight, int64_t n, float reg, float norm_eps, float* __restrict__ block_grad,
     double* __restrict__ block_loss) {
     extern __shared__ __align__(16) float sm[];
     float* Ps = sm;                              // kMlpParams
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_loss_grad_kernel(
 #pragma unroll
         for (int k = 0; k < 5; ++k) s[k] -= c;
         s[2] = 0.0f;
-        mlp_normalise(s, x);
+        mlp_normalise(s, x, norm_eps);
 #pragma unroll 4
         for (int a = 0; a < kMlpH; ++a) {
             float acc = b1[a];
@@ -278,8 +278,9 @@ int64_t shk_mlp_workspace_bytes(int64_t n) {
 }
 
 int shk_mlp_loss_grad_f32(const float* params, const float* stencils, const float* target,
-                          const float* weight, int64_t n, float reg, float* grad, double* loss,
-                          void* workspace, int64_t workspace_bytes, void* stream) {
+                          const float* weight, int64_t n, float reg, float norm_eps,
+                          float* grad, double* loss, void* workspace, int64_t workspace_bytes,
+                          void* stream) {
     if (!params || !stencils || !target || !weight || !grad || n <= 0 || !workspace) return SHK_EINVAL;
     if (workspace_bytes < shk_mlp_workspace_bytes(n)) return SHK_EINVAL;
     const int nb = train_blocks(n);
@@ -290,7 +291,8 @@ int shk_mlp_loss_grad_f32(const float* params, const float* stencils, const floa
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     int r = lcheck(cudaFuncSetAttribute(mlp_loss_grad_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (r) return r;
-    mlp_loss_grad_kernel<<<nb, kTrainThreads, smem, st>>>(params, stencils, target, weight, n, reg, bg, bl);
+    mlp_loss_grad_kernel<<<nb, kTrainThreads, smem, st>>>(params, stencils, target, weight, n, reg,
+                                                          norm_floor(norm_eps), bg, bl);
     r = lcheck(cudaGetLastError());
     if (r) return r;
     mlp_reduce_kernel<<<(kMlpParams + 255) / 256, 256, 0, st>>>(bg, bl, nb, n, grad, loss);
@@ -311,7 +313,7 @@ int shk_learned_faces_f32(const shk_scheme* scheme, const float* stencils, float
                           void* stream) {
     if (!scheme || !scheme->mlp || !stencils || !out || n <= 0) return SHK_EINVAL;
     LearnedParams lp{scheme->mlp, static_cast<float>(scheme->eps), scheme->tau, scheme->band,
-                     scheme->dev};
+                     scheme->dev, norm_floor(scheme->norm_eps)};
     const int64_t tiles = (n + 31) / 32;
     const int blocks = static_cast<int>((tiles + 7) / 8 < 4096 ? (tiles + 7) / 8 : 4096);
     learned_faces_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(lp, stencils, out, n);

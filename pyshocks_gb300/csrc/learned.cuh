@@ -46,7 +46,15 @@ struct LearnedParams {
     float tau;         // JS weight below which a sub-stencil counts as non-smooth
     float band;        // largest network weight allowed on non-smooth sub-stencils
     float dev;         // largest |omega_k - omega_JS,k| allowed
+    float norm_eps;    // floor of the stencil range in the input normalisation
 };
+
+// The normalisation floor plays the part of WENO-JS's eps: features far below
+// it (a few rounding units on a flat state) reach the network as ~0 inputs, so
+// the weights do not follow rounding noise and the scheme's Jacobian stays
+// bounded there (with a floor of 1e-12 the linearised learned scheme amplified
+// such noise until the adjoint overflowed).
+__host__ __device__ inline float norm_floor(float e) { return e > 0.0f ? e : kNormEps; }
 
 __device__ __forceinline__ bool outside_band(const float w[3], const float wj[3],
                                              const LearnedParams& lp) {
@@ -56,12 +64,12 @@ __device__ __forceinline__ bool outside_band(const float w[3], const float wj[3]
     return excess > lp.band || d > lp.dev;
 }
 
-// x = (s - mean) / (max - min + 1e-12)
-__device__ __forceinline__ void mlp_normalise(const float s[5], float x[5]) {
+// x = (s - mean) / (max - min + norm_eps)
+__device__ __forceinline__ void mlp_normalise(const float s[5], float x[5], float norm_eps) {
     float m = (s[0] + s[1] + s[2] + s[3] + s[4]) * 0.2f;
     float lo = fminf(fminf(fminf(s[0], s[1]), fminf(s[2], s[3])), s[4]);
     float hi = fmaxf(fmaxf(fmaxf(s[0], s[1]), fmaxf(s[2], s[3])), s[4]);
-    const float inv = 1.0f / (hi - lo + kNormEps);
+    const float inv = 1.0f / (hi - lo + norm_eps);
 #pragma unroll
     for (int k = 0; k < 5; ++k) x[k] = (s[k] - m) * inv;
 }
@@ -226,7 +234,7 @@ __device__ __forceinline__ void learned_cell32(const MlpFrags& f, const float ds
     const int lane = threadIdx.x & 31, t = lane & 3, base = lane & ~3;
     // normalised input and its packed column pairs (x0,x1) (x2,x3) (x4,1)
     float x[5];
-    mlp_normalise(ds, x);
+    mlp_normalise(ds, x, lp.norm_eps);
     const uint32_t p0 = pack_bf16(x[0], x[1]), p1 = pack_bf16(x[2], x[3]), p2 = pack_bf16(x[4], 1.0f);
     // A registers of lane (g, t): columns 2t, 2t+1 of rows g and g+8 of each tile,
     // owned by lanes base+0 (A, g), base+1 (A, g+8), base+2 (B, g), base+3 (B, g+8)
@@ -414,7 +422,7 @@ __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpB
     const int lane = threadIdx.x & 31, t = lane & 3, base = lane & ~3;
     // ---- forward (as learned_cell32), keeping the activations
     float x[5];
-    mlp_normalise(s, x);
+    mlp_normalise(s, x, lp.norm_eps);
     const uint32_t p0 = pack_bf16(x[0], x[1]), p1 = pack_bf16(x[2], x[3]), p2 = pack_bf16(x[4], 1.0f);
     uint32_t a[4];
 #pragma unroll
@@ -531,11 +539,11 @@ __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpB
         dx[2 * src] = t == 0 ? r0 : (t == 1 ? r2 : (t == 2 ? r4 : r6));
         dx[2 * src + 1] = t == 0 ? r1 : (t == 1 ? r3 : (t == 2 ? r5 : r7));
     }
-    // ---- normalisation x = (s - mean) / (max - min + eps), unscaled
+    // ---- normalisation x = (s - mean) / (max - min + norm_eps), unscaled
     const float m = (s[0] + s[1] + s[2] + s[3] + s[4]) * 0.2f;
     float lo = fminf(fminf(fminf(s[0], s[1]), fminf(s[2], s[3])), s[4]);
     float hi = fmaxf(fmaxf(fmaxf(s[0], s[1]), fmaxf(s[2], s[3])), s[4]);
-    const float inv = 1.0f / (hi - lo + kNormEps);
+    const float inv = 1.0f / (hi - lo + lp.norm_eps);
     float sdx = 0.0f, sxd = 0.0f;
     int nhi = 0, nlo = 0;
 #pragma unroll

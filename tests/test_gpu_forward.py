@@ -227,9 +227,10 @@ def test_batched_float32_error_and_conservation(gb):
     s32.step(nsteps)
     m64 = s64.reduce(0).cpu().numpy()
     m32 = s32.reduce(0).cpu().numpy()
-    # mass is conserved to rounding (periodic flux form)
+    # mass is conserved to rounding (periodic flux form); the float32 stages are
+    # increments about u, so no systematic drift from the inexact float 1/3, 2/3
     assert np.max(np.abs(m64 - m0) / np.array(sizes)) < 1.0e-13
-    assert np.max(np.abs(m32 - m0) / np.array(sizes)) < 1.0e-5
+    assert np.max(np.abs(m32 - m0) / np.array(sizes)) < 1.0e-7
     diff = (s32.u.double() - s64.u).abs()
     assert float(diff.max()) < 1.0e-3
     # reductions agree with torch
