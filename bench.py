@@ -248,10 +248,12 @@ def bench_reference(args, rank: int) -> None:
 
 
 def _config(args) -> dict:
+    what = {"plain": "plain WENO-JS5", "learned": "learned-weight WENO (float64 state)",
+            "learned32": "learned-weight WENO (float32 state)"}[getattr(args, "scheme", "plain")]
     return {
-        "workload": "batched plain WENO-JS5+Rusanov+SSPRK33 Burgers, B=4096, "
+        "workload": f"batched {what}+Rusanov+SSPRK33 Burgers, B={args.batch}, "
                     "N~U{1024..16384}, CFL 0.5, periodic",
-        "batch": BATCH,
+        "batch": args.batch,
         "sizes": list(SIZES),
         "seed": SEED,
         "eps": EPS,
@@ -272,17 +274,19 @@ def bench_gpu(args, rank: int, world: int) -> None:
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    sizes, params = workload_params(SEED + rank)
+    sizes, params = workload_params(SEED + rank, batch=args.batch)
     cells = int(np.sum(sizes))
     rec = gb.reconstruction.make_reconstruction_from_name("wenojs53", eps=EPS)
     scheme = gb.burgers.make_scheme_from_name("rusanov", rec=rec)
     u0 = initial_state(sizes, params, dev)
-    if args.scheme == "learned":
+    if args.scheme != "plain":
+        # profiling aid: the learned-weight step on the same batch (float64
+        # state with the float operator, or float32 state)
         from pyshocks_gb300 import learned
 
         lscheme = gb.burgers.Rusanov(rec=learned.LearnedWENO(params=learned.load_default_params()))
         solver = BatchedSolver(lscheme, sizes, 2.0 / sizes.astype(np.float64), theta=THETA,
-                               dtype=torch.float32)
+                               dtype=torch.float32 if args.scheme == "learned32" else torch.float64)
     else:
         solver = BatchedSolver(scheme, sizes, 2.0 / sizes.astype(np.float64), theta=THETA)
     stream = torch.cuda.Stream(device=dev)
@@ -415,7 +419,10 @@ def bench_gpu(args, rank: int, world: int) -> None:
             "gpu_launches": k,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
-                         "kernel": "batched_step_kernel<double,Burgers,WENOJS53,Rusanov>",
+                         "kernel": ("batched_step_kernel<double,Burgers,WENOJS53,Rusanov>"
+                                    if args.scheme == "plain" else
+                                    f"batched_step_kernel<{'float' if args.scheme == 'learned32' else 'double'},"
+                                    "Burgers,LEARNED,Rusanov>"),
                          "algo_bytes_per_launch": algo_bytes, "peak_source": peak_src},
             "fp64_pipe": fp64,
             "cpu_baseline": cpu,
@@ -627,6 +634,23 @@ def bench_inverse(dev, args) -> dict:
             "note": "cell_steps_per_s counts the forward and the reverse sweep of each iteration"}
 
 
+def profile_adjoint(args) -> None:
+    """The adjoint leg alone (for ncu captures of the reverse-step kernel)."""
+    import torch
+
+    import pyshocks_gb300 as gb
+    from pyshocks_gb300 import learned
+
+    dev = torch.device("cuda", 0)
+    if args.scheme == "plain":
+        sch = gb.burgers.Rusanov(rec=gb.reconstruction.make_reconstruction_from_name("wenojs53", eps=EPS))
+    else:
+        sch = gb.burgers.Rusanov(rec=learned.LearnedWENO(params=learned.load_default_params(device=dev)))
+    dtype = torch.float32 if args.scheme == "learned32" else torch.float64
+    r = _adjoint_rate(sch, dev, args.adjoint_steps, dtype, B=args.batch)
+    print(json.dumps({"profile_adjoint": args.scheme, **r}), flush=True)
+
+
 def ctypes_fp_peak(L):
     import ctypes
 
@@ -648,8 +672,14 @@ def main() -> None:
     ap.add_argument("--adjoint-steps", type=int, default=4000)
     ap.add_argument("--inverse-steps", type=int, default=300,
                     help="SSPRK33 steps per solve of the inverse-problem leg (full: 3000)")
-    ap.add_argument("--scheme", choices=["plain", "learned"], default="plain",
-                    help="profiling aid: time the learned-weight float32 step instead")
+    ap.add_argument("--scheme", choices=["plain", "learned", "learned32"], default="plain",
+                    help="profiling aid: time the learned-weight step (float64 state with the "
+                         "float operator, or float32 state) instead of the plain one")
+    ap.add_argument("--batch", type=int, default=BATCH,
+                    help="profiling aid: instances of the batch (default: the workload's 4096)")
+    ap.add_argument("--profile-adjoint", action="store_true",
+                    help="profiling aid: only the checkpointed adjoint of --scheme on --batch "
+                         "instances of N=4096 for --adjoint-steps steps")
     ap.add_argument("--profile", action="store_true",
                     help="timed region only (no e2e, CPU baseline or FP peak): for ncu")
     args = ap.parse_args()
@@ -659,6 +689,9 @@ def main() -> None:
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         bench_reference(args, rank)
+        return
+    if args.profile_adjoint:
+        profile_adjoint(args)
         return
     if world > 1:
         import torch
