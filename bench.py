@@ -261,6 +261,7 @@ def _config(args) -> dict:
         "precision": "float64",
         "l2": "state (2 x 208 MB ping-pong) larger than the 129 MB L2; no flush",
         "parallelism": f"replicas x{args.gpus}" if args.gpus > 1 else "single GPU",
+        "tile": args.tile,
     }
 
 
@@ -286,9 +287,11 @@ def bench_gpu(args, rank: int, world: int) -> None:
 
         lscheme = gb.burgers.Rusanov(rec=learned.LearnedWENO(params=learned.load_default_params()))
         solver = BatchedSolver(lscheme, sizes, 2.0 / sizes.astype(np.float64), theta=THETA,
-                               dtype=torch.float32 if args.scheme == "learned32" else torch.float64)
+                               dtype=torch.float32 if args.scheme == "learned32" else torch.float64,
+                               tile=args.tile)
     else:
-        solver = BatchedSolver(scheme, sizes, 2.0 / sizes.astype(np.float64), theta=THETA)
+        solver = BatchedSolver(scheme, sizes, 2.0 / sizes.astype(np.float64), theta=THETA,
+                               tile=args.tile)
     stream = torch.cuda.Stream(device=dev)
     dist = None
     if world > 1:
@@ -546,10 +549,12 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
     B = 4096
     u0 = initial_state(np.full(B, n), workload_params(SEED + 4, batch=B)[1], dev)
     rates = {}
+    shapes = {}
     for name, sch, dt in (("plain_f64", plain, torch.float64),
                           ("learned_f64", lscheme, torch.float64),
                           ("learned_f32", lscheme, torch.float32)):
-        s = BatchedSolver(sch, [n] * B, 2.0 / n, dtype=dt)
+        s = BatchedSolver(sch, [n] * B, 2.0 / n, dtype=dt, tile=args.tile)
+        shapes[name] = {"tile": s.tile, "ctas_per_sm": s.ctas_per_sm}
         rates[name] = B * n / (_timed_steps(s, u0, k, stream) * 1e-3)
         del s
     # accuracy
@@ -580,7 +585,8 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
     adj = {"learned_f64": _adjoint_rate(lscheme, dev, args.adjoint_steps, torch.float64),
            "learned_f32": _adjoint_rate(lscheme, dev, args.adjoint_steps, torch.float32)}
     return {
-        "forward": {"unit": "cell-steps/s", "config": {"batch": B, "n": n, "steps": k}, **rates,
+        "forward": {"unit": "cell-steps/s", "config": {"batch": B, "n": n, "steps": k},
+                    "launch_shapes": shapes, **rates,
                     "speedup_learned_f64": rates["learned_f64"] / rates["plain_f64"],
                     "speedup_learned_f32": rates["learned_f32"] / rates["plain_f64"]},
         "adjoint": {"unit": "gradients/s", "plain_f64": adjoint_plain["value"],
@@ -675,6 +681,9 @@ def main() -> None:
     ap.add_argument("--scheme", choices=["plain", "learned", "learned32"], default="plain",
                     help="profiling aid: time the learned-weight step (float64 state with the "
                          "float operator, or float32 state) instead of the plain one")
+    ap.add_argument("--tile", default="auto",
+                    help="cells per work item of the batched plans, or 'auto' (autotuner: tile "
+                         "and CTAs/SM timed on the batch); 0 = library default")
     ap.add_argument("--batch", type=int, default=BATCH,
                     help="profiling aid: instances of the batch (default: the workload's 4096)")
     ap.add_argument("--profile-adjoint", action="store_true",
@@ -685,6 +694,8 @@ def main() -> None:
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.tile != "auto":
+        args.tile = int(args.tile)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":

@@ -56,6 +56,10 @@ class BatchedSolver:
     :arg theta: Courant factor of the driver closure ``theta * predict_timestep``.
     :arg dtype: ``torch.float64`` or ``torch.float32`` state.
     :arg max_steps: capacity of the per-step dt history (for the adjoint).
+    :arg tile: cells per work item (0: the library default, 1024; ``"auto"``:
+        chosen with ``ctas_per_sm`` by :func:`pyshocks_gb300.autotune.tune`).
+    :arg ctas_per_sm: resident CTAs per SM of the persistent grid (0: as many
+        as the shared memory allows, at most 8).
     """
 
     def __init__(
@@ -66,7 +70,7 @@ class BatchedSolver:
         *,
         theta: float = 1.0,
         dtype: torch.dtype = torch.float64,
-        tile: int = 0,
+        tile: int | str = 0,
         max_steps: int = 0,
         ctas_per_sm: int = 0,
         device: str | torch.device = "cuda",
@@ -87,6 +91,14 @@ class BatchedSolver:
         self.device = torch.device(device)
         self.max_steps = int(max_steps)
         self._cs = scheme.c_scheme(float(dxs[0]))
+        if tile == "auto":
+            from pyshocks_gb300 import autotune
+
+            best = autotune.tune(scheme, self.sizes, dxs, dtype=dtype, theta=theta,
+                                 device=self.device, adjoint=self.max_steps > 0)
+            tile, ctas_per_sm = best.tile, best.ctas_per_sm
+        self.tile = int(tile)
+        self.ctas_per_sm = int(ctas_per_sm)
         opts = L.ShkPlanOpts(dtype=_DTYPES[dtype], tile=int(tile), max_steps=self.max_steps,
                              ctas_per_sm=int(ctas_per_sm))
         plan = ctypes.c_void_p()

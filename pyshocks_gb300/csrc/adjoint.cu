@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
     __shared__ __align__(8) uint64_t bar;
     constexpr int HL = step_halo<T>();
     Smem<T> sm;
-    sm.carve(smem_raw, P.tile + 2 * HL);
+    carve_step<T, REC>(sm, smem_raw, P.tile + 2 * HL);
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_mbar_init();
@@ -699,8 +699,16 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
     const size_t asmem = mixed ? sizeof(float) * kMixedAdjSlots * size_t(W)
                                : (dtype == SHK_F64 ? AdjSmem<double>::host_bytes(W)
                                                    : AdjSmem<float>::host_bytes(W));
-    const size_t fsmem = dtype == SHK_F64 ? Smem<double>::host_bytes(D.tile + 2 * step_halo<double>())
-                                          : Smem<float>::host_bytes(D.tile + 2 * step_halo<float>());
+    {
+        // the reverse step keeps ~20 windows of the tile in shared memory: plans
+        // with longer tiles can step forward but not run the adjoint
+        int dev0 = 0, optin = 0;
+        cudaGetDevice(&dev0);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev0);
+        if (asmem > static_cast<size_t>(optin)) return SHK_EUNSUPPORTED;
+    }
+    const size_t fsmem = dtype == SHK_F64 ? Smem<double>::step_bytes(D.tile + 2 * step_halo<double>(), sch.rec)
+                                          : Smem<float>::step_bytes(D.tile + 2 * step_halo<float>(), sch.rec);
     // adjoint grid: resident CTAs for its larger shared-memory footprint
     int dev = 0, sms = 1;
     cudaGetDevice(&dev);

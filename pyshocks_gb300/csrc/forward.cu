@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) batc
     using B = typename Bits<T>::type;
 
     Smem<T> sm;
-    sm.carve(smem_raw, P.tile + 2 * HL);
+    carve_step<T, REC>(sm, smem_raw, P.tile + 2 * HL);
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_mbar_init();
@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kThreads) single_step_kernel(const T* __restri
     __shared__ __align__(8) uint64_t bar;
     constexpr int HL = step_halo<T>();
     Smem<T> sm;
-    sm.carve(smem_raw, tile + 2 * HL);
+    carve_step<T, REC>(sm, smem_raw, tile + 2 * HL);
     if (threadIdx.x == 0) {
         mbar_init(&bar, 1);
         fence_mbar_init();
@@ -404,6 +404,22 @@ struct BatchedStepLaunch {
     }
 };
 
+// resident CTAs per SM of the step kernel a scheme dispatches to, at the
+// given dynamic shared memory (registers and shared memory both counted)
+struct StepOccupancy {
+    size_t smem; int* out;
+    template <class T, int EQ, int REC, int FLUX> int operator()() {
+        if constexpr (FLUX == SHK_FLUX_LF) {
+            return SHK_EUNSUPPORTED;
+        } else {
+            auto k = batched_step_kernel<T, EQ, REC, FLUX>;
+            SHK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            SHK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k, kThreads, smem));
+            return SHK_OK;
+        }
+    }
+};
+
 }  // namespace
 
 struct shk_plan {
@@ -464,7 +480,7 @@ int launch_max(shk_plan* P, const void* u, int slot, cudaStream_t st) {
 template <class T>
 int launch_step(shk_plan* P, const void* uin, void* uout, cudaStream_t st) {
     const PlanDev D = P->dev();
-    const size_t smem = Smem<T>::host_bytes(P->tile + 2 * step_halo<T>());
+    const size_t smem = Smem<T>::step_bytes(P->tile + 2 * step_halo<T>(), P->scheme.rec);
     OpParams<T> p = make_params<T>(&P->scheme);
     BatchedStepLaunch<T> f{D, static_cast<const T*>(uin), static_cast<T*>(uout), p, smem, P->grid, st};
     return dispatch_scheme<T>(&P->scheme, f);
@@ -549,7 +565,7 @@ int shk_ssprk33_step_f64(const shk_scheme* scheme, const double* u, double* u_ou
     cudaStream_t st = as_stream(stream);
     const int tile = 512;
     const int W = tile + 2 * step_halo<double>();
-    const size_t smem = Smem<double>::host_bytes(W);
+    const size_t smem = Smem<double>::step_bytes(W, scheme->rec);
     const int blocks = static_cast<int>((n + tile - 1) / tile);
     OpParams<double> p = make_params<double>(scheme);
     SingleStepLaunch f{u, u_out, n, nghosts, tile, dt / dx, p, smem, blocks, st};
@@ -645,10 +661,16 @@ int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_of
     // persistent grid: resident CTAs per SM x SMs
     int per_sm = opts && opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 0;
     if (per_sm == 0) {
-        const size_t smem = dtype == SHK_F64 ? Smem<double>::host_bytes(tile + 2 * step_halo<double>())
-                                             : Smem<float>::host_bytes(tile + 2 * step_halo<float>());
-        per_sm = std::max(1, static_cast<int>((200 * 1024) / std::max<size_t>(smem, 1)));
-        per_sm = std::min(per_sm, 8);
+        const size_t smem = dtype == SHK_F64 ? Smem<double>::step_bytes(tile + 2 * step_halo<double>(), scheme->rec)
+                                             : Smem<float>::step_bytes(tile + 2 * step_halo<float>(), scheme->rec);
+        int resident = 0;
+        const int r = dtype == SHK_F64 ? dispatch_scheme<double>(scheme, StepOccupancy{smem, &resident})
+                                       : dispatch_scheme<float>(scheme, StepOccupancy{smem, &resident});
+        if (r != SHK_OK || resident < 1) {
+            shk_plan_destroy(P);
+            return r != SHK_OK ? r : SHK_EINVAL;  // the window does not fit one SM
+        }
+        per_sm = std::min(resident, 8);
     }
     P->grid = std::max(1, std::min(P->nitems, per_sm * sm_count()));
     *out = P;

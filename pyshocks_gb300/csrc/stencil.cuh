@@ -46,6 +46,27 @@ struct Smem {
     // float states carry one more array (the stage increments)
     static constexpr int kArrays = sizeof(T) == 4 ? 8 : 7;
     __host__ static size_t host_bytes(int W) { return size_t(kArrays) * W * sizeof(T); }
+    // the step tile of a double state with the learned reconstruction runs in
+    // mixed precision (step_tile_mixed) on the double window and 7 float arrays
+    __host__ static size_t step_bytes(int W, int rec) {
+        if (sizeof(T) == 8 && rec == SHK_REC_LEARNED) return size_t(W) * (sizeof(double) + 7 * sizeof(float));
+        return host_bytes(W);
+    }
+    // compact layout of that mixed step: U (double window), then as float
+    // arrays S (2W: uf, k), H (2W: cell differences, increments), D, UL, UR;
+    // Q aliases D (the learned reconstruction does not use it)
+    __device__ void carve_mixed(unsigned char* base, int W) {
+        U = reinterpret_cast<T*>(base);
+        float* f = reinterpret_cast<float*>(base + size_t(W) * sizeof(double));
+        S = reinterpret_cast<T*>(f);
+        H = reinterpret_cast<T*>(f + 2 * W);
+        D = reinterpret_cast<T*>(f + 4 * W);
+        UL = reinterpret_cast<T*>(f + 5 * W);
+        UR = reinterpret_cast<T*>(f + 6 * W);
+        Q = D;
+        I = nullptr;
+        this->W = W;
+    }
     __device__ void carve(unsigned char* base, int W) {
         T* p = reinterpret_cast<T*>(base);
         U = p; S = p + W; H = p + 2 * W; D = p + 3 * W; Q = p + 4 * W;
@@ -62,6 +83,13 @@ struct OpParams {
     LearnedParams lp;      // learned reconstruction (float32 state only)
     T fscale;              // face values F are stored as F / fscale (see face_fluxes)
 };
+
+// shared-memory layout of a step tile (see Smem::step_bytes)
+template <class T, int REC>
+__device__ __forceinline__ void carve_step(Smem<T>& sm, unsigned char* base, int W) {
+    if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED) sm.carve_mixed(base, W);
+    else sm.carve(base, W);
+}
 
 // float copy of the operator parameters (the mixed-precision learned path)
 template <class T>
@@ -288,9 +316,9 @@ __host__ __device__ inline DtState compute_dt(double smax, double cfl, double th
 // inputs to float perturbs the increments only (the state itself is never
 // rounded), and the learned reconstruction works in float/bfloat16 anyway;
 // the double pipe then carries three operations per cell and step instead of
-// the whole operator. The float arrays live inside the double layout: U is the
-// loaded double window, S holds the float window uf and the float stage state,
-// H the float cell differences and the increments.
+// the whole operator. Layout (Smem::carve_mixed, or the full double layout):
+// U is the loaded double window, S holds the float window uf and the float
+// stage state, H the float cell differences and the increments.
 template <int EQ, int FLUX>
 __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* gout, int te,
                                               double dtdx, const OpParams<double>& p) {

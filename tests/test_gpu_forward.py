@@ -271,3 +271,29 @@ def test_clipped_dt_stays_finite_like_the_reference(gb):
     solver.step(1)
     assert solver.status() == 0
     assert float(solver.dt_history()[0, 0]) == float(np.finfo(np.float64).max)
+
+
+def test_autotuned_plan_matches_default_plan(gb, tmp_path, monkeypatch):
+    """The autotuner picks a (tile, CTAs/SM) shape by timing; any shape gives
+    the same states (tiles only change the work split), and the result is
+    cached per batch shape."""
+    from pyshocks_gb300 import autotune
+    from pyshocks_gb300.batched import BatchedSolver
+
+    monkeypatch.setenv("PYSHOCKS_GB300_CACHE", str(tmp_path / "tune.json"))
+    autotune._MEMO.clear()
+    sizes = [3000, 1500, 4096, 700]
+    rng = np.random.default_rng(21)
+    u0 = torch.tensor(np.concatenate([R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes]))
+    scheme = _scheme(gb, "rusanov")
+    dx = [2.0 / n for n in sizes]
+    a = BatchedSolver(scheme, sizes, dx, tile="auto")
+    res = autotune.tune(scheme, sizes, dx)
+    assert (a.tile, a.ctas_per_sm) == (res.tile, res.ctas_per_sm)
+    assert len(res.table) >= 4 and res.ms_per_step == min(r[2] for r in res.table)
+    assert (tmp_path / "tune.json").exists()
+    b = BatchedSolver(scheme, sizes, dx)
+    for s in (a, b):
+        s.reset(u0)
+        s.step(6)
+    assert torch.equal(a.u, b.u)

@@ -148,3 +148,49 @@ def test_learned_adjoint_matches_autograd(dtype):
                                    dts=solver.dt_history().cpu(), rec="learned", weights=wts)
     err = float((g - ref[0]).abs().max() / ref.abs().max())
     assert err < 5.0e-3, err
+
+
+def test_trained_network_gains_over_plain_wenojs_and_untrained():
+    """What training buys. (1) Solver level: the committed network (learned
+    weights in the flux kernel, float64 state) against plain WENO-JS5 (eps
+    1e-6) at N=1024, t=0.4, both measured by L1 against the plain float64
+    solution on a 4x finer grid restricted by averaging. (2) Data level: the
+    face loss on held-out training-style pairs, trained vs the network at
+    initialisation."""
+    from pyshocks_gb300 import burgers, learned, reconstruction
+    from pyshocks_gb300.batched import BatchedSolver
+
+    trained = learned.load_default_params()
+    assert learned.DEFAULT_PARAMS.exists()
+    B, n, r, T = 16, 1024, 4, 0.4
+    rng = np.random.default_rng(31)
+    plain = burgers.Rusanov(rec=reconstruction.WENOJS53(eps=1.0e-6))
+
+    def ic(m):
+        return torch.cat([torch.tensor(R.random_fourier_ic(np.random.default_rng(100 + b),
+                                                           np.linspace(-1, 1, m + 1)))
+                          for b in range(B)])
+
+    def run(scheme, m):
+        s = BatchedSolver(scheme, [m] * B, 2.0 / m)
+        s.reset(ic(m), tfinal=T)
+        while float(s.time().min()) < T:
+            s.step(64)
+        assert s.status() == 0
+        return s.u.reshape(B, m)
+
+    ref = run(plain, n * r).reshape(B, n, r).mean(-1)
+
+    def l1(u):
+        return float((u - ref).abs().sum(-1).mean() * 2.0 / n)
+
+    e_plain = l1(run(plain, n))
+    e_learned = l1(run(burgers.Rusanov(rec=learned.LearnedWENO(params=trained)), n))
+    assert e_learned < 0.95 * e_plain, (e_learned, e_plain)
+    # held-out pairs (seed not used for the committed network)
+    s, t, w = learned.generate_pairs(n_coarse=128, ratio=8, n_ics=8, snapshots=4,
+                                     steps_between=64, seed=12345)
+    lt = learned.Trainer(trained.clone(), reg=0.0)
+    lu = learned.Trainer(learned.init_params(seed=0), reg=0.0)
+    assert float(lt.loss_and_grad(s, t, w)) < 0.9 * float(lu.loss_and_grad(s, t, w))
+    del rng
