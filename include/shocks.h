@@ -34,11 +34,15 @@ typedef enum {
     SHK_ETOOLARGE = 7     /* size beyond the static scratch of a no-allocation call  */
 } shk_status;
 
-/* numerical flux (burgers/schemes.py:98-153,205-256) */
-enum { SHK_FLUX_RUSANOV = 0, SHK_FLUX_LF = 1, SHK_FLUX_ESWENO = 2 };
-/* reconstruction (reconstruction.py:335-348,386-439); SHK_REC_LEARNED: learned
- * WENO weights (an MLP over the normalised stencil, float32 state only) */
-enum { SHK_REC_WENOJS53 = 0, SHK_REC_ESWENO32 = 1, SHK_REC_LEARNED = 2 };
+/* numerical flux (burgers/schemes.py:71-96,98-153,160-196,205-256);
+ * SHK_FLUX_GODUNOV (upwind, scalar.py:91-132) and SHK_FLUX_EO (Engquist-Osher,
+ * scalar.py:287-322, omega = 0) are Burgers fluxes */
+enum { SHK_FLUX_RUSANOV = 0, SHK_FLUX_LF = 1, SHK_FLUX_ESWENO = 2, SHK_FLUX_GODUNOV = 3,
+       SHK_FLUX_EO = 4 };
+/* reconstruction (reconstruction.py:128-163,320-348,386-439); SHK_REC_LEARNED:
+ * learned WENO weights (an MLP over the normalised stencil) */
+enum { SHK_REC_WENOJS53 = 0, SHK_REC_ESWENO32 = 1, SHK_REC_LEARNED = 2, SHK_REC_CONSTANT = 3,
+       SHK_REC_WENOJS32 = 4 };
 /* physical flux f(u) and wave speed f'(u) */
 enum { SHK_EQ_BURGERS = 0, SHK_EQ_ADVECTION = 1, SHK_EQ_LWR = 2 };
 /* state precision */

@@ -291,9 +291,11 @@ class SchemeSpec:
     """A plain description of a scheme on the hot path.
 
     * ``flux_kind``: ``"rusanov"`` (``burgers/schemes.py:110-118``),
-      ``"lf"`` (``burgers/schemes.py:145-153``) or ``"esweno"``
-      (``burgers/schemes.py:230-256``).
-    * ``rec``: ``"wenojs53"``, ``"wenojs32"`` or ``"esweno32"``.
+      ``"lf"`` (``burgers/schemes.py:145-153``), ``"esweno"``
+      (``burgers/schemes.py:230-256``), ``"godunov"`` (``burgers/schemes.py:83-89``)
+      or ``"eo"`` (``burgers/schemes.py:188-196``).
+    * ``rec``: ``"wenojs53"``, ``"wenojs32"``, ``"esweno32"`` or ``"constant"``
+      (``reconstruction.py:153-163``).
     * ``equation``: ``"burgers"``, ``"advection"`` or ``"lwr"``.
     """
 
@@ -312,6 +314,8 @@ class SchemeSpec:
 
 
 def reconstruct(spec: SchemeSpec, f: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    if spec.rec == "constant":
+        return f, f
     if spec.rec == "esweno32":
         return reconstruct_esweno32(spec.stencil, spec.eps, f)
     return reconstruct_wenojs(spec.stencil, spec.eps, f)
@@ -338,6 +342,14 @@ def numerical_flux(spec: SchemeSpec, grid: CellGrid, u: np.ndarray) -> np.ndarra
         a = speed(u)
         al, ar = reconstruct(spec, a)
         return scalar_flux_upwind(ul, ur, al, ar, flux)
+    if spec.flux_kind == "eo":
+        # scalar.py:287-322 with omega = 0 (burgers/schemes.py:184-196)
+        ul, ur = reconstruct(spec, u)
+        omega = 0.0
+        fr = flux(np.maximum(ur, omega))
+        fl = flux(np.minimum(ul, omega))
+        fomega = flux(np.full(u.size - 1, omega))
+        return np.pad(fr[:-1] + fl[1:] - fomega, 1)
     if spec.flux_kind == "esweno":
         # burgers/schemes.py:230-256
         s = weno_js_32_coefficients()

@@ -62,6 +62,24 @@ def weno53(u: torch.Tensor, eps: float) -> tuple[torch.Tensor, torch.Tensor]:
 _D32 = (1.0 / 3.0, 2.0 / 3.0)
 
 
+def weno32_side(u: torch.Tensor, eps: float) -> torch.Tensor:
+    """WENO-JS 3/2 value at ``x_{i+1/2}`` from cell ``i`` (``weno.py:166-203``,
+    ``:247-256``): beta = ((u_i - u_{i-1})^2, (u_{i+1} - u_i)^2),
+    uhat = (3/2 u_i - 1/2 u_{i-1}, 1/2 (u_i + u_{i+1}))."""
+    um1, u0, up1 = _sh(u, -1), u, _sh(u, 1)
+    a0 = _D32[0] / (eps + (u0 - um1) ** 2) ** 2
+    a1 = _D32[1] / (eps + (up1 - u0) ** 2) ** 2
+    s = a0 + a1
+    return (a0 / s) * (1.5 * u0 - 0.5 * um1) + (a1 / s) * (0.5 * up1 + 0.5 * u0)
+
+
+def weno32(u: torch.Tensor, eps: float) -> tuple[torch.Tensor, torch.Tensor]:
+    """``(ul, ur)`` of WENO-JS 3/2 (``reconstruction.py:358-377``)."""
+    ur = weno32_side(u, eps)
+    ul = torch.flip(weno32_side(torch.flip(u, dims=(-1,)), eps), dims=(-1,))
+    return ul, ur
+
+
 def _es_weno32_weights(u: torch.Tensor, eps: float) -> tuple[torch.Tensor, torch.Tensor]:
     """ES-WENO weights (``src/pyshocks/weno.py:284-296``) of the right side."""
     um1, u0, up1 = _sh(u, -1), u, _sh(u, 1)
@@ -124,6 +142,11 @@ def face_flux(
         ul, ur = weno53(u, eps)
     elif rec == "esweno32":
         ul, ur = esweno32(u, eps)
+    elif rec == "wenojs32":
+        ul, ur = weno32(u, eps)
+    elif rec == "constant":
+        # reconstruction.py:153-163
+        ul, ur = u, u
     elif rec == "learned":
         from oracle.learned_ref import learned_recon
 
@@ -144,6 +167,16 @@ def face_flux(
             amax = torch.maximum(_sh(a, 1), a)
         # src/pyshocks/scalar.py:248
         return 0.5 * (fl + fr) - 0.5 * amax * (ulp - ur)
+    if flux_kind == "godunov":
+        # src/pyshocks/scalar.py:91-132 with a = u (burgers/schemes.py:83-89):
+        # the reconstructed speeds are the reconstructed states
+        return torch.where((ur + ulp) / 2 > 0, fr, fl)
+    if flux_kind == "eo":
+        # src/pyshocks/scalar.py:287-322, omega = 0 (burgers/schemes.py:184-196)
+        zero = torch.zeros_like(u)
+        return (physical_flux(equation, torch.maximum(ur, zero))
+                + physical_flux(equation, torch.minimum(ulp, zero))
+                - physical_flux(equation, zero))
     if flux_kind == "esweno":
         # src/pyshocks/scalar.py:91-132 upwind with a = u, then the ES-WENO
         # dissipation of src/pyshocks/burgers/schemes.py:242-256

@@ -24,8 +24,8 @@ SHK_ENOMEM = 5
 SHK_EUNSUPPORTED = 6
 SHK_ETOOLARGE = 7
 
-SHK_FLUX_RUSANOV, SHK_FLUX_LF, SHK_FLUX_ESWENO = 0, 1, 2
-SHK_REC_WENOJS53, SHK_REC_ESWENO32, SHK_REC_LEARNED = 0, 1, 2
+SHK_FLUX_RUSANOV, SHK_FLUX_LF, SHK_FLUX_ESWENO, SHK_FLUX_GODUNOV, SHK_FLUX_EO = 0, 1, 2, 3, 4
+SHK_REC_WENOJS53, SHK_REC_ESWENO32, SHK_REC_LEARNED, SHK_REC_CONSTANT, SHK_REC_WENOJS32 = 0, 1, 2, 3, 4
 SHK_EQ_BURGERS, SHK_EQ_ADVECTION, SHK_EQ_LWR = 0, 1, 2
 SHK_F64, SHK_F32 = 0, 1
 

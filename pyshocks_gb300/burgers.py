@@ -83,6 +83,27 @@ def _flux_burgers(scheme, t, x, u):
 
 
 @dataclass(frozen=True)
+class Godunov(BurgersScheme):
+    """Godunov (upwind) scheme, ``src/pyshocks/burgers/schemes.py:71-89``: the
+    upwind flux of ``src/pyshocks/scalar.py:91-132`` with ``a = u``."""
+
+    flux_code: ClassVar[int] = L.SHK_FLUX_GODUNOV
+
+
+@dataclass(frozen=True)
+class EngquistOsher(BurgersScheme):
+    """Engquist-Osher scheme, ``src/pyshocks/burgers/schemes.py:160-196``:
+    ``f(max(ul, w)) + f(min(ur, w)) - f(w)`` with ``w = 0`` the minimum of the
+    convex Burgers flux (``src/pyshocks/scalar.py:287-322``)."""
+
+    flux_code: ClassVar[int] = L.SHK_FLUX_EO
+
+    @property
+    def omega(self) -> float:
+        return 0.0
+
+
+@dataclass(frozen=True)
 class Rusanov(BurgersScheme):
     """``src/pyshocks/burgers/schemes.py:98-107``."""
 
@@ -250,8 +271,10 @@ def ssprk33_step(scheme, grid: Grid, bc: Boundary, dt: float, u: torch.Tensor) -
 
 _SCHEMES: dict[str, type[SchemeBase]] = {
     "default": LaxFriedrichs,
+    "godunov": Godunov,
     "rusanov": Rusanov,
     "lf": LaxFriedrichs,
+    "eo": EngquistOsher,
     "esweno32": ESWENO32,
 }
 

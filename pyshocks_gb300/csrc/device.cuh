@@ -221,6 +221,20 @@ __device__ __forceinline__ void esweno32_cell(T vm1, T v, T vp1, T eps, T& ul, T
     ul = (al0 / sl) * (T(1.5) * v - T(0.5) * vp1) + (al1 / sl) * (T(0.5) * vm1 + T(0.5) * v);
 }
 
+// WENO-JS3 (weno.py:166-203, weights weno.py:247-256) of cell c: right face
+// from v_{c-1..c+1} with beta = ((v_c - v_{c-1})^2, (v_{c+1} - v_c)^2), uhat =
+// (v + dm/2, v + dp/2), d = (1/3, 2/3); left face on the mirrored stencil. The
+// weights are in product form (alpha_k s_0^2 s_1^2 3): one division per face.
+template <class T>
+__device__ __forceinline__ void weno32_cell(T vm1, T v, T vp1, T eps, T& ul, T& ur) {
+    const T dm = v - vm1, dp = vp1 - v;
+    T s0 = fma(dm, dm, eps), s1 = fma(dp, dp, eps);
+    s0 = s0 * s0;
+    s1 = s1 * s1;
+    ur = fma(T(0.5) * fma(s1, dm, T(2) * s0 * dp), T(1) / fma(T(2), s0, s1), v);
+    ul = fma(T(-0.5) * fma(s0, dp, T(2) * s1 * dm), T(1) / fma(T(2), s1, s0), v);
+}
+
 // ---- numerical fluxes at face j+1/2 -----------------------------------------
 // R = ur_j, L = ul_{j+1}, vj, vj1 cell values.
 template <int EQ, class T>
@@ -257,6 +271,22 @@ __device__ __forceinline__ T esweno_face(T R, T L, T vj, T vj1, T w0j, T w0j1, T
     const T mu = sqrt(dw * dw + delta * delta) / T(8);
     const T g = -(mu + dw / T(8)) * (vj1 - vj);
     return fnum + g;
+}
+
+// Godunov / upwind (scalar.py:91-132 with a = u, burgers/schemes.py:83-89):
+// the reconstructed speeds are the reconstructed states, S = (R + L)/2
+template <int EQ, class T>
+__device__ __forceinline__ T godunov_face(T R, T L, T c) {
+    const T aavg = (wave_speed<EQ>(R, c) + wave_speed<EQ>(L, c)) / T(2);
+    return aavg > T(0) ? phys_flux<EQ>(R, c) : phys_flux<EQ>(L, c);
+}
+
+// Engquist-Osher for a convex flux with its minimum at omega = 0
+// (scalar.py:287-322, burgers/schemes.py:184-196): f(max(R, 0)) + f(min(L, 0)) - f(0)
+template <int EQ, class T>
+__device__ __forceinline__ T eo_face(T R, T L, T c) {
+    return phys_flux<EQ>(fmax(R, T(0)), c) + phys_flux<EQ>(fmin(L, T(0)), c) -
+           phys_flux<EQ>(T(0), c);
 }
 
 // ---- mbarrier / bulk copy (inline PTX) -------------------------------------

@@ -307,11 +307,18 @@ int cuda_check(cudaError_t e) {
 
 bool valid_scheme(const shk_scheme* s) {
     if (!s) return false;
-    if (s->flux < 0 || s->flux > SHK_FLUX_ESWENO) return false;
-    if (s->rec < 0 || s->rec > SHK_REC_LEARNED) return false;
+    if (s->flux < 0 || s->flux > SHK_FLUX_EO) return false;
+    if (s->rec < 0 || s->rec > SHK_REC_WENOJS32) return false;
     if (s->equation < 0 || s->equation > SHK_EQ_LWR) return false;
     if ((s->flux == SHK_FLUX_ESWENO) != (s->rec == SHK_REC_ESWENO32)) return false;
     if (s->rec == SHK_REC_LEARNED && (s->flux != SHK_FLUX_RUSANOV || !s->mlp)) return false;
+    // the upwind and Engquist-Osher fluxes are the reference's Burgers schemes;
+    // the constant and WENO-JS3 reconstructions run with Rusanov, Godunov or EO
+    if ((s->flux == SHK_FLUX_GODUNOV || s->flux == SHK_FLUX_EO) &&
+        (s->equation != SHK_EQ_BURGERS || s->rec == SHK_REC_LEARNED))
+        return false;
+    if ((s->rec == SHK_REC_CONSTANT || s->rec == SHK_REC_WENOJS32) && s->flux == SHK_FLUX_LF)
+        return false;
     return true;
 }
 
@@ -343,11 +350,34 @@ int sm_count() {
 }
 
 // dispatch helpers: call F.template operator()<T, EQ, REC, FLUX>()
+// Burgers with the Godunov / Engquist-Osher flux and a WENO-JS5, WENO-JS3 or
+// constant reconstruction
+template <class T, class F>
+int dispatch_upwind(const shk_scheme* s, F&& f) {
+    constexpr int EQ = SHK_EQ_BURGERS;
+    if (s->flux == SHK_FLUX_GODUNOV) {
+        if (s->rec == SHK_REC_CONSTANT) return f.template operator()<T, EQ, SHK_REC_CONSTANT, SHK_FLUX_GODUNOV>();
+        if (s->rec == SHK_REC_WENOJS32) return f.template operator()<T, EQ, SHK_REC_WENOJS32, SHK_FLUX_GODUNOV>();
+        return f.template operator()<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_GODUNOV>();
+    }
+    if (s->rec == SHK_REC_CONSTANT) return f.template operator()<T, EQ, SHK_REC_CONSTANT, SHK_FLUX_EO>();
+    if (s->rec == SHK_REC_WENOJS32) return f.template operator()<T, EQ, SHK_REC_WENOJS32, SHK_FLUX_EO>();
+    return f.template operator()<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_EO>();
+}
+
 template <class T, class F>
 int dispatch_scheme(const shk_scheme* s, F&& f) {
     switch (s->equation) {
 #define SHK_EQ_CASE(EQ)                                                                 \
     case EQ:                                                                            \
+        if constexpr (EQ == SHK_EQ_BURGERS) {                                           \
+            if (s->flux == SHK_FLUX_GODUNOV || s->flux == SHK_FLUX_EO)                  \
+                return dispatch_upwind<T>(s, f);                                        \
+        }                                                                               \
+        if (s->rec == SHK_REC_CONSTANT)                                                 \
+            return f.template operator()<T, EQ, SHK_REC_CONSTANT, SHK_FLUX_RUSANOV>();  \
+        if (s->rec == SHK_REC_WENOJS32)                                                 \
+            return f.template operator()<T, EQ, SHK_REC_WENOJS32, SHK_FLUX_RUSANOV>();  \
         if (s->rec == SHK_REC_LEARNED)                                                  \
             return f.template operator()<T, EQ, SHK_REC_LEARNED, SHK_FLUX_RUSANOV>();   \
         if (s->rec == SHK_REC_ESWENO32) return f.template operator()<T, EQ, SHK_REC_ESWENO32, SHK_FLUX_ESWENO>(); \

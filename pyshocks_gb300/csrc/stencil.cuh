@@ -195,6 +195,21 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
     } else if constexpr (REC == SHK_REC_LEARNED) {
         learned_phase<T>(v, lo - 1, hi + 1, sm.UL, sm.UR, reinterpret_cast<float*>(sm.H), p.lp);
         __syncthreads();
+    } else if constexpr (REC == SHK_REC_CONSTANT) {
+        // reconstruction.py:153-163: ul = ur = u
+        for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
+            sm.UL[c] = v[c];
+            sm.UR[c] = v[c];
+        }
+        __syncthreads();
+    } else if constexpr (REC == SHK_REC_WENOJS32) {
+        for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
+            T ul, ur;
+            weno32_cell<T>(v[c - 1], v[c], v[c + 1], p.eps, ul, ur);
+            sm.UL[c] = ul;
+            sm.UR[c] = ur;
+        }
+        __syncthreads();
     } else {
         for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
             T ul, ur, w0;
@@ -221,6 +236,10 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
             f = rusanov_face<EQ, T>(sm.UR[j], sm.UL[j + 1], v[j], v[j + 1], p.hnu, p.c);
         } else if constexpr (FLUX == SHK_FLUX_LF) {
             f = lf_face<EQ, T>(sm.UR[j], sm.UL[j + 1], p.hnu_amax, p.c);
+        } else if constexpr (FLUX == SHK_FLUX_GODUNOV) {
+            f = godunov_face<EQ, T>(sm.UR[j], sm.UL[j + 1], p.c);
+        } else if constexpr (FLUX == SHK_FLUX_EO) {
+            f = eo_face<EQ, T>(sm.UR[j], sm.UL[j + 1], p.c);
         } else {
             f = esweno_face<EQ, T>(sm.UR[j], sm.UL[j + 1], v[j], v[j + 1], sm.Q[j], sm.Q[j + 1],
                                    p.delta, p.c);

@@ -31,6 +31,26 @@ class Reconstruction:
 
 
 @dataclass(frozen=True)
+class ConstantReconstruction(Reconstruction):
+    """First-order constant reconstruction, ``ul = ur = u``
+    (``src/pyshocks/reconstruction.py:128-163``)."""
+
+    @property
+    def name(self) -> str:
+        return "constant"
+
+    @property
+    def order(self) -> int:
+        return 1
+
+    @property
+    def stencil_width(self) -> int:
+        return 1
+
+    code = L.SHK_REC_CONSTANT
+
+
+@dataclass(frozen=True)
 class WENOJS(Reconstruction):
     """``src/pyshocks/reconstruction.py:305-317``."""
 
@@ -39,6 +59,20 @@ class WENOJS(Reconstruction):
     @property
     def stencil_width(self) -> int:
         return self.order
+
+
+@dataclass(frozen=True)
+class WENOJS32(WENOJS):
+    """Third-order WENO-JS, second order in non-smooth regions
+    (``src/pyshocks/reconstruction.py:320-333``)."""
+
+    eps: float = 1.0e-6
+
+    @property
+    def order(self) -> int:
+        return 2
+
+    code = L.SHK_REC_WENOJS32
 
 
 @dataclass(frozen=True)
@@ -73,6 +107,9 @@ class ESWENO32(Reconstruction):
 
 
 _RECONSTRUCTION: dict[str, type[Reconstruction]] = {
+    "default": ConstantReconstruction,
+    "constant": ConstantReconstruction,
+    "wenojs32": WENOJS32,
     "wenojs53": WENOJS53,
     "esweno32": ESWENO32,
 }

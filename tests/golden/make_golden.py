@@ -121,7 +121,10 @@ def main(refdir: pathlib.Path) -> None:
         if kind == "lwr":
             rec = reconstruction.make_reconstruction_from_name("wenojs53", eps=1.0e-6)
             return LWRRusanov(rec=rec)
-        raise ValueError(kind)
+        # "<scheme>-<reconstruction>": the other Burgers fluxes and reconstructions
+        sname, rname = kind.split("-")
+        rec = reconstruction.make_reconstruction_from_name(rname, eps=1.0e-6)
+        return burgers.make_scheme_from_name(sname, rec=rec)
 
     bc = PeriodicBoundary()
 
@@ -181,6 +184,13 @@ def main(refdir: pathlib.Path) -> None:
     out["fourier_lf_n64_s21"] = run("lf", 64, fourier_ic(21), maxit=40)
     out["fourier_esweno_n64_s22"] = run("esweno", 64, fourier_ic(22), maxit=40)
     out["lwr_rusanov_n128_s31"] = run("lwr", 128, lwr_ic(31), maxit=60)
+    # Godunov / Engquist-Osher fluxes and the constant / WENO-JS32 reconstructions
+    out["config1_godunov_wenojs53_n256"] = run("godunov-wenojs53", 256, sine_ic, tfinal=1.0)
+    out["config1_eo_wenojs53_n256"] = run("eo-wenojs53", 256, sine_ic, tfinal=1.0)
+    for sname in ("rusanov", "godunov", "eo"):
+        for rname, seed in (("constant", 41), ("wenojs32", 42)):
+            out[f"fourier_{sname}_{rname}_n96_s{seed}"] = run(f"{sname}-{rname}", 96,
+                                                               fourier_ic(seed), maxit=40)
 
     # }}}
 

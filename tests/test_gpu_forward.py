@@ -34,6 +34,11 @@ def gb():
 def _scheme(gb, kind, eq="burgers", eps=1.0e-6):
     from pyshocks_gb300 import burgers
 
+    if "-" in kind:
+        # "<flux>-<reconstruction>": the other Burgers fluxes and reconstructions
+        sname, rname = kind.split("-")
+        rec = gb.reconstruction.make_reconstruction_from_name(rname, eps=eps)
+        return burgers.make_scheme_from_name(sname, rec=rec)
     rec = gb.reconstruction.make_reconstruction_from_name("wenojs53", eps=eps)
     if kind == "rusanov":
         return burgers.Rusanov(rec=rec) if eq == "burgers" else (
@@ -46,6 +51,9 @@ def _scheme(gb, kind, eq="burgers", eps=1.0e-6):
 
 
 def _oracle_spec(kind, eq="burgers", eps=1.0e-6, grid=None):
+    if "-" in kind:
+        f, r = kind.split("-")
+        return R.SchemeSpec(flux_kind=f, rec=r, eps=eps, equation=eq)
     if kind == "esweno":
         e, d = R.es_weno_parameters(grid, np.ones_like(grid.x))
         return R.SchemeSpec(flux_kind="esweno", rec="esweno32", eps=e, delta=d, equation=eq)
@@ -63,6 +71,14 @@ CASES = [
     ("esweno", "burgers", 777),
     ("rusanov", "lwr", 512),
     ("rusanov", "advection", 300),
+    ("godunov-wenojs53", "burgers", 300),
+    ("eo-wenojs53", "burgers", 257),
+    ("godunov-constant", "burgers", 128),
+    ("eo-constant", "burgers", 1200),
+    ("godunov-wenojs32", "burgers", 640),
+    ("eo-wenojs32", "burgers", 96),
+    ("rusanov-constant", "burgers", 200),
+    ("rusanov-wenojs32", "burgers", 2049),
 ]
 
 
@@ -112,7 +128,9 @@ def test_fused_step_matches_oracle(gb, kind, eq, n):
 
 @pytest.mark.parametrize("name,kind", [("config1_rusanov_n256", "rusanov"),
                                        ("config1_esweno_n256", "esweno"),
-                                       ("config1_lf_n256", "lf")])
+                                       ("config1_lf_n256", "lf"),
+                                       ("config1_godunov_wenojs53_n256", "godunov-wenojs53"),
+                                       ("config1_eo_wenojs53_n256", "eo-wenojs53")])
 def test_config1_step_api_matches_reference(gb, name, kind):
     """N=256 Burgers to t_final = 1 through the reference-style ``step()`` API:
     within 1e-10 max-abs of the reference's own solution (golden vectors from
@@ -297,3 +315,23 @@ def test_autotuned_plan_matches_default_plan(gb, tmp_path, monkeypatch):
         s.reset(u0)
         s.step(6)
     assert torch.equal(a.u, b.u)
+
+
+@pytest.mark.parametrize("flux_kind", ["rusanov", "godunov", "eo"])
+@pytest.mark.parametrize(("rname", "seed"), [("constant", 41), ("wenojs32", 42)])
+def test_batched_other_schemes_match_reference(gb, flux_kind, rname, seed):
+    """The reference's own 40-step runs (golden vectors from its source) of the
+    Godunov / Engquist-Osher / Rusanov Burgers schemes with the constant and
+    WENO-JS3 reconstructions, through the batched plan with the reference's
+    dt sequence prescribed, and the plan's own CFL steps against its dts."""
+    from pyshocks_gb300.batched import BatchedSolver
+
+    g = _golden(f"fourier_{flux_kind}_{rname}_n96_s{seed}")
+    n = int(g["n"])
+    scheme = _scheme(gb, f"{flux_kind}-{rname}")
+    s = BatchedSolver(scheme, [n], 2.0 / n, max_steps=len(g["dts"]))
+    s.reset(torch.tensor(g["u0"][3:-3]))
+    s.step(len(g["dts"]))
+    np.testing.assert_allclose(s.dt_history().cpu().numpy()[:, 0], g["dts"], rtol=1e-13, atol=0)
+    err = np.max(np.abs(s.u.cpu().numpy() - g["u"][3:-3]))
+    assert err < 1.0e-12, err

@@ -23,7 +23,9 @@ GOLDEN = pathlib.Path(__file__).parent / "golden"
 
 
 def _load(name):
-    return dict(np.load(GOLDEN / f"{name}.npz"))
+    g = dict(np.load(GOLDEN / f"{name}.npz"))
+    g["__name__"] = name
+    return g
 
 
 # {{{ golden vectors from the reference
@@ -60,14 +62,19 @@ RUNS = [
     ("fourier_lf_n64_s21", "lf", "burgers", {"maxit": 40}),
     ("fourier_esweno_n64_s22", "esweno", "burgers", {"maxit": 40}),
     ("lwr_rusanov_n128_s31", "rusanov", "lwr", {"maxit": 60}),
-]
+    ("config1_godunov_wenojs53_n256", "godunov", "burgers", {"tfinal": 1.0}),
+    ("config1_eo_wenojs53_n256", "eo", "burgers", {"tfinal": 1.0}),
+] + [(f"fourier_{f}_{r}_n96_s{s}", f, "burgers", {"maxit": 40})
+     for f in ("rusanov", "godunov", "eo") for r, s in (("constant", 41), ("wenojs32", 42))]
 
 
 def _spec(g, flux_kind, equation):
     if flux_kind == "esweno":
         return R.SchemeSpec(flux_kind="esweno", rec="esweno32", eps=float(g["eps"]),
                             delta=float(g["delta"]), equation=equation)
-    return R.SchemeSpec(flux_kind=flux_kind, rec="wenojs53", eps=1.0e-6, equation=equation)
+    name = str(g.get("__name__", ""))
+    rec = "constant" if "_constant_" in name else ("wenojs32" if "_wenojs32_" in name else "wenojs53")
+    return R.SchemeSpec(flux_kind=flux_kind, rec=rec, eps=1.0e-6, equation=equation)
 
 
 @pytest.mark.parametrize(("name", "flux_kind", "equation", "kw"), RUNS)
