@@ -69,6 +69,21 @@ typedef struct {
                         * means 1e-12 */
 } shk_scheme;
 
+/* Boundary conditions (scalar.py:397-540). Periodic is the default of every
+ * entry point. Dirichlet sets the 3 ghost cells of a side to g_d(t, x) at
+ * their centres (scalar.py:419-429); Neumann mirrors the interior about the
+ * boundary face, ghost k = u_mirror - (2k + 1) dx g_n(t) (scalar.py:469-495).
+ * The boundary is applied before every operator evaluation, at the stage
+ * times of the call: t for apply_operator; t, t + dt, t + dt/2 for an SSPRK33
+ * step (timestepping.py:312-320 via schemes.py:339-346). */
+enum { SHK_BC_PERIODIC = 0, SHK_BC_DIRICHLET = 1, SHK_BC_NEUMANN = 2 };
+typedef struct {
+    int32_t left, right;        /* SHK_BC_* of each side (periodic: both or neither) */
+    double dirichlet[3][2][3];  /* g_d(t_s, x) [stage][side 0 left / 1 right][k], k = 0
+                                 * the ghost next to the interior */
+    double neumann[3][2];       /* g_n(t_s) [stage][side] */
+} shk_boundary;
+
 const char* shk_strerror(int status);
 int shk_version(void);
 
@@ -101,6 +116,18 @@ int shk_predict_timestep_f64(const shk_scheme* scheme, const double* u, int64_t 
 int shk_ssprk33_step_f64(const shk_scheme* scheme, const double* u, double* u_out,
                          int64_t n, int32_t nghosts, double dx, double dt,
                          void* stream);
+
+/* shk_apply_operator_f64 / shk_ssprk33_step_f64 with the boundary `bc`
+ * (NULL: periodic) at the stage time(s) of the call. Output ghost cells:
+ * apply_operator writes 0 there (the reference's values are unspecified and
+ * overwritten by its next apply_boundary); the step writes the boundary at
+ * t + dt (stage 1 data). */
+int shk_apply_operator_bc_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
+                              double* out, int64_t n, int32_t nghosts, double dx,
+                              const double* amax, void* stream);
+int shk_ssprk33_step_bc_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
+                            double* u_out, int64_t n, int32_t nghosts, double dx, double dt,
+                            void* stream);
 
 /* ---- batched plans ----------------------------------------------------- */
 
@@ -151,6 +178,15 @@ int shk_plan_step(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps, void* st
  * history (shk_plan_copy_dt_history) replays exactly. nsteps = 0 returns to
  * CFL steps. Drops a captured step graph. */
 int shk_plan_set_fixed_dt(shk_plan* plan, const double* dt, int32_t nsteps, void* stream);
+
+/* time-independent Dirichlet / Neumann boundaries for every instance of the
+ * plan: dirichlet [B][2][3] ghost values, neumann [B][2] gradients (device or
+ * host memory, copied on `stream`; either may be NULL if no side uses it).
+ * left = right = SHK_BC_PERIODIC restores periodic instances. Plans with a
+ * non-periodic boundary step forward only (shk_plan_adjoint:
+ * SHK_EUNSUPPORTED). Drops a captured step graph. */
+int shk_plan_set_boundary(shk_plan* plan, int32_t left, int32_t right, const double* dirichlet,
+                          const double* neumann, void* stream);
 
 /* capture two steps (u_a -> u_b -> u_a) into a CUDA graph and replay it
  * nsteps/2 times (nsteps must be even). */

@@ -205,6 +205,36 @@ def apply_boundary_periodic(u: np.ndarray, g: int) -> np.ndarray:
     return u
 
 
+def apply_boundary_dirichlet(u: np.ndarray, grid: "CellGrid", t: float, ga: Callable,
+                             gb: Callable) -> np.ndarray:
+    """Dirichlet ghost fill (``src/pyshocks/scalar.py:419-429``): the ghost
+    cells of each side take ``g(t, x)`` at their centres (left, then right,
+    as ``TwoSidedBoundary`` applies them, ``scalar.py:373-382``)."""
+    u = u.copy()
+    g = grid.nghosts
+    u[:g] = ga(t, grid.x[:g])
+    u[u.size - g:] = gb(t, grid.x[u.size - g:])
+    return u
+
+
+def apply_boundary_neumann(u: np.ndarray, grid: "CellGrid", t: float, ga: Callable,
+                           gb: Callable) -> np.ndarray:
+    """Neumann ghost fill (``src/pyshocks/scalar.py:469-495``): ghost cells
+    mirrored about the boundary face, ``u_from + side (x_from - x_to) g(t)``."""
+    u = u.copy()
+    g = grid.nghosts
+    n = u.size
+    for side, fn in ((-1, ga), (+1, gb)):
+        if side == -1:
+            ifrom = np.arange(g, 2 * g)
+            ito = np.arange(g - 1, -1, -1)
+        else:
+            ifrom = np.arange(n - 2 * g, n - g)
+            ito = np.arange(n - 1, n - g - 1, -1)
+        u[ito] = u[ifrom] + side * (grid.x[ifrom] - grid.x[ito]) * fn(t)
+    return u
+
+
 # }}}
 
 
@@ -363,9 +393,11 @@ def numerical_flux(spec: SchemeSpec, grid: CellGrid, u: np.ndarray) -> np.ndarra
     raise ValueError(f"unknown flux kind: {spec.flux_kind!r}")
 
 
-def apply_operator(spec: SchemeSpec, grid: CellGrid, u: np.ndarray) -> np.ndarray:
-    """``src/pyshocks/schemes.py:339-346`` with periodic boundaries."""
-    u = apply_boundary_periodic(u, grid.nghosts)
+def apply_operator(spec: SchemeSpec, grid: CellGrid, u: np.ndarray, t: float = 0.0,
+                   bc: Callable | None = None) -> np.ndarray:
+    """``src/pyshocks/schemes.py:339-346``; *bc* ``(t, u) -> u`` fills the
+    ghost cells (periodic by default)."""
+    u = apply_boundary_periodic(u, grid.nghosts) if bc is None else bc(t, u)
     f = numerical_flux(spec, grid, u)
     return -(f[1:] - f[:-1]) / grid.dx
 
@@ -458,6 +490,7 @@ def evolve(
     theta: float = 1.0,
     maxit: int | None = None,
     tfinal: float | None = None,
+    bc: Callable | None = None,
 ) -> tuple[np.ndarray, list[float]]:
     """Run :func:`step` with the driver closures of ``examples/burgers.py:161-178``
     (``dt = theta * predict_timestep``); return the final state and the
@@ -467,7 +500,7 @@ def evolve(
         return theta * predict_timestep(spec, grid, u)
 
     def _source(t, u):
-        return apply_operator(spec, grid, u)
+        return apply_operator(spec, grid, u, t, bc)
 
     dts = []
     event = None

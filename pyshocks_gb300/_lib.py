@@ -53,6 +53,18 @@ class ShkScheme(ctypes.Structure):
     ]
 
 
+SHK_BC_PERIODIC, SHK_BC_DIRICHLET, SHK_BC_NEUMANN = 0, 1, 2
+
+
+class ShkBoundary(ctypes.Structure):
+    _fields_ = [
+        ("left", ctypes.c_int32),
+        ("right", ctypes.c_int32),
+        ("dirichlet", ctypes.c_double * 18),  # [stage][side][k]
+        ("neumann", ctypes.c_double * 6),     # [stage][side]
+    ]
+
+
 class ShkPlanOpts(ctypes.Structure):
     _fields_ = [
         ("dtype", ctypes.c_int32),
@@ -76,6 +88,10 @@ SIGNATURES: dict[str, tuple] = {
     "shk_apply_operator_f64": (ctypes.c_int, [_SCH, _P, _P, _I64, _I32, _D, _P, _P]),
     "shk_predict_timestep_f64": (ctypes.c_int, [_SCH, _P, _I64, _I32, _D, _D, _P, _P]),
     "shk_ssprk33_step_f64": (ctypes.c_int, [_SCH, _P, _P, _I64, _I32, _D, _D, _P]),
+    "shk_apply_operator_bc_f64": (ctypes.c_int, [_SCH, ctypes.POINTER(ShkBoundary), _P, _P, _I64,
+                                                 _I32, _D, _P, _P]),
+    "shk_ssprk33_step_bc_f64": (ctypes.c_int, [_SCH, ctypes.POINTER(ShkBoundary), _P, _P, _I64,
+                                               _I32, _D, _D, _P]),
     "shk_plan_create": (
         ctypes.c_int,
         [_SCH, _I32, _P, _P, _P, _D, ctypes.POINTER(ShkPlanOpts), ctypes.POINTER(_P)],
@@ -85,6 +101,7 @@ SIGNATURES: dict[str, tuple] = {
     "shk_plan_step": (ctypes.c_int, [_P, _P, _P, _I32, _P]),
     "shk_plan_step_graph": (ctypes.c_int, [_P, _P, _P, _I32, _P]),
     "shk_plan_set_fixed_dt": (ctypes.c_int, [_P, _P, _I32, _P]),
+    "shk_plan_set_boundary": (ctypes.c_int, [_P, _I32, _I32, _P, _P, _P]),
     "shk_plan_state": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "shk_plan_copy_time": (ctypes.c_int, [_P, _P, _P]),
     "shk_plan_copy_dt_history": (ctypes.c_int, [_P, _P, _P]),

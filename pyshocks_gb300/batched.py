@@ -181,6 +181,33 @@ class BatchedSolver:
         )
         self._keep = (t0d, tfd)
 
+    def set_boundary(self, left: str = "periodic", right: str | None = None, *,
+                     dirichlet=None, neumann=None) -> None:
+        """Time-independent boundaries of every instance (``"periodic"``,
+        ``"dirichlet"`` or ``"neumann"`` per side; periodic on both sides or
+        on neither). *dirichlet*: ghost values ``(B, 2, 3)`` (side, then the
+        ghost next to the interior first), or ``(2,)`` per side for all
+        ghosts and instances; *neumann*: gradients ``(B, 2)`` or ``(2,)``.
+        Plans with non-periodic boundaries step forward only."""
+        kinds = {"periodic": L.SHK_BC_PERIODIC, "dirichlet": L.SHK_BC_DIRICHLET,
+                 "neumann": L.SHK_BC_NEUMANN}
+        right = left if right is None else right
+        lk, rk = kinds[left], kinds[right]
+
+        def table(v, shape):
+            if v is None:
+                return None
+            t = torch.as_tensor(v, dtype=torch.float64, device=self.device)
+            if t.dim() == 1 and t.numel() == 2:
+                t = t.reshape((1, 2) + (1,) * (len(shape) - 2)).expand((self.B,) + shape[1:])
+            return t.reshape(shape).contiguous()
+
+        d = table(dirichlet, (self.B, 2, 3))
+        nm = table(neumann, (self.B, 2))
+        L.check(self.lib.shk_plan_set_boundary(self._plan, lk, rk, L.ptr(d), L.ptr(nm),
+                                               L.stream_handle()), "plan_set_boundary")
+        self._bc_keep = (d, nm)
+
     def set_fixed_dt(self, dt=None, nsteps: int | None = None) -> None:
         """Prescribe the time steps instead of the CFL step.
 

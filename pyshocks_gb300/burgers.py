@@ -11,6 +11,8 @@ class: Burgers ``u^2/2`` (``burgers/schemes.py:37-39``), linear advection
 
 from __future__ import annotations
 
+import ctypes
+
 from dataclasses import dataclass, fields, replace
 from typing import Any, ClassVar
 
@@ -19,7 +21,12 @@ import torch
 from pyshocks_gb300 import _lib as L
 from pyshocks_gb300 import reconstruction as rec_mod
 from pyshocks_gb300.grid import Grid
-from pyshocks_gb300.scalar import PeriodicBoundary
+from pyshocks_gb300.scalar import (
+    DirichletBoundary,
+    NeumannBoundary,
+    PeriodicBoundary,
+    TwoSidedBoundary,
+)
 from pyshocks_gb300.schemes import (
     Boundary,
     ConservationLawScheme,
@@ -202,8 +209,40 @@ def _check_state(grid: Grid, u: torch.Tensor) -> None:
 
 
 def _check_bc(bc: Boundary) -> None:
-    if not isinstance(bc, PeriodicBoundary):
-        raise NotImplementedError(f"{type(bc).__name__} is not on the GB300 path (periodic only)")
+    if isinstance(bc, PeriodicBoundary):
+        return
+    if isinstance(bc, TwoSidedBoundary) and all(
+            isinstance(b, (DirichletBoundary, NeumannBoundary)) for b in (bc.left, bc.right)):
+        return
+    raise NotImplementedError(f"{type(bc).__name__} is not on the GB300 path")
+
+
+def c_boundary(bc: Boundary, grid: Grid, times) -> L.ShkBoundary | None:
+    """The boundary data of a call at its stage times (``None``: periodic).
+    Dirichlet: ``g(t_s, x)`` at the three ghost centres of each side (the one
+    next to the interior first); Neumann: ``g(t_s)``."""
+    _check_bc(bc)
+    if isinstance(bc, PeriodicBoundary):
+        return None
+    out = L.ShkBoundary()
+    g, n = grid.nghosts, grid.ncells
+    for side, b in ((0, bc.left), (1, bc.right)):
+        kind = L.SHK_BC_DIRICHLET if isinstance(b, DirichletBoundary) else L.SHK_BC_NEUMANN
+        if side == 0:
+            out.left = kind
+            idx = [g - 1 - k for k in range(3)]
+        else:
+            out.right = kind
+            idx = [g + n + k for k in range(3)]
+        x = grid.x[torch.tensor(idx, device=grid.x.device)]
+        for s_, ts in enumerate(times):
+            if kind == L.SHK_BC_DIRICHLET:
+                vals = torch.as_tensor(b.g(ts, x), dtype=torch.float64).reshape(-1).cpu()
+                for k in range(3):
+                    out.dirichlet[(s_ * 2 + side) * 3 + k] = float(vals[k])
+            else:
+                out.neumann[s_ * 2 + side] = float(b.g(ts))
+    return out
 
 
 @apply_operator.register(GpuConservationLawScheme)
@@ -219,13 +258,25 @@ def _apply_operator_gpu(scheme, grid: Grid, bc: Boundary, t: Any, u: torch.Tenso
     out = torch.empty_like(u)
     stream = L.stream_handle()
     amax = None
+    cb = c_boundary(bc, grid, (float(t),))
     if scheme.flux_code == L.SHK_FLUX_LF:
-        amax = torch.empty((), dtype=torch.float64, device=u.device)
-        L.check(lib.shk_max_wavespeed_f64(cs, u.data_ptr(), n, g, amax.data_ptr(), stream),
-                "max_wavespeed")
+        if cb is None:
+            amax = torch.empty((), dtype=torch.float64, device=u.device)
+            L.check(lib.shk_max_wavespeed_f64(cs, u.data_ptr(), n, g, amax.data_ptr(), stream),
+                    "max_wavespeed")
+        else:
+            # scalar.py:277: the max over the whole array, ghosts filled by the boundary
+            from pyshocks_gb300.schemes import apply_boundary
+
+            ub = apply_boundary(bc, grid, t, u)
+            speed = torch.abs(ub) if scheme.equation_code == L.SHK_EQ_BURGERS else (
+                torch.abs(1 - 2 * ub) if scheme.equation_code == L.SHK_EQ_LWR
+                else torch.full_like(ub, abs(scheme.speed)))
+            amax = speed.max().reshape(())
+    bptr = None if cb is None else ctypes.byref(cb)
     L.check(
-        lib.shk_apply_operator_f64(cs, u.data_ptr(), out.data_ptr(), n, g, float(grid.dx_min),
-                                   L.ptr(amax), stream),
+        lib.shk_apply_operator_bc_f64(cs, bptr, u.data_ptr(), out.data_ptr(), n, g,
+                                      float(grid.dx_min), L.ptr(amax), stream),
         "apply_operator",
     )
     return out
@@ -247,17 +298,23 @@ def _predict_timestep_gpu(scheme, grid: Grid, bc: Boundary, t: Any, u: torch.Ten
     return dt
 
 
-def ssprk33_step(scheme, grid: Grid, bc: Boundary, dt: float, u: torch.Tensor) -> torch.Tensor:
-    """One fused SSPRK33 step (``src/pyshocks/timestepping.py:312-320``)."""
+def ssprk33_step(scheme, grid: Grid, bc: Boundary, dt: float, u: torch.Tensor,
+                 t: float = 0.0) -> torch.Tensor:
+    """One fused SSPRK33 step (``src/pyshocks/timestepping.py:312-320``) from
+    time *t*; a Dirichlet / Neumann boundary is applied before each stage at
+    the stage times t, t + dt, t + dt/2."""
     _check_bc(bc)
     _check_state(grid, u)
     if scheme.flux_code == L.SHK_FLUX_LF:
         raise NotImplementedError("fused step of the global Lax-Friedrichs flux")
     out = torch.empty_like(u)
+    dt = float(dt)
+    cb = c_boundary(bc, grid, (float(t), float(t) + dt, float(t) + 0.5 * dt))
     L.check(
-        L.lib().shk_ssprk33_step_f64(scheme.c_scheme(grid.dx_min), u.data_ptr(), out.data_ptr(),
-                                     grid.ncells, grid.nghosts, float(grid.dx_min), float(dt),
-                                     L.stream_handle()),
+        L.lib().shk_ssprk33_step_bc_f64(scheme.c_scheme(grid.dx_min),
+                                        None if cb is None else ctypes.byref(cb), u.data_ptr(),
+                                        out.data_ptr(), grid.ncells, grid.nghosts,
+                                        float(grid.dx_min), dt, L.stream_handle()),
         "ssprk33_step",
     )
     return out

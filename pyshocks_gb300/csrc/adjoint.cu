@@ -690,6 +690,7 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
     int r = plan_view(plan, &D, &dtype, &grid, &sch, &total, nullptr);
     if (r != SHK_OK) return r;
     if (!adjoint_supported(&sch)) return SHK_EUNSUPPORTED;
+    if (D.bc_left != SHK_BC_PERIODIC || D.bc_right != SHK_BC_PERIODIC) return SHK_EUNSUPPORTED;
     if (!D.dt_hist || D.max_steps < nsteps) return SHK_EINVAL;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const size_t esz = dtype == SHK_F64 ? 8 : 4;

@@ -95,7 +95,8 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) batc
                 break;
             }
             const T dtdx = static_cast<T>(ds.dt * P.inv_dx[b]);
-            mx = step_tile<T, EQ, REC, FLUX>(sm, uout + off + s0, te, dtdx, p);
+            mx = step_tile<T, EQ, REC, FLUX>(sm, uout + off + s0, te, dtdx, p, plan_bc(P, b),
+                                             s0 - HL, n);
         }
         const B bm = block_max<B>(mx, reinterpret_cast<B*>(red));
         if (threadIdx.x == 0) atomicMax(P.amax + size_t(nxt) * P.B + b, to_double_bits<T>(bm));
@@ -193,11 +194,46 @@ __global__ void instance_sum_kernel(PlanDev P, const int32_t* item_first, int mo
 // ---------------------------------------------------------------------------
 // single-instance kernels on the reference's ghosted layout (n + 2g cells)
 // ---------------------------------------------------------------------------
+// the boundary of a single-instance call (kernel parameter copy)
+__device__ __forceinline__ BcView call_bc(const shk_boundary& b, double dx) {
+    BcView v;
+    v.left = b.left;
+    v.right = b.right;
+    v.dir = &b.dirichlet[0][0][0];
+    v.dir_ss = 6;
+    v.neu = &b.neumann[0][0];
+    v.neu_ss = 2;
+    v.dx = dx;
+    return v;
+}
+
+// ghost cells of a single-instance output after a non-periodic call: the
+// boundary at `stage` applied to the new interior (Neumann mirrors it), or 0
+// (zero_ghosts: the operator output, whose ghost values are unspecified)
+template <class T>
+__global__ void bc_ghost_kernel(T* __restrict__ out, int64_t n, int g, shk_boundary b, double dx,
+                                int stage, int zero_ghosts) {
+    const int t = threadIdx.x;
+    if (t >= 2 * g) return;
+    const int side = t / g, k = t - g * side;
+    const int kind = side ? b.right : b.left;
+    const int64_t gidx = side ? g + n + k : g - 1 - k;  // ghosted index of ghost k
+    if (kind == SHK_BC_PERIODIC) return;
+    if (zero_ghosts || k >= 3) {
+        out[gidx] = T(0);
+    } else if (kind == SHK_BC_DIRICHLET) {
+        out[gidx] = static_cast<T>(b.dirichlet[stage][side][k]);
+    } else {
+        const int64_t mirror = side ? g + n - 1 - k : g + k;
+        out[gidx] = out[mirror] - static_cast<T>((2 * k + 1) * dx * b.neumann[stage][side]);
+    }
+}
+
 template <class T, int EQ, int REC, int FLUX>
 __global__ void __launch_bounds__(kThreads) apply_operator_kernel(const T* __restrict__ u, T* __restrict__ out,
                                                                   int64_t n, int g, int tile, T dx,
                                                                   const double* amax, OpParams<T> p,
-                                                                  int32_t* err) {
+                                                                  int32_t* err, shk_boundary bcp) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     constexpr int HL = op_halo<T>();
@@ -216,6 +252,9 @@ __global__ void __launch_bounds__(kThreads) apply_operator_kernel(const T* __res
         if (threadIdx.x == 0 && err) atomicOr(err, ERR_TIMEOUT);
         return;
     }
+    const BcView bc = call_bc(bcp, static_cast<double>(dx));
+    const bool periodic = bc.periodic();
+    if (!periodic) apply_bc(sm.U, s0 - HL, n, 0, te + 2 * HL, bc, 0);
     face_fluxes<T, EQ, REC, FLUX>(sm.U, HL, HL + te, sm, p);
     for (int i = threadIdx.x; i < te; i += blockDim.x) {
         const int w = HL + i;
@@ -224,8 +263,10 @@ __global__ void __launch_bounds__(kThreads) apply_operator_kernel(const T* __res
         const int64_t gi = s0 + i;
         out[g + gi] = r;
         // ghost cells of the output: periodic image of the interior output
-        if (gi < g) out[g + n + gi] = r;
-        if (gi >= n - g) out[gi - (n - g)] = r;
+        if (periodic) {
+            if (gi < g) out[g + n + gi] = r;
+            if (gi >= n - g) out[gi - (n - g)] = r;
+        }
     }
 }
 
@@ -252,7 +293,8 @@ __global__ void finalize_dt_kernel(double* dt, double cfl, double theta) {
 template <class T, int EQ, int REC, int FLUX>
 __global__ void __launch_bounds__(kThreads) single_step_kernel(const T* __restrict__ u, T* __restrict__ uout,
                                                                int64_t n, int g, int tile, T dtdx,
-                                                               OpParams<T> p, int32_t* err) {
+                                                               OpParams<T> p, int32_t* err,
+                                                               shk_boundary bcp, double dx) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     constexpr int HL = step_halo<T>();
@@ -270,8 +312,10 @@ __global__ void __launch_bounds__(kThreads) single_step_kernel(const T* __restri
         if (threadIdx.x == 0 && err) atomicOr(err, ERR_TIMEOUT);
         return;
     }
-    step_tile<T, EQ, REC, FLUX>(sm, uout + g + s0, te, dtdx, p);
+    const BcView bc = call_bc(bcp, dx);
+    step_tile<T, EQ, REC, FLUX>(sm, uout + g + s0, te, dtdx, p, bc, s0 - HL, n);
     __syncthreads();
+    if (!bc.periodic()) return;  // ghosts: bc_ghost_kernel after the step
     // periodic ghost image of the new state
     for (int i = threadIdx.x; i < te; i += blockDim.x) {
         const int64_t gi = s0 + i;
@@ -320,6 +364,20 @@ bool valid_scheme(const shk_scheme* s) {
     if ((s->rec == SHK_REC_CONSTANT || s->rec == SHK_REC_WENOJS32) && s->flux == SHK_FLUX_LF)
         return false;
     return true;
+}
+
+shk_boundary periodic_boundary() {
+    shk_boundary b;
+    std::memset(&b, 0, sizeof(b));
+    b.left = b.right = SHK_BC_PERIODIC;
+    return b;
+}
+
+// both sides periodic, or each Dirichlet / Neumann
+bool valid_boundary(const shk_boundary& b) {
+    auto ok = [](int k) { return k >= SHK_BC_PERIODIC && k <= SHK_BC_NEUMANN; };
+    if (!ok(b.left) || !ok(b.right)) return false;
+    return (b.left == SHK_BC_PERIODIC) == (b.right == SHK_BC_PERIODIC);
 }
 
 template <class T>
@@ -395,25 +453,25 @@ int dispatch_scheme(const shk_scheme* s, F&& f) {
 // launch functors (namespace scope: member templates are not allowed in local classes)
 struct ApplyOpLaunch {
     const double* u; double* out; int64_t n; int g; int tile; double dx; const double* amax;
-    OpParams<double> p; size_t smem; int blocks; cudaStream_t st;
+    OpParams<double> p; size_t smem; int blocks; cudaStream_t st; shk_boundary bc;
     template <class T, int EQ, int REC, int FLUX> int operator()() {
         auto k = apply_operator_kernel<T, EQ, REC, FLUX>;
         SHK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<blocks, kThreads, smem, st>>>(u, out, n, g, tile, dx, amax, p, nullptr);
+        k<<<blocks, kThreads, smem, st>>>(u, out, n, g, tile, dx, amax, p, nullptr, bc);
         return cuda_check(cudaGetLastError());
     }
 };
 
 struct SingleStepLaunch {
     const double* u; double* uo; int64_t n; int g; int tile; double dtdx;
-    OpParams<double> p; size_t smem; int blocks; cudaStream_t st;
+    OpParams<double> p; size_t smem; int blocks; cudaStream_t st; shk_boundary bc; double dx;
     template <class T, int EQ, int REC, int FLUX> int operator()() {
         if constexpr (FLUX == SHK_FLUX_LF) {
             return SHK_EUNSUPPORTED;
         } else {
             auto k = single_step_kernel<T, EQ, REC, FLUX>;
             SHK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            k<<<blocks, kThreads, smem, st>>>(u, uo, n, g, tile, dtdx, p, nullptr);
+            k<<<blocks, kThreads, smem, st>>>(u, uo, n, g, tile, dtdx, p, nullptr, bc, dx);
             return cuda_check(cudaGetLastError());
         }
     }
@@ -475,6 +533,9 @@ struct shk_plan {
     double* partial = nullptr;
     double* dt_fixed = nullptr;  // prescribed steps [fixed_cap][B], active when fixed_steps > 0
     int64_t fixed_cap = 0, fixed_steps = 0;
+    int bc_left = SHK_BC_PERIODIC, bc_right = SHK_BC_PERIODIC;
+    double* bc_dir = nullptr;  // [B][2][3]
+    double* bc_neu = nullptr;  // [B][2]
     // host mirror of the number of steps launched since reset
     int64_t host_steps = 0;
     // captured two-step graph
@@ -488,7 +549,8 @@ struct shk_plan {
         P.inv_dx = inv_dx; P.tfinal = tfinal; P.theta = theta; P.amax = amax; P.t = t;
         P.dt_hist = dt_hist; P.step = step; P.done = done; P.status = status;
         P.partial = partial; P.B = B;
-        P.dt_fixed = fixed_steps > 0 ? dt_fixed : nullptr; P.fixed_steps = fixed_steps; P.nitems = nitems; P.tile = tile; P.max_steps = max_steps;
+        P.dt_fixed = fixed_steps > 0 ? dt_fixed : nullptr; P.fixed_steps = fixed_steps;
+        P.bc_left = bc_left; P.bc_right = bc_right; P.bc_dir = bc_dir; P.bc_neu = bc_neu; P.nitems = nitems; P.tile = tile; P.max_steps = max_steps;
         return P;
     }
 };
@@ -565,18 +627,29 @@ int shk_max_wavespeed_f64(const shk_scheme* scheme, const double* u, int64_t n, 
     return cuda_check(cudaGetLastError());
 }
 
-int shk_apply_operator_f64(const shk_scheme* scheme, const double* u, double* out, int64_t n,
-                           int32_t nghosts, double dx, const double* amax, void* stream) {
+int shk_apply_operator_bc_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
+                              double* out, int64_t n, int32_t nghosts, double dx,
+                              const double* amax, void* stream) {
     if (!valid_scheme(scheme) || !u || !out || n < 3 || nghosts < 3 || !(dx > 0)) return SHK_EINVAL;
     if (scheme->flux == SHK_FLUX_LF && !amax) return SHK_EINVAL;
+    const shk_boundary b = bc ? *bc : periodic_boundary();
+    if (!valid_boundary(b)) return SHK_EINVAL;
     cudaStream_t st = as_stream(stream);
     const int tile = 512;
     const int W = tile + 2 * op_halo<double>();
     const size_t smem = Smem<double>::host_bytes(W);
     const int blocks = static_cast<int>((n + tile - 1) / tile);
     OpParams<double> p = make_params<double>(scheme);
-    ApplyOpLaunch f{u, out, n, nghosts, tile, dx, amax, p, smem, blocks, st};
-    return dispatch_scheme<double>(scheme, f);
+    ApplyOpLaunch f{u, out, n, nghosts, tile, dx, amax, p, smem, blocks, st, b};
+    const int r = dispatch_scheme<double>(scheme, f);
+    if (r != SHK_OK || (b.left == SHK_BC_PERIODIC && b.right == SHK_BC_PERIODIC)) return r;
+    bc_ghost_kernel<double><<<1, 64, 0, st>>>(out, n, nghosts, b, dx, 0, 1);
+    return cuda_check(cudaGetLastError());
+}
+
+int shk_apply_operator_f64(const shk_scheme* scheme, const double* u, double* out, int64_t n,
+                           int32_t nghosts, double dx, const double* amax, void* stream) {
+    return shk_apply_operator_bc_f64(scheme, nullptr, u, out, n, nghosts, dx, amax, stream);
 }
 
 int shk_predict_timestep_f64(const shk_scheme* scheme, const double* u, int64_t n, int32_t nghosts,
@@ -587,19 +660,30 @@ int shk_predict_timestep_f64(const shk_scheme* scheme, const double* u, int64_t 
     return cuda_check(cudaGetLastError());
 }
 
-int shk_ssprk33_step_f64(const shk_scheme* scheme, const double* u, double* u_out, int64_t n,
-                         int32_t nghosts, double dx, double dt, void* stream) {
+int shk_ssprk33_step_bc_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
+                            double* u_out, int64_t n, int32_t nghosts, double dx, double dt,
+                            void* stream) {
     if (!valid_scheme(scheme) || !u || !u_out || n < 3 || nghosts < 3 || !(dx > 0)) return SHK_EINVAL;
     if (!std::isfinite(dt)) return SHK_ENONFINITE;
     if (scheme->flux == SHK_FLUX_LF) return SHK_EUNSUPPORTED;  // global max per stage
+    const shk_boundary b = bc ? *bc : periodic_boundary();
+    if (!valid_boundary(b)) return SHK_EINVAL;
     cudaStream_t st = as_stream(stream);
     const int tile = 512;
     const int W = tile + 2 * step_halo<double>();
     const size_t smem = Smem<double>::step_bytes(W, scheme->rec);
     const int blocks = static_cast<int>((n + tile - 1) / tile);
     OpParams<double> p = make_params<double>(scheme);
-    SingleStepLaunch f{u, u_out, n, nghosts, tile, dt / dx, p, smem, blocks, st};
-    return dispatch_scheme<double>(scheme, f);
+    SingleStepLaunch f{u, u_out, n, nghosts, tile, dt / dx, p, smem, blocks, st, b, dx};
+    const int r = dispatch_scheme<double>(scheme, f);
+    if (r != SHK_OK || (b.left == SHK_BC_PERIODIC && b.right == SHK_BC_PERIODIC)) return r;
+    bc_ghost_kernel<double><<<1, 64, 0, st>>>(u_out, n, nghosts, b, dx, 1, 0);
+    return cuda_check(cudaGetLastError());
+}
+
+int shk_ssprk33_step_f64(const shk_scheme* scheme, const double* u, double* u_out, int64_t n,
+                         int32_t nghosts, double dx, double dt, void* stream) {
+    return shk_ssprk33_step_bc_f64(scheme, nullptr, u, u_out, n, nghosts, dx, dt, stream);
 }
 
 // ---------------------------------------------------------------------------
@@ -610,7 +694,8 @@ int shk_plan_destroy(shk_plan* plan) {
     if (plan->graph) cudaGraphExecDestroy(plan->graph);
     void* ptrs[] = {plan->item_inst, plan->item_tile, plan->item_first, plan->offsets, plan->cfl,
                     plan->inv_dx, plan->tfinal, plan->amax, plan->t, plan->dt_hist, plan->step,
-                    plan->done, plan->status, plan->partial, plan->dt_fixed};
+                    plan->done, plan->status, plan->partial, plan->dt_fixed, plan->bc_dir,
+                    plan->bc_neu};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete plan;
@@ -800,6 +885,37 @@ int shk_plan_set_fixed_dt(shk_plan* plan, const double* dt, int32_t nsteps, void
     return SHK_OK;
 }
 
+int shk_plan_set_boundary(shk_plan* plan, int32_t left, int32_t right, const double* dirichlet,
+                          const double* neumann, void* stream) {
+    if (!plan) return SHK_EINVAL;
+    shk_boundary b = periodic_boundary();
+    b.left = left;
+    b.right = right;
+    if (!valid_boundary(b)) return SHK_EINVAL;
+    const bool need_dir = left == SHK_BC_DIRICHLET || right == SHK_BC_DIRICHLET;
+    const bool need_neu = left == SHK_BC_NEUMANN || right == SHK_BC_NEUMANN;
+    if ((need_dir && !dirichlet) || (need_neu && !neumann)) return SHK_EINVAL;
+    cudaStream_t st = as_stream(stream);
+    const size_t B = static_cast<size_t>(plan->B);
+    if (need_dir && !plan->bc_dir &&
+        cudaMalloc(reinterpret_cast<void**>(&plan->bc_dir), sizeof(double) * 6 * B) != cudaSuccess)
+        return SHK_ENOMEM;
+    if (need_neu && !plan->bc_neu &&
+        cudaMalloc(reinterpret_cast<void**>(&plan->bc_neu), sizeof(double) * 2 * B) != cudaSuccess)
+        return SHK_ENOMEM;
+    if (need_dir)
+        SHK_CUDA(cudaMemcpyAsync(plan->bc_dir, dirichlet, sizeof(double) * 6 * B, cudaMemcpyDefault, st));
+    if (need_neu)
+        SHK_CUDA(cudaMemcpyAsync(plan->bc_neu, neumann, sizeof(double) * 2 * B, cudaMemcpyDefault, st));
+    plan->bc_left = left;
+    plan->bc_right = right;
+    if (plan->graph) {  // kernels take the plan's device view by value
+        cudaGraphExecDestroy(plan->graph);
+        plan->graph = nullptr;
+    }
+    return SHK_OK;
+}
+
 int shk_plan_step_graph(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps, void* stream) {
     if (!plan || !u_a || !u_b || u_a == u_b || nsteps < 0 || nsteps % 2) return SHK_EINVAL;
     if (plan->host_steps % 2) return SHK_EINVAL;
@@ -956,7 +1072,8 @@ extern "C" int shk_apply_operator_lf_noalloc_f64(const shk_scheme* scheme, const
     const int W = kNoAllocTile + 2 * op_halo<double>();
     const size_t smem = Smem<double>::host_bytes(W);
     OpParams<double> p = make_params<double>(scheme);
-    ApplyOpLaunch f{u, out, n, nghosts, kNoAllocTile, dx, scratch + kNoAllocMaxTiles, p, smem, nt, st};
+    ApplyOpLaunch f{u, out, n, nghosts, kNoAllocTile, dx, scratch + kNoAllocMaxTiles, p, smem, nt, st,
+                    periodic_boundary()};
     return dispatch_scheme<double>(scheme, f);
 }
 

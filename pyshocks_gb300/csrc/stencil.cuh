@@ -91,6 +91,48 @@ __device__ __forceinline__ void carve_step(Smem<T>& sm, unsigned char* base, int
     else sm.carve(base, W);
 }
 
+// ---------------------------------------------------------------------------
+// Dirichlet / Neumann boundaries (scalar.py:397-511) on a window. The window
+// loader fills every position circularly; for a non-periodic instance the
+// three ghost cells of each side (global cells -1-k and n+k, k = 0..2) are
+// then overwritten before each operator evaluation. Positions beyond the
+// ghosts keep the wrapped values: they reach only ghost outputs, which the
+// next overwrite replaces, never an interior output (stencil reach 3).
+// ---------------------------------------------------------------------------
+struct BcView {
+    int left = SHK_BC_PERIODIC, right = SHK_BC_PERIODIC;
+    const double* dir = nullptr;  // dir[stage * dir_ss + side * 3 + k]
+    int dir_ss = 0;
+    const double* neu = nullptr;  // neu[stage * neu_ss + side]
+    int neu_ss = 0;
+    double dx = 1.0;
+    __device__ bool periodic() const { return left == SHK_BC_PERIODIC && right == SHK_BC_PERIODIC; }
+};
+
+// S: window array; g0: global cell of window position 0; [wlo, whi): the
+// positions holding values of this stage. Call after a barrier; ends with one.
+template <class V>
+__device__ void apply_bc(V* S, int64_t g0, int64_t n, int wlo, int whi, const BcView& bc,
+                         int stage) {
+    const int t = threadIdx.x;
+    if (t < 6) {
+        const int side = t / 3, k = t - 3 * side;
+        const int kind = side ? bc.right : bc.left;
+        const int64_t w = (side ? n + k : -1 - k) - g0;
+        if (kind != SHK_BC_PERIODIC && w >= wlo && w < whi) {
+            V val;
+            if (kind == SHK_BC_DIRICHLET) {
+                val = static_cast<V>(bc.dir[stage * bc.dir_ss + side * 3 + k]);
+            } else {
+                const int64_t wm = (side ? n - 1 - k : k) - g0;  // mirrored interior cell
+                val = S[wm] - static_cast<V>((2 * k + 1) * bc.dx * bc.neu[stage * bc.neu_ss + side]);
+            }
+            S[w] = val;
+        }
+    }
+    __syncthreads();
+}
+
 // float copy of the operator parameters (the mixed-precision learned path)
 template <class T>
 __host__ __device__ inline OpParams<float> float_params(const OpParams<T>& p) {
@@ -340,7 +382,8 @@ __host__ __device__ inline DtState compute_dt(double smax, double cfl, double th
 // stage state, H the float cell differences and the increments.
 template <int EQ, int FLUX>
 __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* gout, int te,
-                                              double dtdx, const OpParams<double>& p) {
+                                              double dtdx, const OpParams<double>& p,
+                                              const BcView& bc, int64_t g0, int64_t n) {
     constexpr int HL = step_halo<double>();
     const int tid = threadIdx.x, nt = blockDim.x, W = sm.W;
     const OpParams<float> pf = float_params(p);
@@ -358,6 +401,7 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
     const float dtf = static_cast<float>(dtdx);
     for (int i = tid; i < te + 2 * HL; i += nt) fs.U[i] = static_cast<float>(sm.U[i]);
     __syncthreads();
+    if (!bc.periodic()) apply_bc(fs.U, g0, n, 0, te + 2 * HL, bc, 0);
     {
         const int lo = HL - 6, hi = HL + te + 6;
         face_fluxes<float, EQ, SHK_REC_LEARNED, FLUX>(fs.U, lo, hi, fs, pf);
@@ -367,6 +411,7 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
             fs.S[i] = fs.U[i] + d;
         }
         __syncthreads();
+        if (!bc.periodic()) apply_bc(fs.S, g0, n, lo, hi, bc, 1);
     }
     {
         const int lo = HL - 3, hi = HL + te + 3;
@@ -377,6 +422,7 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
             fs.S[i] = fs.U[i] + d;
         }
         __syncthreads();
+        if (!bc.periodic()) apply_bc(fs.S, g0, n, lo, hi, bc, 2);
     }
     unsigned long long mx = 0;
     {
@@ -393,13 +439,18 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
     return mx;
 }
 
+// g0: global cell of window position 0 (s - HL); n: cells of the instance;
+// bc: its boundary (periodic: nothing to overwrite)
 template <class T, int EQ, int REC, int FLUX>
 __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, T dtdx,
-                                            const OpParams<T>& p) {
+                                            const OpParams<T>& p, const BcView& bc = BcView(),
+                                            int64_t g0 = 0, int64_t n = 0) {
     if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED)
-        return step_tile_mixed<EQ, FLUX>(sm, gout, te, dtdx, p);
+        return step_tile_mixed<EQ, FLUX>(sm, gout, te, dtdx, p, bc, g0, n);
     constexpr int HL = step_halo<T>();
     const int tid = threadIdx.x, nt = blockDim.x;
+    const bool np = !bc.periodic();
+    if (np) apply_bc(sm.U, g0, n, 0, te + 2 * HL, bc, 0);
     dtdx *= p.fscale;
     if constexpr (sizeof(T) == 4) {
         // float state: the stages as increments about u (as step_tile_mixed).
@@ -415,6 +466,7 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
                 sm.S[i] = sm.U[i] + d;
             }
             __syncthreads();
+            if (np) apply_bc(sm.S, g0, n, lo, hi, bc, 1);
         }
         {
             const int lo = HL - 3, hi = HL + te + 3;
@@ -425,6 +477,7 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
                 sm.S[i] = sm.U[i] + d;
             }
             __syncthreads();
+            if (np) apply_bc(sm.S, g0, n, lo, hi, bc, 2);
         }
         using B = typename Bits<T>::type;
         B mx = 0;
@@ -445,6 +498,7 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
         face_fluxes<T, EQ, REC, FLUX>(sm.U, lo, hi, sm, p);
         for (int i = lo + tid; i < hi; i += nt) sm.S[i] = fma(dtdx, sm.D[i - 1] - sm.D[i], sm.U[i]);
         __syncthreads();
+        if (np) apply_bc(sm.S, g0, n, lo, hi, bc, 1);
     }
     // stage 2: k2 = 3/4 u + 1/4 (k1 + dt L(k1)) on [HL-3, HL+te+3) (in place over k1)
     {
@@ -455,6 +509,7 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
             sm.S[i] = fma(T(1.0 / 4.0), k, T(3.0 / 4.0) * sm.U[i]);
         }
         __syncthreads();
+        if (np) apply_bc(sm.S, g0, n, lo, hi, bc, 2);
     }
     // stage 3: u+ = 1/3 u + 2/3 (k2 + dt L(k2)) on the tile
     using B = typename Bits<T>::type;
@@ -491,8 +546,24 @@ struct PlanDev {
     double* partial;  // [nitems]
     const double* dt_fixed;  // [fixed_steps][B] prescribed steps, or null (CFL steps)
     int64_t fixed_steps;
+    int bc_left, bc_right;   // SHK_BC_* of every instance
+    const double* bc_dir;    // [B][2][3] Dirichlet ghost values
+    const double* bc_neu;    // [B][2] Neumann gradients
     int32_t B, nitems, tile, max_steps;
 };
+
+// the boundary of instance b (time-independent data: one stage for all three)
+__device__ __forceinline__ BcView plan_bc(const PlanDev& P, int b) {
+    BcView v;
+    v.left = P.bc_left;
+    v.right = P.bc_right;
+    if (!v.periodic()) {
+        v.dir = P.bc_dir ? P.bc_dir + size_t(b) * 6 : nullptr;
+        v.neu = P.bc_neu ? P.bc_neu + size_t(b) * 2 : nullptr;
+        v.dx = 1.0 / P.inv_dx[b];
+    }
+    return v;
+}
 
 // time step k of instance b: the prescribed step when the plan has a dt table
 // (a step <= 0 or past the table's end leaves the instance unchanged, a

@@ -170,7 +170,7 @@ def _advance_ssprk33(stepper, dt, t, u):
         if isinstance(src.scheme, burgers.GpuConservationLawScheme) and (
             src.scheme.flux_code != burgers.L.SHK_FLUX_LF
         ):
-            return burgers.ssprk33_step(src.scheme, src.grid, src.bc, dt, u)
+            return burgers.ssprk33_step(src.scheme, src.grid, src.bc, dt, u, t=float(t))
     fn = src
     k1 = u + dt * fn(t, u)
     k2 = 3.0 / 4.0 * u + 1.0 / 4.0 * (k1 + dt * fn(t + dt, k1))

@@ -128,7 +128,7 @@ def main(refdir: pathlib.Path) -> None:
 
     bc = PeriodicBoundary()
 
-    def run(kind, n, u0_fn, *, tfinal=None, maxit=None, theta=1.0):
+    def run(kind, n, u0_fn, *, tfinal=None, maxit=None, theta=1.0, bc=bc):
         scheme = make_scheme(kind)
         grid = make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
         scheme = bind(scheme, grid, bc)
@@ -184,6 +184,23 @@ def main(refdir: pathlib.Path) -> None:
     out["fourier_lf_n64_s21"] = run("lf", 64, fourier_ic(21), maxit=40)
     out["fourier_esweno_n64_s22"] = run("esweno", 64, fourier_ic(22), maxit=40)
     out["lwr_rusanov_n128_s31"] = run("lwr", 128, lwr_ic(31), maxit=60)
+    # Dirichlet and Neumann boundaries (scalar.py:397-511) with time-dependent
+    # data: g_d(t, x) = 0.6 + 0.25 sin(pi x - t), g_n(t) = 0.3 cos(2 t) on the
+    # left, -0.2 on the right
+    from pyshocks.scalar import make_dirichlet_boundary, make_neumann_boundary
+
+    dbc = make_dirichlet_boundary(ga=lambda t, x: 0.6 + 0.25 * jnp.sin(jnp.pi * x - t))
+    nbc = make_neumann_boundary(ga=lambda t: 0.3 * jnp.cos(2.0 * t), gb=lambda t: jnp.array(-0.2))
+
+    def smooth_ic(grid):
+        x = np.asarray(grid.x)
+        return 0.6 + 0.25 * np.sin(np.pi * x) + 0.1 * np.cos(3.0 * np.pi * x)
+
+    out["dirichlet_rusanov_n128"] = run("rusanov", 128, smooth_ic, maxit=60, bc=dbc)
+    out["neumann_rusanov_n128"] = run("rusanov", 128, smooth_ic, maxit=60, bc=nbc)
+    out["dirichlet_eo_wenojs32_n100"] = run("eo-wenojs32", 100, smooth_ic, maxit=60, bc=dbc)
+    out["neumann_godunov_constant_n90"] = run("godunov-constant", 90, smooth_ic, maxit=60, bc=nbc)
+
     # Godunov / Engquist-Osher fluxes and the constant / WENO-JS32 reconstructions
     out["config1_godunov_wenojs53_n256"] = run("godunov-wenojs53", 256, sine_ic, tfinal=1.0)
     out["config1_eo_wenojs53_n256"] = run("eo-wenojs53", 256, sine_ic, tfinal=1.0)

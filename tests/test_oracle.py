@@ -256,3 +256,50 @@ def test_torch_step_vjp_vs_finite_differences():
 
 
 # }}}
+
+
+# {{{ Dirichlet / Neumann boundaries (golden runs of the reference)
+
+
+def dirichlet_data(t, x):
+    return 0.6 + 0.25 * np.sin(np.pi * x - t)
+
+
+def neumann_left(t):
+    return 0.3 * np.cos(2.0 * t)
+
+
+def neumann_right(t):
+    return -0.2
+
+
+BC_RUNS = [
+    ("dirichlet_rusanov_n128", "rusanov", "wenojs53", "dirichlet"),
+    ("neumann_rusanov_n128", "rusanov", "wenojs53", "neumann"),
+    ("dirichlet_eo_wenojs32_n100", "eo", "wenojs32", "dirichlet"),
+    ("neumann_godunov_constant_n90", "godunov", "constant", "neumann"),
+]
+
+
+@pytest.mark.parametrize(("name", "flux_kind", "rec", "kind"), BC_RUNS)
+def test_numpy_oracle_boundary_runs_golden(name, flux_kind, rec, kind):
+    """``apply_boundary`` of ``DirichletBoundary`` / ``NeumannBoundary``
+    (``src/pyshocks/scalar.py:397-511``) restated: bit-identical 60-step runs."""
+    g = _load(name)
+    n = int(g["n"])
+    grid = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+    spec = R.SchemeSpec(flux_kind=flux_kind, rec=rec, eps=1.0e-6)
+    if kind == "dirichlet":
+        def bc(t, u):
+            return R.apply_boundary_dirichlet(u, grid, t, dirichlet_data, dirichlet_data)
+    else:
+        def bc(t, u):
+            return R.apply_boundary_neumann(u, grid, t, neumann_left, neumann_right)
+    rhs0 = R.apply_operator(spec, grid, g["u0"], 0.0, bc)
+    np.testing.assert_array_equal(rhs0[3:-3], g["rhs0"][3:-3])
+    u, dts = R.evolve(spec, grid, g["u0"], theta=1.0, maxit=60, bc=bc)
+    np.testing.assert_array_equal(np.array(dts), g["dts"])
+    np.testing.assert_array_equal(u[3:-3], g["u"][3:-3])
+
+
+# }}}
