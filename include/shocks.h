@@ -42,7 +42,12 @@ enum { SHK_FLUX_RUSANOV = 0, SHK_FLUX_LF = 1, SHK_FLUX_ESWENO = 2, SHK_FLUX_GODU
 /* reconstruction (reconstruction.py:128-163,320-348,386-439); SHK_REC_LEARNED:
  * learned WENO weights (an MLP over the normalised stencil) */
 enum { SHK_REC_WENOJS53 = 0, SHK_REC_ESWENO32 = 1, SHK_REC_LEARNED = 2, SHK_REC_CONSTANT = 3,
-       SHK_REC_WENOJS32 = 4 };
+       SHK_REC_WENOJS32 = 4, SHK_REC_MUSCL = 5, SHK_REC_MUSCLS = 6 };
+/* limiters of SHK_REC_MUSCL (flux limiter, reconstruction.py:172-245) and
+ * SHK_REC_MUSCLS (slope limiter, :248-290), limiters.py:133-407; Koren has no
+ * slope form */
+enum { SHK_LIM_NONE = 0, SHK_LIM_MINMOD = 1, SHK_LIM_MC = 2, SHK_LIM_SUPERBEE = 3,
+       SHK_LIM_VANALBADA = 4, SHK_LIM_VANLEER = 5, SHK_LIM_KOREN = 6 };
 /* physical flux f(u) and wave speed f'(u) */
 enum { SHK_EQ_BURGERS = 0, SHK_EQ_ADVECTION = 1, SHK_EQ_LWR = 2 };
 /* state precision */
@@ -55,7 +60,8 @@ typedef struct {
     int32_t flux;      /* SHK_FLUX_*                                         */
     int32_t rec;       /* SHK_REC_*                                          */
     int32_t equation;  /* SHK_EQ_*                                           */
-    int32_t reserved;
+    int32_t limiter;   /* SHK_REC_MUSCL / MUSCLS: SHK_LIM_* (its theta or van
+                        * Albada variant in delta, the slope-ratio cut atol in eps) */
     double eps;        /* WENO epsilon (WENOJS53 default 1e-12; configs 1e-6) */
     double delta;      /* ES-WENO delta (bound to dx^2 by burgers bind)       */
     double nu;         /* Rusanov artificial viscosity dx^(alpha-1); 1 if alpha=1 */

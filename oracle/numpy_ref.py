@@ -19,7 +19,7 @@ Array layout follows the reference: one instance is a ghosted array of
 from __future__ import annotations
 
 from dataclasses import dataclass
-from typing import Callable, Iterator
+from typing import Any, Callable, Iterator
 
 import numpy as np
 
@@ -150,6 +150,112 @@ def _reconstruct_es_weno_side(s: Stencil, eps: float, f: np.ndarray) -> np.ndarr
     omega = es_weno_weights(s, f, eps)
     uhat = weno_interp(s, f)
     return np.sum(omega * uhat, axis=0)
+
+
+# {{{ MUSCL (src/pyshocks/limiters.py, src/pyshocks/reconstruction.py:172-296)
+
+LIMITERS = ("none", "minmod", "mc", "superbee", "vanalbada", "vanleer", "koren")
+#: limiters with phi(1/r) = phi(r)/r (limiters.py: is_symmetric)
+SYMMETRIC = {"minmod", "mc", "superbee", "vanleer"}
+
+
+def limiter_phi(name: str, r: np.ndarray, param: float = 1.0) -> np.ndarray:
+    """``evaluate(lm, r)`` (``limiters.py:137-139,194-198,229-231,265-267,
+    316-323,359-362,386-388``); *param* is theta (minmod) or the van Albada
+    variant."""
+    if name == "none":
+        return np.ones_like(r)
+    if name == "minmod":
+        return np.maximum(0.0, np.minimum(np.minimum(param, param * r), (1 + r) / 2))
+    if name == "mc":
+        return np.maximum(0.0, np.minimum(np.minimum(2, 2 * r), (1 + r) / 2))
+    if name == "superbee":
+        return np.maximum(0.0, np.maximum(np.minimum(1, 2 * r), np.minimum(2, r)))
+    if name == "vanalbada":
+        phi = (r**2 + r) / (r**2 + 1) if int(param) == 1 else 2 * r / (r**2 + 1)
+        return np.maximum(0.0, phi)
+    if name == "vanleer":
+        rabs = np.abs(r)
+        return np.maximum(0.0, (r + rabs) / (1 + rabs))
+    if name == "koren":
+        return np.maximum(0.0, np.minimum(np.minimum(2, 2 * r), (1 + 2 * r) / 3))
+    raise ValueError(name)
+
+
+def is_symmetric(name: str, param: float = 1.0) -> bool:
+    return name in SYMMETRIC or (name == "vanalbada" and int(param) == 1)
+
+
+def local_slope_ratio(u: np.ndarray, atol: float = 1.0e-12) -> np.ndarray:
+    """``limiters.py:110-125``."""
+    sl = u[1:-1] - u[:-2]
+    sr = u[2:] - u[1:-1]
+    mask = (np.abs(sr) < atol).astype(u.dtype)
+    sl = np.where(mask, 0.0, sl)
+    sr = np.where(mask, 1.0, sr)
+    return sl / sr
+
+
+def reconstruct_muscl(name: str, param: float, atol: float, f: np.ndarray,
+                      u: np.ndarray | None = None):
+    """``(ul, ur)`` of the flux-limited MUSCL reconstruction
+    (``reconstruction.py:212-245``); the limiter works on *u* (default *f*)."""
+    u = f if u is None else u
+    r = np.pad(local_slope_ratio(u, atol=atol), 1)
+    phi_r = limiter_phi(name, r, param)
+    if is_symmetric(name, param):
+        with np.errstate(divide="ignore", invalid="ignore"):
+            phi_inv_r = np.where(np.abs(r) < atol, 0.0, phi_r / r)
+    else:
+        with np.errstate(divide="ignore"):
+            inv_r = np.where(np.abs(r) < atol, atol, 1 / r)
+        phi_inv_r = limiter_phi(name, inv_r, param)
+    ur = np.pad(f[:-1] + 0.5 * phi_r[:-1] * (f[1:] - f[:-1]), (0, 1))
+    ul = np.pad(f[1:] - 0.5 * phi_inv_r[1:] * (f[1:] - f[:-1]), (1, 0))
+    return ul, ur
+
+
+def _minmod(a, b):
+    return np.where(a * b < 0.0, 0.0, np.where(np.abs(a) < np.abs(b), a, b))
+
+
+def slope_limit(name: str, param: float, x: np.ndarray, u: np.ndarray) -> np.ndarray:
+    """``slope_limit(lm, grid, u)`` (``limiters.py:147-155,201-209,234-245,
+    270-278,326-339,365-375``); Koren has no slope form in the reference."""
+    sl = (u[1:-1] - u[:-2]) / (x[1:-1] - x[:-2])
+    sr = (u[2:] - u[1:-1]) / (x[2:] - x[1:-1])
+    if name == "none":
+        # the reference's unlimited slope adds the neighbours (limiters.py:150)
+        s = (u[2:] + u[:-2]) / (x[2:] - x[:-2])
+    elif name == "minmod":
+        s = _minmod(sl, sr)
+    elif name == "mc":
+        sc = (u[2:] - u[:-2]) / (x[2:] - x[:-2])
+        s = _minmod(_minmod(sl, sr), sc)
+    elif name == "superbee":
+        s = np.maximum(_minmod(sl, 2 * sr), _minmod(2 * sl, sr))
+    elif name == "vanalbada":
+        with np.errstate(divide="ignore", invalid="ignore"):
+            if int(param) == 1:
+                s = np.where(sl * sr <= 0.0, 0.0, sl * sr * (sl + sr) / (sl**2 + sr**2))
+            else:
+                s = np.where(sl * sr <= 0.0, 0.0, 2.0 * sl * sr / (sl**2 + sr**2))
+    elif name == "vanleer":
+        with np.errstate(divide="ignore", invalid="ignore"):
+            s = np.where(sl * sr <= 0.0, 0.0, 2.0 * sl * sr / (sl + sr))
+    else:
+        raise NotImplementedError(name)
+    return np.pad(s, 1)
+
+
+def reconstruct_muscls(name: str, param: float, x: np.ndarray, dx: float, f: np.ndarray):
+    """``(ul, ur)`` of the slope-limited MUSCL reconstruction
+    (``reconstruction.py:271-290``)."""
+    du = slope_limit(name, param, x, f)
+    return f - 0.5 * dx * du, f + 0.5 * dx * du
+
+
+# }}}
 
 
 def reconstruct_esweno32(
@@ -335,6 +441,13 @@ class SchemeSpec:
     delta: float = 1.0e-6
     alpha: float = 1.0
     equation: str = "burgers"
+    #: MUSCL / MUSCLS (``rec="muscl"`` / ``"muscls"``): limiter name, its
+    #: parameter (theta or variant), the slope cut atol and the grid
+    limiter: str = "minmod"
+    limiter_param: float = 1.0
+    atol: float = 1.0e-12
+    x: Any = None
+    dx: float = 0.0
 
     @property
     def stencil(self) -> Stencil:
@@ -346,6 +459,10 @@ class SchemeSpec:
 def reconstruct(spec: SchemeSpec, f: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     if spec.rec == "constant":
         return f, f
+    if spec.rec == "muscl":
+        return reconstruct_muscl(spec.limiter, spec.limiter_param, spec.atol, f)
+    if spec.rec == "muscls":
+        return reconstruct_muscls(spec.limiter, spec.limiter_param, spec.x, spec.dx, f)
     if spec.rec == "esweno32":
         return reconstruct_esweno32(spec.stencil, spec.eps, f)
     return reconstruct_wenojs(spec.stencil, spec.eps, f)

@@ -26,6 +26,9 @@ SHK_ETOOLARGE = 7
 
 SHK_FLUX_RUSANOV, SHK_FLUX_LF, SHK_FLUX_ESWENO, SHK_FLUX_GODUNOV, SHK_FLUX_EO = 0, 1, 2, 3, 4
 SHK_REC_WENOJS53, SHK_REC_ESWENO32, SHK_REC_LEARNED, SHK_REC_CONSTANT, SHK_REC_WENOJS32 = 0, 1, 2, 3, 4
+SHK_REC_MUSCL, SHK_REC_MUSCLS = 5, 6
+(SHK_LIM_NONE, SHK_LIM_MINMOD, SHK_LIM_MC, SHK_LIM_SUPERBEE, SHK_LIM_VANALBADA, SHK_LIM_VANLEER,
+ SHK_LIM_KOREN) = range(7)
 SHK_EQ_BURGERS, SHK_EQ_ADVECTION, SHK_EQ_LWR = 0, 1, 2
 SHK_F64, SHK_F32 = 0, 1
 
@@ -40,7 +43,7 @@ class ShkScheme(ctypes.Structure):
         ("flux", ctypes.c_int32),
         ("rec", ctypes.c_int32),
         ("equation", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("limiter", ctypes.c_int32),
         ("eps", ctypes.c_double),
         ("delta", ctypes.c_double),
         ("nu", ctypes.c_double),

@@ -65,6 +65,11 @@ class GpuConservationLawScheme(ConservationLawScheme):
         s.equation = self.equation_code
         s.eps = float(getattr(rec, "eps", 1.0e-6))
         s.delta = float(getattr(rec, "delta", 0.0))
+        if isinstance(rec, rec_mod.MUSCL):
+            # the limiter, its parameter and the slope-ratio cut
+            s.limiter = int(rec.lm.code)
+            s.delta = float(rec.lm.param)
+            s.eps = float(rec.atol)
         s.nu = float(self.nu_for(dx))
         s.speed = float(self.speed)
         if s.rec < 0:

@@ -565,6 +565,10 @@ OpParams<T> adj_params(const shk_scheme* s) {
                          norm_floor(s->norm_eps)};
     p.fscale = (sizeof(T) == 8 && s->flux == SHK_FLUX_RUSANOV && s->rec == SHK_REC_WENOJS53 &&
                 s->equation == SHK_EQ_BURGERS && s->nu == 1.0) ? T(0.25) : T(1);
+    p.lim = s->limiter;
+    p.lim_param = static_cast<T>(s->delta);
+    p.atol = static_cast<T>(s->eps);
+    p.dx = T(1);
     return p;
 }
 

@@ -235,6 +235,85 @@ __device__ __forceinline__ void weno32_cell(T vm1, T v, T vp1, T eps, T& ul, T& 
     ul = fma(T(-0.5) * fma(s0, dp, T(2) * s1 * dm), T(1) / fma(T(2), s1, s0), v);
 }
 
+// ---- MUSCL limiters (limiters.py) --------------------------------------------
+// flux limiter phi(r) (evaluate(lm, r)); param: theta (minmod) or the van
+// Albada variant
+template <class T>
+__device__ __forceinline__ T limiter_phi(int lim, T r, T param) {
+    switch (lim) {
+        case SHK_LIM_MINMOD: return fmax(T(0), fmin(fmin(param, param * r), (T(1) + r) / T(2)));
+        case SHK_LIM_MC: return fmax(T(0), fmin(fmin(T(2), T(2) * r), (T(1) + r) / T(2)));
+        case SHK_LIM_SUPERBEE: return fmax(T(0), fmax(fmin(T(1), T(2) * r), fmin(T(2), r)));
+        case SHK_LIM_VANALBADA:
+            return fmax(T(0), param == T(1) ? (r * r + r) / (r * r + T(1)) : T(2) * r / (r * r + T(1)));
+        case SHK_LIM_VANLEER: return fmax(T(0), (r + fabs(r)) / (T(1) + fabs(r)));
+        case SHK_LIM_KOREN: return fmax(T(0), fmin(fmin(T(2), T(2) * r), (T(1) + T(2) * r) / T(3)));
+        default: return T(1);  // unlimited
+    }
+}
+
+// phi(1/r) = phi(r)/r holds for these (limiters.py: is_symmetric)
+__device__ __forceinline__ bool limiter_symmetric(int lim, double param) {
+    return lim == SHK_LIM_MINMOD || lim == SHK_LIM_MC || lim == SHK_LIM_SUPERBEE ||
+           lim == SHK_LIM_VANLEER || (lim == SHK_LIM_VANALBADA && param == 1.0);
+}
+
+// flux-limited MUSCL of cell c (reconstruction.py:212-245): slope ratio
+// r = (v - v_{c-1}) / (v_{c+1} - v) with the atol cut of limiters.py:110-125,
+// ur = v + phi(r)/2 (v_{c+1} - v), ul = v - phi(1/r)/2 (v - v_{c-1})
+template <class T>
+__device__ __forceinline__ void muscl_cell(T vm1, T v, T vp1, int lim, T param, T atol, T& ul,
+                                           T& ur) {
+    T sl = v - vm1, sr = vp1 - v;
+    const T dl = sl, dr = sr;
+    if (fabs(sr) < atol) {
+        sl = T(0);
+        sr = T(1);
+    }
+    const T r = sl / sr;
+    const T phi_r = limiter_phi<T>(lim, r, param);
+    T phi_inv;
+    if (limiter_symmetric(lim, static_cast<double>(param))) {
+        phi_inv = fabs(r) < atol ? T(0) : phi_r / r;
+    } else {
+        const T inv_r = fabs(r) < atol ? atol : T(1) / r;
+        phi_inv = limiter_phi<T>(lim, inv_r, param);
+    }
+    ur = v + T(0.5) * phi_r * dr;
+    ul = v - T(0.5) * phi_inv * dl;
+}
+
+template <class T>
+__device__ __forceinline__ T minmod2(T a, T b) {
+    return a * b < T(0) ? T(0) : (fabs(a) < fabs(b) ? a : b);
+}
+
+// slope-limited MUSCL of cell c (reconstruction.py:271-290 with
+// limiters.py:147-155,201-209,234-245,270-278,326-339,365-375) on a uniform
+// grid: du dx from the raw differences; ul, ur = v -+ (du dx) / 2
+template <class T>
+__device__ __forceinline__ void muscls_cell(T vm1, T v, T vp1, int lim, T param, T dx, T& ul,
+                                            T& ur) {
+    const T sl = v - vm1, sr = vp1 - v;
+    T s;
+    switch (lim) {
+        case SHK_LIM_MINMOD: s = minmod2(sl, sr); break;
+        case SHK_LIM_MC: s = minmod2(minmod2(sl, sr), (vp1 - vm1) / T(2)); break;
+        case SHK_LIM_SUPERBEE: s = fmax(minmod2(sl, T(2) * sr), minmod2(T(2) * sl, sr)); break;
+        case SHK_LIM_VANALBADA:
+            // variant 2's "slope" 2 sl sr / (sl^2 + sr^2) is scale-free in the
+            // reference and still multiplied by dx / 2: the face offset keeps dx
+            s = sl * sr <= T(0) ? T(0)
+                                : (param == T(1) ? sl * sr * (sl + sr) / (sl * sl + sr * sr)
+                                                 : dx * (T(2) * sl * sr / (sl * sl + sr * sr)));
+            break;
+        case SHK_LIM_VANLEER: s = sl * sr <= T(0) ? T(0) : T(2) * sl * sr / (sl + sr); break;
+        default: s = (vp1 + vm1) / T(2); break;  // the reference's unlimited slope (limiters.py:150)
+    }
+    ur = v + T(0.5) * s;
+    ul = v - T(0.5) * s;
+}
+
 // ---- numerical fluxes at face j+1/2 -----------------------------------------
 // R = ur_j, L = ul_{j+1}, vj, vj1 cell values.
 template <int EQ, class T>

@@ -95,7 +95,9 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) batc
                 break;
             }
             const T dtdx = static_cast<T>(ds.dt * P.inv_dx[b]);
-            mx = step_tile<T, EQ, REC, FLUX>(sm, uout + off + s0, te, dtdx, p, plan_bc(P, b),
+            OpParams<T> pb = p;
+            pb.dx = static_cast<T>(1.0 / P.inv_dx[b]);
+            mx = step_tile<T, EQ, REC, FLUX>(sm, uout + off + s0, te, dtdx, pb, plan_bc(P, b),
                                              s0 - HL, n);
         }
         const B bm = block_max<B>(mx, reinterpret_cast<B*>(red));
@@ -352,7 +354,13 @@ int cuda_check(cudaError_t e) {
 bool valid_scheme(const shk_scheme* s) {
     if (!s) return false;
     if (s->flux < 0 || s->flux > SHK_FLUX_EO) return false;
-    if (s->rec < 0 || s->rec > SHK_REC_WENOJS32) return false;
+    if (s->rec < 0 || s->rec > SHK_REC_MUSCLS) return false;
+    if (s->rec == SHK_REC_MUSCL || s->rec == SHK_REC_MUSCLS) {
+        if (s->limiter < SHK_LIM_NONE || s->limiter > SHK_LIM_KOREN) return false;
+        if (s->rec == SHK_REC_MUSCLS && s->limiter == SHK_LIM_KOREN) return false;  // no slope form
+        if (s->limiter == SHK_LIM_MINMOD && !(s->delta >= 1.0 && s->delta <= 2.0)) return false;
+        if (s->limiter == SHK_LIM_VANALBADA && s->delta != 1.0 && s->delta != 2.0) return false;
+    }
     if (s->equation < 0 || s->equation > SHK_EQ_LWR) return false;
     if ((s->flux == SHK_FLUX_ESWENO) != (s->rec == SHK_REC_ESWENO32)) return false;
     if (s->rec == SHK_REC_LEARNED && (s->flux != SHK_FLUX_RUSANOV || !s->mlp)) return false;
@@ -361,7 +369,8 @@ bool valid_scheme(const shk_scheme* s) {
     if ((s->flux == SHK_FLUX_GODUNOV || s->flux == SHK_FLUX_EO) &&
         (s->equation != SHK_EQ_BURGERS || s->rec == SHK_REC_LEARNED))
         return false;
-    if ((s->rec == SHK_REC_CONSTANT || s->rec == SHK_REC_WENOJS32) && s->flux == SHK_FLUX_LF)
+    if ((s->rec == SHK_REC_CONSTANT || s->rec == SHK_REC_WENOJS32 || s->rec == SHK_REC_MUSCL ||
+         s->rec == SHK_REC_MUSCLS) && s->flux == SHK_FLUX_LF)
         return false;
     return true;
 }
@@ -388,6 +397,10 @@ OpParams<T> make_params(const shk_scheme* s) {
     p.hnu = static_cast<T>(0.5 * s->nu);
     p.c = static_cast<T>(s->speed);
     p.hnu_amax = T(0);
+    p.lim = s->limiter;
+    p.lim_param = static_cast<T>(s->delta);
+    p.atol = static_cast<T>(s->eps);
+    p.dx = T(1);  // set per call / per instance
     p.lp = LearnedParams{s->mlp, static_cast<float>(s->eps), s->tau, s->band, s->dev,
                          norm_floor(s->norm_eps)};
     // FP64 Burgers-Rusanov with nu = 1 stores 4 F (see face_fluxes)
@@ -414,10 +427,14 @@ template <class T, class F>
 int dispatch_upwind(const shk_scheme* s, F&& f) {
     constexpr int EQ = SHK_EQ_BURGERS;
     if (s->flux == SHK_FLUX_GODUNOV) {
+        if (s->rec == SHK_REC_MUSCL) return f.template operator()<T, EQ, SHK_REC_MUSCL, SHK_FLUX_GODUNOV>();
+        if (s->rec == SHK_REC_MUSCLS) return f.template operator()<T, EQ, SHK_REC_MUSCLS, SHK_FLUX_GODUNOV>();
         if (s->rec == SHK_REC_CONSTANT) return f.template operator()<T, EQ, SHK_REC_CONSTANT, SHK_FLUX_GODUNOV>();
         if (s->rec == SHK_REC_WENOJS32) return f.template operator()<T, EQ, SHK_REC_WENOJS32, SHK_FLUX_GODUNOV>();
         return f.template operator()<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_GODUNOV>();
     }
+    if (s->rec == SHK_REC_MUSCL) return f.template operator()<T, EQ, SHK_REC_MUSCL, SHK_FLUX_EO>();
+    if (s->rec == SHK_REC_MUSCLS) return f.template operator()<T, EQ, SHK_REC_MUSCLS, SHK_FLUX_EO>();
     if (s->rec == SHK_REC_CONSTANT) return f.template operator()<T, EQ, SHK_REC_CONSTANT, SHK_FLUX_EO>();
     if (s->rec == SHK_REC_WENOJS32) return f.template operator()<T, EQ, SHK_REC_WENOJS32, SHK_FLUX_EO>();
     return f.template operator()<T, EQ, SHK_REC_WENOJS53, SHK_FLUX_EO>();
@@ -436,6 +453,10 @@ int dispatch_scheme(const shk_scheme* s, F&& f) {
             return f.template operator()<T, EQ, SHK_REC_CONSTANT, SHK_FLUX_RUSANOV>();  \
         if (s->rec == SHK_REC_WENOJS32)                                                 \
             return f.template operator()<T, EQ, SHK_REC_WENOJS32, SHK_FLUX_RUSANOV>();  \
+        if (s->rec == SHK_REC_MUSCL)                                                    \
+            return f.template operator()<T, EQ, SHK_REC_MUSCL, SHK_FLUX_RUSANOV>();     \
+        if (s->rec == SHK_REC_MUSCLS)                                                   \
+            return f.template operator()<T, EQ, SHK_REC_MUSCLS, SHK_FLUX_RUSANOV>();    \
         if (s->rec == SHK_REC_LEARNED)                                                  \
             return f.template operator()<T, EQ, SHK_REC_LEARNED, SHK_FLUX_RUSANOV>();   \
         if (s->rec == SHK_REC_ESWENO32) return f.template operator()<T, EQ, SHK_REC_ESWENO32, SHK_FLUX_ESWENO>(); \
@@ -640,6 +661,7 @@ int shk_apply_operator_bc_f64(const shk_scheme* scheme, const shk_boundary* bc, 
     const size_t smem = Smem<double>::host_bytes(W);
     const int blocks = static_cast<int>((n + tile - 1) / tile);
     OpParams<double> p = make_params<double>(scheme);
+    p.dx = dx;
     ApplyOpLaunch f{u, out, n, nghosts, tile, dx, amax, p, smem, blocks, st, b};
     const int r = dispatch_scheme<double>(scheme, f);
     if (r != SHK_OK || (b.left == SHK_BC_PERIODIC && b.right == SHK_BC_PERIODIC)) return r;
@@ -674,6 +696,7 @@ int shk_ssprk33_step_bc_f64(const shk_scheme* scheme, const shk_boundary* bc, co
     const size_t smem = Smem<double>::step_bytes(W, scheme->rec);
     const int blocks = static_cast<int>((n + tile - 1) / tile);
     OpParams<double> p = make_params<double>(scheme);
+    p.dx = dx;
     SingleStepLaunch f{u, u_out, n, nghosts, tile, dt / dx, p, smem, blocks, st, b, dx};
     const int r = dispatch_scheme<double>(scheme, f);
     if (r != SHK_OK || (b.left == SHK_BC_PERIODIC && b.right == SHK_BC_PERIODIC)) return r;

@@ -82,6 +82,10 @@ struct OpParams {
     T hnu_amax;            // LF: nu/2 * global max |f'|
     LearnedParams lp;      // learned reconstruction (float32 state only)
     T fscale;              // face values F are stored as F / fscale (see face_fluxes)
+    int lim;               // MUSCL / MUSCLS limiter (SHK_LIM_*)
+    T lim_param;           // its theta / van Albada variant
+    T atol;                // MUSCL slope-ratio cut
+    T dx;                  // cell size (the MUSCLS van Albada variant 2 slope)
 };
 
 // shared-memory layout of a step tile (see Smem::step_bytes)
@@ -144,6 +148,10 @@ __host__ __device__ inline OpParams<float> float_params(const OpParams<T>& p) {
     f.hnu_amax = static_cast<float>(p.hnu_amax);
     f.lp = p.lp;
     f.fscale = 1.0f;
+    f.lim = p.lim;
+    f.lim_param = static_cast<float>(p.lim_param);
+    f.atol = static_cast<float>(p.atol);
+    f.dx = static_cast<float>(p.dx);
     return f;
 }
 
@@ -242,6 +250,17 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
         for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
             sm.UL[c] = v[c];
             sm.UR[c] = v[c];
+        }
+        __syncthreads();
+    } else if constexpr (REC == SHK_REC_MUSCL || REC == SHK_REC_MUSCLS) {
+        for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
+            T ul, ur;
+            if constexpr (REC == SHK_REC_MUSCL)
+                muscl_cell<T>(v[c - 1], v[c], v[c + 1], p.lim, p.lim_param, p.atol, ul, ur);
+            else
+                muscls_cell<T>(v[c - 1], v[c], v[c + 1], p.lim, p.lim_param, p.dx, ul, ur);
+            sm.UL[c] = ul;
+            sm.UR[c] = ur;
         }
         __syncthreads();
     } else if constexpr (REC == SHK_REC_WENOJS32) {

@@ -106,12 +106,56 @@ class ESWENO32(Reconstruction):
     code = L.SHK_REC_ESWENO32
 
 
+@dataclass(frozen=True)
+class MUSCL(Reconstruction):
+    """Second-order MUSCL with a flux limiter on the slope ratio
+    (``src/pyshocks/reconstruction.py:172-245``)."""
+
+    lm: Any = None
+    atol: float = 1.0e-12
+
+    def __post_init__(self) -> None:
+        if self.lm is None:
+            from pyshocks_gb300.limiters import MINMODLimiter
+
+            object.__setattr__(self, "lm", MINMODLimiter(theta=1.0))
+
+    @property
+    def name(self) -> str:
+        return f"{type(self).__name__}_{type(self.lm).__name__[:-7]}".lower()
+
+    @property
+    def order(self) -> int:
+        return 2
+
+    @property
+    def stencil_width(self) -> int:
+        return 2
+
+    code = L.SHK_REC_MUSCL
+
+
+@dataclass(frozen=True)
+class MUSCLS(MUSCL):
+    """Second-order MUSCL with a slope limiter
+    (``src/pyshocks/reconstruction.py:251-290``)."""
+
+    code = L.SHK_REC_MUSCLS
+
+    def __post_init__(self) -> None:
+        super().__post_init__()
+        if type(self.lm).__name__ == "KorenLimiter":
+            raise NotImplementedError("the Koren limiter has no slope form")
+
+
 _RECONSTRUCTION: dict[str, type[Reconstruction]] = {
     "default": ConstantReconstruction,
     "constant": ConstantReconstruction,
     "wenojs32": WENOJS32,
     "wenojs53": WENOJS53,
     "esweno32": ESWENO32,
+    "muscl": MUSCL,
+    "muscls": MUSCLS,
 }
 
 

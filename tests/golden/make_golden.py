@@ -121,8 +121,21 @@ def main(refdir: pathlib.Path) -> None:
         if kind == "lwr":
             rec = reconstruction.make_reconstruction_from_name("wenojs53", eps=1.0e-6)
             return LWRRusanov(rec=rec)
-        # "<scheme>-<reconstruction>": the other Burgers fluxes and reconstructions
+        # "<scheme>-<reconstruction>": the other Burgers fluxes and reconstructions;
+        # "<scheme>-muscl[s]_<limiter>[_<param>]": MUSCL with a limiter
         sname, rname = kind.split("-")
+        if rname.startswith("muscl"):
+            from pyshocks.limiters import make_limiter_from_name
+
+            parts = rname.split("_")
+            lkw = {}
+            if parts[1] == "minmod":
+                lkw["theta"] = float(parts[2])
+            elif parts[1] == "vanalbada":
+                lkw["variant"] = int(parts[2])
+            lm = make_limiter_from_name(parts[1], **lkw)
+            cls = reconstruction.MUSCLS if parts[0] == "muscls" else reconstruction.MUSCL
+            return burgers.make_scheme_from_name(sname, rec=cls(lm=lm))
         rec = reconstruction.make_reconstruction_from_name(rname, eps=1.0e-6)
         return burgers.make_scheme_from_name(sname, rec=rec)
 
@@ -200,6 +213,18 @@ def main(refdir: pathlib.Path) -> None:
     out["neumann_rusanov_n128"] = run("rusanov", 128, smooth_ic, maxit=60, bc=nbc)
     out["dirichlet_eo_wenojs32_n100"] = run("eo-wenojs32", 100, smooth_ic, maxit=60, bc=dbc)
     out["neumann_godunov_constant_n90"] = run("godunov-constant", 90, smooth_ic, maxit=60, bc=nbc)
+
+    # MUSCL (flux limiters) and MUSCLS (slope limiters), reconstruction.py:172-296
+    for lim in ("none", "minmod_1.0", "minmod_1.5", "mc", "superbee", "vanalbada_1",
+                "vanalbada_2", "vanleer", "koren"):
+        out[f"muscl_godunov_{lim}_n96_s51"] = run(f"godunov-muscl_{lim}", 96, fourier_ic(51),
+                                                  maxit=40)
+    for lim in ("minmod_1.0", "mc", "superbee", "vanalbada_1", "vanalbada_2", "vanleer"):
+        out[f"muscls_godunov_{lim}_n96_s52"] = run(f"godunov-muscls_{lim}", 96, fourier_ic(52),
+                                                   maxit=40)
+    out["muscl_rusanov_minmod_1.0_n128_s53"] = run("rusanov-muscl_minmod_1.0", 128,
+                                                    fourier_ic(53), maxit=40)
+    out["muscls_eo_mc_n128_s54"] = run("eo-muscls_mc", 128, fourier_ic(54), maxit=40)
 
     # Godunov / Engquist-Osher fluxes and the constant / WENO-JS32 reconstructions
     out["config1_godunov_wenojs53_n256"] = run("godunov-wenojs53", 256, sine_ic, tfinal=1.0)

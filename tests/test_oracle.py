@@ -303,3 +303,62 @@ def test_numpy_oracle_boundary_runs_golden(name, flux_kind, rec, kind):
 
 
 # }}}
+
+
+# {{{ MUSCL / MUSCLS (golden runs of the reference, reconstruction.py:172-296)
+
+
+def _muscl_runs():
+    out = []
+    for p in sorted(GOLDEN.glob("muscl*_n*_s*.npz")):
+        parts = p.stem.split("_")
+        kind, flux_kind, lim = parts[0], parts[1], parts[2]
+        param = 1.0
+        if lim in ("minmod", "vanalbada"):
+            param = float(parts[3])
+        out.append((p.stem, kind, flux_kind, lim, param))
+    return out
+
+
+MUSCL_RUNS = _muscl_runs()
+
+
+def muscl_spec(kind, flux_kind, lim, param, grid):
+    return R.SchemeSpec(flux_kind=flux_kind, rec=kind, limiter=lim, limiter_param=param,
+                        atol=1.0e-12, x=grid.x, dx=grid.dx)
+
+
+@pytest.mark.parametrize(("name", "kind", "flux_kind", "lim", "param"), MUSCL_RUNS)
+def test_numpy_oracle_muscl_runs_golden(name, kind, flux_kind, lim, param):
+    """The limiters and both MUSCL forms restated: bit-identical 40-step runs."""
+    g = _load(name)
+    n = int(g["n"])
+    grid = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+    spec = muscl_spec(kind, flux_kind, lim, param, grid)
+    np.testing.assert_array_equal(R.apply_operator(spec, grid, g["u0"])[3:-3], g["rhs0"][3:-3])
+    u, dts = R.evolve(spec, grid, g["u0"], theta=1.0, maxit=40)
+    np.testing.assert_array_equal(np.array(dts), g["dts"])
+    np.testing.assert_array_equal(u[3:-3], g["u"][3:-3])
+
+
+@pytest.mark.parametrize(("lim", "param"), [("minmod", 1.0), ("minmod", 1.5), ("minmod", 2.0),
+                                            ("mc", 1.0), ("superbee", 1.0), ("vanalbada", 1),
+                                            ("vanalbada", 2), ("vanleer", 1.0), ("koren", 1.0)])
+@pytest.mark.parametrize("smooth", [True, False])
+def test_flux_limiters(lim, param, smooth):
+    """``tests/test_muscl.py:38-90``: on a sine the limiter is active somewhere;
+    on a step (piecewise constant) it vanishes, i.e. first order everywhere."""
+    n = 128
+    grid = R.make_uniform_cell_grid(-1.0, 1.0, n, 1)
+    if smooth:
+        u = np.sin(np.pi * grid.x)
+    else:
+        u = ((grid.x > -0.5) & (grid.x < 0.5)).astype(np.float64)
+    phi = np.pad(R.limiter_phi(lim, R.local_slope_ratio(u), param), 1)
+    if smooth:
+        assert np.max(phi[1:-1]) > 0.0
+    else:
+        assert np.max(phi[1:-1]) < 1.0e-12
+
+
+# }}}
