@@ -155,23 +155,24 @@ __device__ __forceinline__ void weno53_cell(T v, T Hm2, T Hm1, T H0, T Hp1, T Dm
 }
 
 // Forward-path variant of weno53_cell on unscaled differences (fewer FP64
-// instructions): d_k = v_{k+1} - v_k, E_k = d_k - d_{k-1}, G_k = 13/3 E_k^2, and
-// 4 beta_j = G + h'^2 with h'_0 = E_{c-1} + 2 d_{c-1}, h'_1 = d_c + d_{c-1},
-// h'_2 = E_{c+1} - 2 d_c. With eps4 = 4 eps every s_j and P_j is scaled by a
-// common power of two, which cancels in the normalised weights. The
+// instructions): d_k = v_{k+1} - v_k, E_k = d_k - d_{k-1}, G_k = 13/3 E_k^2 + 4 eps,
+// and 4 (beta_j + eps) = G + h'^2 with h'_0 = E_{c-1} + 2 d_{c-1}, h'_1 = d_c + d_{c-1},
+// h'_2 = E_{c+1} - 2 d_c. Every s_j and P_j is thus scaled by a common power
+// of two, which cancels in the normalised weights. The
 // corrections 6 (uhat_k - v) (weights (1, 6, 3) folded as in weno53_cell) use
 // d_{c-2} = 3 d_{c-1} - h'_0 and d_{c+1} = h'_2 + 3 d_c:
 //   cr0 = 2 h'_0 - d_{c-1}      cr1 = 6 d_{c-1} + 12 d_c     cr2 = 3 (d_c - h'_2)
 //   cl0 = 2 h'_2 + d_c          cl1 = 6 E_c - cr1            cl2 = -3 (h'_0 + d_{c-1})
 __device__ __forceinline__ void weno53_cell_d(double v, double dm1, double d0, double Em1,
                                               double E0, double Ep1, double Gm1, double G0,
-                                              double Gp1, double eps4, double& ul, double& ur) {
+                                              double Gp1, double& ul, double& ur) {
+    // G_k = 13/3 E_k^2 + 4 eps (eps folded in when G is formed)
     const double h0 = fma(2.0, dm1, Em1);
     const double h1 = d0 + dm1;
     const double h2 = fma(-2.0, d0, Ep1);
-    double s0 = eps4 + fma(h0, h0, Gm1); s0 = s0 * s0;
-    double s1 = eps4 + fma(h1, h1, G0); s1 = s1 * s1;
-    double s2 = eps4 + fma(h2, h2, Gp1); s2 = s2 * s2;
+    double s0 = fma(h0, h0, Gm1); s0 = s0 * s0;
+    double s1 = fma(h1, h1, G0); s1 = s1 * s1;
+    double s2 = fma(h2, h2, Gp1); s2 = s2 * s2;
     const double P0 = s1 * s2, P1 = s0 * s2, P2 = s0 * s1;
     const double cr0 = fma(2.0, h0, -dm1);
     const double cr1 = fma(12.0, d0, 6.0 * dm1);

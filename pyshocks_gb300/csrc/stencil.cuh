@@ -203,19 +203,19 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
         // phase A: d_c = v_{c+1} - v_c, c in [lo-3, hi+2)
         for (int c = lo - 3 + tid; c < hi + 2; c += nt) sm.H[c] = v[c + 1] - v[c];
         __syncthreads();
-        // phase B: E_c = d_c - d_{c-1}, G_c = 13/3 E_c^2, c in [lo-2, hi+2)
+        // phase B: E_c = d_c - d_{c-1}, G_c = 13/3 E_c^2 + 4 eps, c in [lo-2, hi+2)
+        const T eps4 = T(4) * p.eps;
         for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
             const T e = sm.H[c] - sm.H[c - 1];
             sm.D[c] = e;
-            sm.Q[c] = (T(13.0 / 3.0) * e) * e;
+            sm.Q[c] = fma(T(13.0 / 3.0) * e, e, eps4);
         }
         __syncthreads();
-        const T eps4 = T(4) * p.eps;
 #pragma unroll 2
         for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
             T ul, ur;
             weno53_cell_d(v[c], sm.H[c - 1], sm.H[c], sm.D[c - 1], sm.D[c], sm.D[c + 1],
-                          sm.Q[c - 1], sm.Q[c], sm.Q[c + 1], eps4, ul, ur);
+                          sm.Q[c - 1], sm.Q[c], sm.Q[c + 1], ul, ur);
             sm.UL[c] = ul;
             sm.UR[c] = ur;
         }
