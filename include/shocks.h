@@ -188,9 +188,9 @@ int shk_plan_set_fixed_dt(shk_plan* plan, const double* dt, int32_t nsteps, void
 /* time-independent Dirichlet / Neumann boundaries for every instance of the
  * plan: dirichlet [B][2][3] ghost values, neumann [B][2] gradients (device or
  * host memory, copied on `stream`; either may be NULL if no side uses it).
- * left = right = SHK_BC_PERIODIC restores periodic instances. Plans with a
- * non-periodic boundary step forward only (shk_plan_adjoint:
- * SHK_EUNSUPPORTED). Drops a captured step graph. */
+ * left = right = SHK_BC_PERIODIC restores periodic instances; the adjoint of
+ * such a plan is the exact transpose with the boundary data as constants.
+ * Drops a captured step graph. */
 int shk_plan_set_boundary(shk_plan* plan, int32_t left, int32_t right, const double* dirichlet,
                           const double* neumann, void* stream);
 
@@ -220,6 +220,13 @@ int shk_plan_status(shk_plan* plan, int32_t* h_status, void* stream);
 int shk_ssprk33_vjp_f64(const shk_scheme* scheme, const double* u, const double* p_next,
                         double* p_out, int64_t n, int32_t nghosts, double dx, double dt,
                         void* stream);
+
+/* shk_ssprk33_vjp_f64 for a step taken with a Dirichlet / Neumann boundary
+ * (shk_ssprk33_step_bc_f64 with the same `bc`): the exact transpose, the
+ * boundary's data entering as constants (NULL: periodic). */
+int shk_ssprk33_vjp_bc_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
+                           const double* p_next, double* p_out, int64_t n, int32_t nghosts,
+                           double dx, double dt, void* stream);
 
 /* forward run of `nsteps` steps (as shk_plan_step) that also copies the state
  * before every step k with k % stride == 0 into ckpt[k / stride] (caller-owned,

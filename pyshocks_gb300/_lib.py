@@ -111,6 +111,8 @@ SIGNATURES: dict[str, tuple] = {
     "shk_plan_status": (ctypes.c_int, [_P, ctypes.POINTER(_I32), _P]),
     "shk_plan_reduce": (ctypes.c_int, [_P, _P, _I32, _P, _P]),
     "shk_ssprk33_vjp_f64": (ctypes.c_int, [_SCH, _P, _P, _P, _I64, _I32, _D, _D, _P]),
+    "shk_ssprk33_vjp_bc_f64": (ctypes.c_int, [_SCH, ctypes.POINTER(ShkBoundary), _P, _P, _P, _I64,
+                                              _I32, _D, _D, _P]),
     "shk_plan_forward_checkpointed": (ctypes.c_int, [_P, _P, _P, _I32, _P, _I32, _P]),
     "shk_plan_adjoint": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _P]),
     "shk_apply_operator_lf_noalloc_f64": (ctypes.c_int, [_SCH, _P, _P, _I64, _I32, _D, _P]),

@@ -20,6 +20,8 @@ same interior result, because interior outputs do not depend on input ghosts
 
 from __future__ import annotations
 
+import ctypes
+
 import math
 
 import torch
@@ -92,18 +94,29 @@ def solve(u0: torch.Tensor, checkpointed: CheckpointedSolve, *, t0=None, tfinal=
     return _SolveFn.apply(u0, checkpointed, t0, tfinal)
 
 
-def vjp_step(scheme, grid, dt: float, u: torch.Tensor, p_next: torch.Tensor) -> torch.Tensor:
+def vjp_step(scheme, grid, dt: float, u: torch.Tensor, p_next: torch.Tensor, *,
+             bc=None, t: float = 0.0) -> torch.Tensor:
     """``(d advance / d u)^T p_next`` of one SSPRK33 step of a ghosted single
-    instance (``jac.T @ p`` of ``src/pyshocks/timestepping.py:205-206``)."""
-    for name, t in (("u", u), ("p", p_next)):
-        if not (t.is_cuda and t.dtype == torch.float64 and t.is_contiguous()
-                and t.shape[0] == grid.x.shape[0]):
+    instance (``jac.T @ p`` of ``src/pyshocks/timestepping.py:205-206``). With
+    a Dirichlet / Neumann *bc* the step from time *t* is transposed exactly,
+    the boundary data entering as constants."""
+    for name, arr in (("u", u), ("p", p_next)):
+        if not (arr.is_cuda and arr.dtype == torch.float64 and arr.is_contiguous()
+                and arr.shape[0] == grid.x.shape[0]):
             raise ValueError(f"{name}: expected a contiguous float64 CUDA array of {grid.x.shape[0]}")
     out = torch.empty_like(u)
+    cb = None
+    if bc is not None:
+        from pyshocks_gb300.burgers import c_boundary
+
+        dt_ = float(dt)
+        cb = c_boundary(bc, grid, (float(t), float(t) + dt_, float(t) + 0.5 * dt_))
     L.check(
-        L.lib().shk_ssprk33_vjp_f64(scheme.c_scheme(grid.dx_min), u.data_ptr(), p_next.data_ptr(),
-                                    out.data_ptr(), grid.ncells, grid.nghosts,
-                                    float(grid.dx_min), float(dt), L.stream_handle()),
+        L.lib().shk_ssprk33_vjp_bc_f64(scheme.c_scheme(grid.dx_min),
+                                       None if cb is None else ctypes.byref(cb), u.data_ptr(),
+                                       p_next.data_ptr(), out.data_ptr(), grid.ncells,
+                                       grid.nghosts, float(grid.dx_min), float(dt),
+                                       L.stream_handle()),
         "ssprk33_vjp",
     )
     return out

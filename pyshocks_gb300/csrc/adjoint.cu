@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "stencil.cuh"
@@ -266,15 +267,21 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
 // a.U, which is dead once af.U is written).
 template <int EQ>
 __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float>& af, double* gout,
-                                   int te, double dtdx, const OpParams<double>& p) {
+                                   int te, double dtdx, const OpParams<double>& p,
+                                   const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0) {
     constexpr int HU = adj_uhalo<double>(), HP = adj_phalo<double>();
     constexpr int REC = SHK_REC_LEARNED;
     const int tid = threadIdx.x, nt = blockDim.x;
+    const bool np = !bc.periodic();
     const OpParams<float> pf = float_params(p);
     const float dtf = static_cast<float>(dtdx);
     for (int i = tid; i < te + 2 * HU; i += nt) af.U[i] = static_cast<float>(a.U[i]);
     for (int i = HU - HP + tid; i < HU + te + HP; i += nt) af.PB[i] = static_cast<float>(a.PB[i]);
     __syncthreads();
+    if (np) {
+        apply_bc(af.U, g0, n, 0, te + 2 * HU, bc, 0);
+        zero_outside(af.PB, g0, n, HU - HP, HU + te + HP);
+    }
     // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12)
     {
         const int lo = HU - 15, hi = HU + te + 15;
@@ -285,6 +292,7 @@ __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float
             af.K1[i] = af.U[i] + d;
         }
         __syncthreads();
+        if (np) apply_bc(af.K1, g0, n, lo, hi, bc, 1);
     }
     {
         const int lo = HU - 12, hi = HU + te + 12;
@@ -294,11 +302,13 @@ __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float
             af.K2[i] = af.U[i] + d;
         }
         __syncthreads();
+        if (np) apply_bc(af.K2, g0, n, lo, hi, bc, 2);
     }
     // reverse stage 3: k2b = 2/3 (p + Z3), Z3 = dt J(k2)^T p
     {
         const int lo = HU - 6, hi = HU + te + 6;
         vjp_stage<float, EQ, REC>(af.K2, af.PB, af.Z, lo, hi, af, pf, dtf);
+        if (np) bc_transpose(af.Z, g0, n, lo, hi, bc);
         for (int i = lo + tid; i < hi; i += nt) af.CB[i] = (2.0f / 3.0f) * (af.PB[i] + af.Z[i]);
         for (int i = HU + tid; i < HU + te; i += nt) af.ACC[i] = (2.0f / 3.0f) * af.Z[i];
         __syncthreads();
@@ -307,29 +317,54 @@ __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float
     {
         const int lo = HU - 3, hi = HU + te + 3;
         vjp_stage<float, EQ, REC>(af.K1, af.CB, af.Z, lo, hi, af, pf, dtf);
+        if (np) bc_transpose(af.Z, g0, n, lo, hi, bc);
         for (int i = HU + tid; i < HU + te; i += nt) af.ACC[i] = fmaf(0.25f, af.Z[i], af.ACC[i]);
         for (int i = lo + tid; i < hi; i += nt) af.CB[i] = 0.25f * (af.CB[i] + af.Z[i]);
         __syncthreads();
     }
     // reverse stage 1: Z1 = dt J(u)^T k1b; ub = p + (2/3 Z3 + 1/4 Z2 + Z1)
+    // (and on the ghosts of a boundary tile)
     {
-        const int lo = HU, hi = HU + te;
+        int lo = HU, hi = HU + te;
+        if (np) {
+            for (int i = tid; i < 3; i += nt) {  // k1b beyond its range: zero
+                af.CB[HU - 6 + i] = 0.0f;
+                af.CB[HU + te + 3 + i] = 0.0f;
+            }
+            __syncthreads();
+            if (g0 + HU == 0) lo -= 3;
+            if (g0 + HU + te == n) hi += 3;
+        }
         vjp_stage<float, EQ, REC>(af.U, af.CB, af.Z, lo, hi, af, pf, dtf);
-        for (int i = lo + tid; i < hi; i += nt)
+        if (np) bc_transpose(af.Z, g0, n, lo, hi, bc);
+        for (int i = HU + tid; i < HU + te; i += nt)
             gout[i - HU] = a.PB[i] + static_cast<double>(af.ACC[i] + af.Z[i]);
     }
 }
 
 // one adjoint step of a tile: p_out[s, s+te) from u_m (window, halo 20) and
 // p_next (window, halo 10/12). gout points at p_out + s.
+// With a Dirichlet / Neumann boundary (bc; g0 = s - HU the global cell of
+// window position 0, n the instance's cells) the forward recompute applies the
+// boundary at each stage, the cotangent window is zeroed outside the instance,
+// each reverse stage is followed by the boundary's transpose, and the first
+// reverse stage of a boundary tile also covers the ghost cells (their
+// cotangents reach the interior through the Neumann mirrors).
 template <class T, int EQ, int REC>
-__device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const OpParams<T>& p) {
+__device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const OpParams<T>& p,
+                             const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0) {
     if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED) {
         // full double layout: the float arrays fit from CB on (20 in 16 double ones)
         AdjSmem<float> af;
         af.carve(reinterpret_cast<unsigned char*>(a.CB), a.W);
-        adjoint_tile_mixed<EQ>(a, af, gout, te, dtdx, p);
+        adjoint_tile_mixed<EQ>(a, af, gout, te, dtdx, p, bc, g0, n);
         return;
+    }
+    const bool np = !bc.periodic();
+    if (np) {
+        constexpr int HU0 = adj_uhalo<T>(), HP0 = adj_phalo<T>();
+        apply_bc(a.U, g0, n, 0, te + 2 * HU0, bc, 0);
+        zero_outside(a.PB, g0, n, HU0 - HP0, HU0 + te + HP0);
     }
     constexpr int HU = adj_uhalo<T>();
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -349,6 +384,7 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
             }
         }
         __syncthreads();
+        if (np) apply_bc(a.K1, g0, n, lo, hi, bc, 1);
     }
     {
         const int lo = HU - 12, hi = HU + te + 12;
@@ -362,11 +398,13 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
             }
         }
         __syncthreads();
+        if (np) apply_bc(a.K2, g0, n, lo, hi, bc, 2);
     }
     // reverse stage 3: k2b = 2/3 (p + dt J(k2)^T p) on [HU-6, HU+te+6)
     {
         const int lo = HU - 6, hi = HU + te + 6;
         vjp_stage<T, EQ, REC>(a.K2, a.PB, a.Z, lo, hi, a, p, dtdx);
+        if (np) bc_transpose(a.Z, g0, n, lo, hi, bc);
         for (int i = lo + tid; i < hi; i += nt) a.CB[i] = T(2.0 / 3.0) * (a.PB[i] + a.Z[i]);
         __syncthreads();
         for (int i = HU + tid; i < HU + te; i += nt)
@@ -377,14 +415,26 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     {
         const int lo = HU - 3, hi = HU + te + 3;
         vjp_stage<T, EQ, REC>(a.K1, a.CB, a.Z, lo, hi, a, p, dtdx);
+        if (np) bc_transpose(a.Z, g0, n, lo, hi, bc);
         for (int i = lo + tid; i < hi; i += nt) a.CB[i] = T(1.0 / 4.0) * (a.CB[i] + a.Z[i]);
         __syncthreads();
     }
     // reverse stage 1: ub = 1/3 p + 3/4 k2b + k1b + dt J(u)^T k1b on the tile
+    // (and on the ghosts of a boundary tile)
     {
-        const int lo = HU, hi = HU + te;
+        int lo = HU, hi = HU + te;
+        if (np) {
+            for (int i = tid; i < 3; i += nt) {  // k1b beyond its range: zero
+                a.CB[HU - 6 + i] = T(0);
+                a.CB[HU + te + 3 + i] = T(0);
+            }
+            __syncthreads();
+            if (g0 + HU == 0) lo -= 3;
+            if (g0 + HU + te == n) hi += 3;
+        }
         vjp_stage<T, EQ, REC>(a.U, a.CB, a.Z, lo, hi, a, p, dtdx);
-        for (int i = lo + tid; i < hi; i += nt) gout[i - HU] = a.ACC[i] + (a.CB[i] + a.Z[i]);
+        if (np) bc_transpose(a.Z, g0, n, lo, hi, bc);
+        for (int i = HU + tid; i < HU + te; i += nt) gout[i - HU] = a.ACC[i] + (a.CB[i] + a.Z[i]);
     }
 }
 
@@ -454,8 +504,10 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
             return;
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
-        if constexpr (kMixed) adjoint_tile_mixed<EQ>(a, af, pout + off + s0, te, dtdx, p);
-        else adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p);
+        const BcView bc = plan_bc(P, b);
+        const int64_t g0 = s0 - adj_uhalo<T>();
+        if constexpr (kMixed) adjoint_tile_mixed<EQ>(a, af, pout + off + s0, te, dtdx, p, bc, g0, n);
+        else adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p, bc, g0, n);
         __syncthreads();
     }
 }
@@ -495,7 +547,8 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
             return;
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
-        step_tile<T, EQ, REC, SHK_FLUX_RUSANOV>(sm, uout + off + s0, te, dtdx, p);
+        step_tile<T, EQ, REC, SHK_FLUX_RUSANOV>(sm, uout + off + s0, te, dtdx, p, plan_bc(P, b),
+                                                s0 - HL, n);
         __syncthreads();
     }
 }
@@ -505,7 +558,7 @@ template <class T, int EQ>
 __global__ void __launch_bounds__(kThreads) single_vjp_kernel(const T* __restrict__ u, const T* __restrict__ pn,
                                                               T* __restrict__ pout, int64_t n, int g,
                                                               int tile, T dtdx, OpParams<T> p,
-                                                              int32_t* err) {
+                                                              int32_t* err, shk_boundary bcp, double dx) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     AdjSmem<T> a;
@@ -522,7 +575,15 @@ __global__ void __launch_bounds__(kThreads) single_vjp_kernel(const T* __restric
         if (threadIdx.x == 0 && err) atomicOr(err, ERR_TIMEOUT);
         return;
     }
-    adjoint_tile<T, EQ, SHK_REC_WENOJS53>(a, pout + g + s0, te, dtdx, p);
+    BcView bc;
+    bc.left = bcp.left;
+    bc.right = bcp.right;
+    bc.dir = &bcp.dirichlet[0][0][0];
+    bc.dir_ss = 6;
+    bc.neu = &bcp.neumann[0][0];
+    bc.neu_ss = 2;
+    bc.dx = dx;
+    adjoint_tile<T, EQ, SHK_REC_WENOJS53>(a, pout + g + s0, te, dtdx, p, bc, s0 - adj_uhalo<T>(), n);
     // ghost cotangents are zero (interior-only adjoint)
     if (blockIdx.x == 0)
         for (int i = threadIdx.x; i < g; i += blockDim.x) {
@@ -627,11 +688,11 @@ struct ReplayLaunch {
 
 struct SingleVjpLaunch {
     const double* u; const double* pn; double* po; int64_t n; int g; int tile; double dtdx;
-    OpParams<double> p; size_t smem; int blocks; cudaStream_t st;
+    OpParams<double> p; size_t smem; int blocks; cudaStream_t st; shk_boundary bc; double dx;
     template <class T, int EQ, int REC> int operator()() {
         auto k = single_vjp_kernel<T, EQ>;
         ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<blocks, kThreads, smem, st>>>(u, pn, po, n, g, tile, dtdx, p, nullptr);
+        k<<<blocks, kThreads, smem, st>>>(u, pn, po, n, g, tile, dtdx, p, nullptr, bc, dx);
         return acuda(cudaGetLastError());
     }
 };
@@ -640,11 +701,17 @@ struct SingleVjpLaunch {
 
 extern "C" {
 
-int shk_ssprk33_vjp_f64(const shk_scheme* scheme, const double* u, const double* p_next,
-                        double* p_out, int64_t n, int32_t nghosts, double dx, double dt,
-                        void* stream) {
+int shk_ssprk33_vjp_bc_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
+                           const double* p_next, double* p_out, int64_t n, int32_t nghosts,
+                           double dx, double dt, void* stream) {
     if (!adjoint_supported(scheme) || scheme->rec != SHK_REC_WENOJS53 || !u || !p_next || !p_out || n < 3 || nghosts < 3 ||
         !(dx > 0) || !(dt >= 0))
+        return SHK_EINVAL;
+    shk_boundary b;
+    std::memset(&b, 0, sizeof(b));
+    if (bc) b = *bc;
+    if (b.left < SHK_BC_PERIODIC || b.left > SHK_BC_NEUMANN || b.right < SHK_BC_PERIODIC ||
+        b.right > SHK_BC_NEUMANN || ((b.left == SHK_BC_PERIODIC) != (b.right == SHK_BC_PERIODIC)))
         return SHK_EINVAL;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int tile = kAdjTile;
@@ -652,8 +719,14 @@ int shk_ssprk33_vjp_f64(const shk_scheme* scheme, const double* u, const double*
     const size_t smem = AdjSmem<double>::host_bytes(W);
     const int blocks = static_cast<int>((n + tile - 1) / tile);
     SingleVjpLaunch f{u, p_next, p_out, n, nghosts, tile, dt / dx, adj_params<double>(scheme),
-                      smem, blocks, st};
+                      smem, blocks, st, b, dx};
     return by_equation<double>(scheme->equation, f);
+}
+
+int shk_ssprk33_vjp_f64(const shk_scheme* scheme, const double* u, const double* p_next,
+                        double* p_out, int64_t n, int32_t nghosts, double dx, double dt,
+                        void* stream) {
+    return shk_ssprk33_vjp_bc_f64(scheme, nullptr, u, p_next, p_out, n, nghosts, dx, dt, stream);
 }
 
 int shk_plan_forward_checkpointed(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps,
@@ -694,7 +767,6 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
     int r = plan_view(plan, &D, &dtype, &grid, &sch, &total, nullptr);
     if (r != SHK_OK) return r;
     if (!adjoint_supported(&sch)) return SHK_EUNSUPPORTED;
-    if (D.bc_left != SHK_BC_PERIODIC || D.bc_right != SHK_BC_PERIODIC) return SHK_EUNSUPPORTED;
     if (!D.dt_hist || D.max_steps < nsteps) return SHK_EINVAL;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const size_t esz = dtype == SHK_F64 ? 8 : 4;

@@ -137,6 +137,40 @@ __device__ void apply_bc(V* S, int64_t g0, int64_t n, int wlo, int whi, const Bc
     __syncthreads();
 }
 
+// Transpose of the ghost fill on a cotangent window z over [wlo, whi): the
+// cotangent of a Dirichlet ghost vanishes (its value is data), that of a
+// Neumann ghost (mirror - (2k+1) dx g) moves to its mirrored interior cell.
+// One thread walks the six ghosts in order (mirrors of the two sides can
+// coincide on tiny instances). Call after a barrier; ends with one.
+template <class V>
+__device__ void bc_transpose(V* z, int64_t g0, int64_t n, int wlo, int whi, const BcView& bc) {
+    if (threadIdx.x == 0) {
+        for (int t = 0; t < 6; ++t) {
+            const int side = t / 3, k = t - 3 * side;
+            const int kind = side ? bc.right : bc.left;
+            const int64_t w = (side ? n + k : -1 - k) - g0;
+            if (kind == SHK_BC_PERIODIC || w < wlo || w >= whi) continue;
+            if (kind == SHK_BC_NEUMANN) {
+                const int64_t wm = (side ? n - 1 - k : k) - g0;
+                if (wm >= wlo && wm < whi) z[wm] += z[w];
+            }
+            z[w] = V(0);
+        }
+    }
+    __syncthreads();
+}
+
+// zero a window array at positions outside the instance [0, n) (the circular
+// loader wrapped them in): cotangents of a non-periodic instance
+template <class V>
+__device__ void zero_outside(V* z, int64_t g0, int64_t n, int wlo, int whi) {
+    for (int w = wlo + threadIdx.x; w < whi; w += blockDim.x) {
+        const int64_t gi = g0 + w;
+        if (gi < 0 || gi >= n) z[w] = V(0);
+    }
+    __syncthreads();
+}
+
 // float copy of the operator parameters (the mixed-precision learned path)
 template <class T>
 __host__ __device__ inline OpParams<float> float_params(const OpParams<T>& p) {

@@ -208,12 +208,16 @@ def adjoint_step(
     from pyshocks_gb300 import adjoint as adj
     from pyshocks_gb300 import burgers
 
-    fused = isinstance(src, OperatorSource) and isinstance(
-        src.scheme, burgers.GpuConservationLawScheme) and src.scheme.flux_code == burgers.L.SHK_FLUX_RUSANOV
+    gpu = isinstance(src, OperatorSource) and isinstance(src.scheme, burgers.GpuConservationLawScheme)
+    fused = gpu and src.scheme.flux_code == burgers.L.SHK_FLUX_RUSANOV and getattr(
+        src.scheme.rec, "code", -1) == burgers.L.SHK_REC_WENOJS53
+    if gpu and not fused:
+        raise NotImplementedError("the matrix-free adjoint covers Rusanov with WENO-JS5 "
+                                  "(single instance) and the learned scheme (batched plans)")
 
     def _vjp(dt, t, u, p):
         if fused:
-            return adj.vjp_step(src.scheme, src.grid, dt, u, p)
+            return adj.vjp_step(src.scheme, src.grid, dt, u, p, bc=src.bc, t=float(t))
         # generic closures: differentiate advance() with torch (dt, t constant)
         _, fn = torch.func.vjp(lambda v: advance(stepper, dt, t, v), u)
         return fn(p)[0]

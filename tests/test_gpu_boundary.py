@@ -154,14 +154,85 @@ def test_batched_plan_with_boundary_matches_oracle(kind, dtype):
         assert err < tol, (b, err)
 
 
-def test_adjoint_refuses_non_periodic_plans():
+@pytest.mark.parametrize("kind", ["dirichlet", "neumann"])
+def test_batched_adjoint_with_boundary_against_finite_differences(kind):
+    """The exact transpose of the boundary in the batched checkpointed adjoint:
+    dJ/du0 . v against central differences of J with the dt sequence replayed
+    (two instances, one smaller than a tile)."""
     from pyshocks_gb300.adjoint import CheckpointedSolve
     from pyshocks_gb300.batched import BatchedSolver
 
-    s = BatchedSolver(_scheme("rusanov", "wenojs53"), [256], 2.0 / 256, max_steps=4)
-    s.set_boundary("neumann", neumann=[0.0, 0.0])
-    cs = CheckpointedSolve(s, 4)
-    u0 = torch.tensor(0.5 + 0.2 * np.sin(np.linspace(0, 2 * np.pi, 256)), device="cuda")
-    uT = cs.forward(u0)
-    with pytest.raises(Exception):
-        cs.backward(uT.clone())
+    sizes, nsteps = [200, 1300], 24
+    x = [np.linspace(-1, 1, n + 1)[:-1] + 1.0 / n for n in sizes]
+    u0 = torch.tensor(np.concatenate([0.6 + 0.25 * np.sin(np.pi * xx) + 0.1 * np.cos(3 * np.pi * xx)
+                                      for xx in x]), device="cuda")
+    rng = np.random.default_rng(4)
+    tgt = u0 + 0.05 * torch.tensor(rng.standard_normal(u0.numel()), device="cuda")
+    scheme = _scheme("rusanov", "wenojs53")
+    dvals = [[0.7, 0.55], [0.4, 0.8]]
+    nvals = [[0.2, -0.1], [-0.3, 0.25]]
+
+    def solver():
+        s = BatchedSolver(scheme, sizes, [2.0 / n for n in sizes], max_steps=nsteps)
+        if kind == "dirichlet":
+            d = np.array(dvals)[:, :, None].repeat(3, axis=2)
+            s.set_boundary("dirichlet", dirichlet=d)
+        else:
+            s.set_boundary("neumann", neumann=nvals)
+        return s
+
+    s = solver()
+    cs = CheckpointedSolve(s, nsteps, stride=5)
+    uT = cs.forward(u0).clone()
+    g = cs.backward(uT - tgt).clone()
+    dts = s.dt_history().clone()
+
+    def J(u):
+        s2 = solver()
+        s2.set_fixed_dt(dts)
+        uT2 = CheckpointedSolve(s2, nsteps).forward(u)
+        return 0.5 * float(torch.sum((uT2 - tgt) ** 2))
+
+    assert abs(J(u0) - 0.5 * float(torch.sum((uT - tgt) ** 2))) < 1.0e-12
+    h = 1.0e-6
+    for k in range(3):
+        v = torch.tensor(rng.standard_normal(u0.numel()), device="cuda")
+        fd = (J(u0 + h * v) - J(u0 - h * v)) / (2 * h)
+        ad = float(torch.dot(g, v))
+        # 1e-5: the bar of the periodic test (the Rusanov max(|u_j|, |u_j+1|)
+        # switches near extrema within +-h v)
+        assert abs(fd - ad) < 1.0e-5 * max(1.0, abs(ad)), (k, fd, ad)
+
+
+@pytest.mark.parametrize("kind", ["dirichlet", "neumann"])
+def test_single_step_vjp_with_boundary_against_finite_differences(kind):
+    """``vjp_step`` with time-dependent boundary data (ghosted single
+    instance): the transpose of one step against central differences."""
+    import pyshocks_gb300 as gb
+    from pyshocks_gb300 import burgers
+    from pyshocks_gb300.adjoint import vjp_step
+
+    n, t, dt = 300, 0.4, 2.0e-3
+    grid = gb.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
+    bc = _bc(kind)
+    scheme = gb.bind(_scheme("rusanov", "wenojs53"), grid, bc)
+    xg = grid.x
+    u = (0.6 + 0.25 * torch.sin(np.pi * xg) + 0.1 * torch.cos(3 * np.pi * xg)).contiguous()
+    rng = np.random.default_rng(6)
+    p = torch.zeros_like(u)
+    p[3:-3] = torch.tensor(rng.standard_normal(n), device="cuda")
+    g = vjp_step(scheme, grid, dt, u, p, bc=bc, t=t)
+
+    def J(v):
+        out = burgers.ssprk33_step(scheme, grid, bc, dt, v, t=t)
+        return float(torch.dot(out[3:-3], p[3:-3]))
+
+    # h = 1e-7: the WENO weights ~ 1/(eps + beta)^2 at beta ~ (dx u')^2 make
+    # J''' ~ 1e8, so the h^2/6 truncation of h = 1e-6 is ~1e-5 of the gradient
+    h = 1.0e-7
+    for k in range(3):
+        w = torch.zeros_like(u)
+        w[3:-3] = torch.tensor(rng.standard_normal(n), device="cuda")
+        fd = (J(u + h * w) - J(u - h * w)) / (2 * h)
+        ad = float(torch.dot(g[3:-3], w[3:-3]))
+        assert abs(fd - ad) < 2.0e-7 * max(1.0, abs(ad)), (k, fd, ad)
