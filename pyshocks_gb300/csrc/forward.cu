@@ -51,7 +51,7 @@ __device__ void finalize_step(const PlanDev& P, int64_t k) {
 }
 
 template <class T, int EQ, int REC, int FLUX>
-__global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) batched_step_kernel(PlanDev P, const T* __restrict__ uin,
+__global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC == SHK_REC_WENOJS53 && sizeof(T) == 8 ? 3 : 1)) batched_step_kernel(PlanDev P, const T* __restrict__ uin,
                                                                 T* __restrict__ uout, OpParams<T> p) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
