@@ -64,12 +64,21 @@ __device__ __forceinline__ bool outside_band(const float w[3], const float wj[3]
     return excess > lp.band || d > lp.dev;
 }
 
+// 1/x to ~1 ulp (rcp.approx.ftz.f32, one instruction) for the float weights and
+// normalisation of the learned path, where a correctly rounded division buys
+// nothing (all arguments here are >= eps-sized normal numbers)
+__device__ __forceinline__ float fast_rcp(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // x = (s - mean) / (max - min + norm_eps)
 __device__ __forceinline__ void mlp_normalise(const float s[5], float x[5], float norm_eps) {
     float m = (s[0] + s[1] + s[2] + s[3] + s[4]) * 0.2f;
     float lo = fminf(fminf(fminf(s[0], s[1]), fminf(s[2], s[3])), s[4]);
     float hi = fmaxf(fmaxf(fmaxf(s[0], s[1]), fmaxf(s[2], s[3])), s[4]);
-    const float inv = 1.0f / (hi - lo + norm_eps);
+    const float inv = fast_rcp(hi - lo + norm_eps);
 #pragma unroll
     for (int k = 0; k < 5; ++k) x[k] = (s[k] - m) * inv;
 }
@@ -90,10 +99,10 @@ __device__ __forceinline__ void js_betas(const float s[5], float be[3], float q[
 __device__ __forceinline__ void js_weights_pair(const float be[3], float eps, float wr[3],
                                                 float wl[3]) {
     const float e0 = eps + be[0], e1 = eps + be[1], e2 = eps + be[2];
-    const float r0 = 1.0f / (e0 * e0), r1 = 1.0f / (e1 * e1), r2 = 1.0f / (e2 * e2);
+    const float r0 = fast_rcp(e0 * e0), r1 = fast_rcp(e1 * e1), r2 = fast_rcp(e2 * e2);
     const float a1 = 0.6f * r1;
-    const float ir = 1.0f / fmaf(0.1f, r0, fmaf(0.3f, r2, a1));
-    const float il = 1.0f / fmaf(0.1f, r2, fmaf(0.3f, r0, a1));
+    const float ir = fast_rcp(fmaf(0.1f, r0, fmaf(0.3f, r2, a1)));
+    const float il = fast_rcp(fmaf(0.1f, r2, fmaf(0.3f, r0, a1)));
     wr[0] = 0.1f * r0 * ir; wr[1] = a1 * ir; wr[2] = 0.3f * r2 * ir;
     wl[0] = 0.1f * r2 * il; wl[1] = a1 * il; wl[2] = 0.3f * r0 * il;
 }
@@ -543,7 +552,7 @@ __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpB
     const float m = (s[0] + s[1] + s[2] + s[3] + s[4]) * 0.2f;
     float lo = fminf(fminf(fminf(s[0], s[1]), fminf(s[2], s[3])), s[4]);
     float hi = fmaxf(fmaxf(fmaxf(s[0], s[1]), fmaxf(s[2], s[3])), s[4]);
-    const float inv = 1.0f / (hi - lo + lp.norm_eps);
+    const float inv = fast_rcp(hi - lo + lp.norm_eps);
     float sdx = 0.0f, sxd = 0.0f;
     int nhi = 0, nlo = 0;
 #pragma unroll
@@ -558,7 +567,7 @@ __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpB
 #pragma unroll
     for (int k = 0; k < 5; ++k) {
         float dd = inv * (dx[k] - 0.2f * sdx);
-        dd += gr * ((s[k] == hi ? 1.0f / nhi : 0.0f) - (s[k] == lo ? 1.0f / nlo : 0.0f));
+        dd += gr * ((s[k] == hi ? fast_rcp(float(nhi)) : 0.0f) - (s[k] == lo ? fast_rcp(float(nlo)) : 0.0f));
         dsum[k] += dd;
     }
 }
