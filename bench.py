@@ -624,7 +624,7 @@ def bench_inverse(dev, args) -> dict:
                        for m, x in zip(sizes, torch.split(truth, list(sizes)))])
     prob.run(guess, 1, graph=True)  # capture + warm-up
     torch.cuda.synchronize()
-    iters = 3
+    iters = args.inverse_iters
     t0 = time.perf_counter()
     hist = prob.run(guess, iters, graph=True)
     torch.cuda.synchronize()
@@ -678,6 +678,10 @@ def main() -> None:
     ap.add_argument("--adjoint-steps", type=int, default=4000)
     ap.add_argument("--inverse-steps", type=int, default=300,
                     help="SSPRK33 steps per solve of the inverse-problem leg (full: 3000)")
+    ap.add_argument("--inverse-iters", type=int, default=3,
+                    help="timed gradient-descent iterations of the inverse-problem leg (full: 50)")
+    ap.add_argument("--inverse-only", action="store_true",
+                    help="run only the inverse-problem leg (one JSON line)")
     ap.add_argument("--scheme", choices=["plain", "learned", "learned32"], default="plain",
                     help="profiling aid: time the learned-weight step (float64 state with the "
                          "float operator, or float32 state) instead of the plain one")
@@ -703,6 +707,11 @@ def main() -> None:
         return
     if args.profile_adjoint:
         profile_adjoint(args)
+        return
+    if args.inverse_only:
+        import torch
+
+        print(json.dumps({"inverse_lwr": bench_inverse(torch.device("cuda", 0), args)}), flush=True)
         return
     if world > 1:
         import torch
