@@ -120,10 +120,10 @@ __device__ __forceinline__ void cell_substencils(const float ds[5], float ur[3],
 
 // right- and left-face weights from the exponentials e_k = exp(z_k - max z)
 __device__ __forceinline__ void cell_softmax(float e0, float e1, float e2, float wr[3], float wl[3]) {
-    const float ir = __frcp_rn(e0 + e1 + e2);
+    const float ir = fast_rcp(e0 + e1 + e2);
     wr[0] = e0 * ir; wr[1] = e1 * ir; wr[2] = e2 * ir;
     const float l0 = e2 * (1.0f / 3.0f), l2 = 3.0f * e0;
-    const float il = __frcp_rn(l0 + e1 + l2);
+    const float il = fast_rcp(l0 + e1 + l2);
     wl[0] = l0 * il; wl[1] = e1 * il; wl[2] = l2 * il;
 }
 
