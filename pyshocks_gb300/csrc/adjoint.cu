@@ -176,32 +176,84 @@ __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1
 }
 
 // z_i = dt (J_L(v)^T w)_i for i in [lo, hi); v valid on [lo-6, hi+6), w on
-// [lo-3, hi+3). Rusanov flux, WENO-JS5 reconstruction.
+// [lo-3, hi+3). Rusanov flux, WENO-JS5 or learned reconstruction.
 template <class T, int EQ, int REC>
 __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const AdjSmem<T>& a,
                           const OpParams<T>& p, T dtdx) {
     const int tid = threadIdx.x, nt = blockDim.x;
     if constexpr (REC == SHK_REC_LEARNED) {
-        learned_phase<T>(v, lo - 3, hi + 3, a.UL, a.UR, reinterpret_cast<float*>(a.H), p.lp);
+        static_assert(sizeof(T) == 4, "the learned VJP runs on float stage states");
+        // One pass per cell: the network forward (recomputed with the
+        // inference's own mma sequence) gives the cell's face values, from
+        // which the flux VJP seeds of its two faces follow, then the network
+        // backward. Face j+1/2 (L = ul_{j+1}, R = ur_j) seeds cell j with
+        //   gR_j = fb_j (f'(R)/2 + a_j), and cell j+1 with gL = fb_j (f'(L)/2 - a_j),
+        // fb_j = dt/dx (w_{j+1} - w_j), a_j = nu/2 max(|f'(v_j)|, |f'(v_{j+1})|).
+        // The face values are kept for the wave-speed terms below.
+        float* db = reinterpret_cast<float*>(a.H);
+        for (int c = lo - 4 + tid; c < hi + 2; c += nt) db[c] = v[c + 1] - v[c];
+        MlpFrags f;
+        mlp_load_frags(p.lp.mlp, f);
+        MlpBackFrags bk;
+        mlp_load_back_frags(p.lp.mlp, bk);
         __syncthreads();
-    } else {
-        for (int c = lo - 5 + tid; c < hi + 4; c += nt) a.H[c] = T(0.5) * (v[c + 1] - v[c]);
-        __syncthreads();
-        for (int c = lo - 4 + tid; c < hi + 4; c += nt) {
-            const T d = a.H[c] - a.H[c - 1];
-            a.D[c] = d;
-            a.Q[c] = (T(13.0 / 3.0) * d) * d;
+        const int lane = tid & 31, g = lane >> 2, tq = lane & 3;
+        const int myrow = 16 * (tq >> 1) + 8 * (tq & 1) + g;
+        const int c0 = lo - 2, ncell = hi + 2 - c0;
+        for (int qb = tid >> 5; qb * 32 < ncell; qb += nt >> 5) {
+            const int r = qb * 32 + myrow;
+            const int c = c0 + min(r, ncell - 1);
+            const float dm2 = db[c - 2], dm1 = db[c - 1], d0 = db[c], dp1 = db[c + 1];
+            const float sc[5] = {-(dm1 + dm2), -dm1, 0.0f, d0, d0 + dp1};
+            const float vm = v[c - 1], vc = v[c], vp = v[c + 1];
+            const float wm = w[c - 1], wc = w[c], wp = w[c + 1];
+            float ul = 0.0f, ur = 0.0f;
+            auto seed = [&](float cr, float cl, float& gR, float& gL) {
+                ur = vc + cr;
+                ul = vc + cl;
+                const float wsc = wave_speed<EQ>(vc, p.c);
+                const float hp = p.hnu * absmax(wsc, wave_speed<EQ>(vp, p.c));
+                const float hm = p.hnu * absmax(wave_speed<EQ>(vm, p.c), wsc);
+                gR = ((wp - wc) * dtdx) * fmaf(0.5f, flux_prime<EQ>(ur, p.c), hp);
+                gL = ((wc - wm) * dtdx) * fmaf(0.5f, flux_prime<EQ>(ul, p.c), -hm);
+            };
+            float dd[5];
+            learned_cell_vjp32(f, bk, sc, seed, p.lp, dd);
+            if (r < ncell) {
+                a.T0[c] = dd[0]; a.T1[c] = dd[1]; a.T2[c] = dd[2]; a.T3[c] = dd[3]; a.T4[c] = dd[4];
+                a.UL[c] = ul;
+                a.UR[c] = ur;
+            }
         }
         __syncthreads();
-        for (int c = lo - 3 + tid; c < hi + 3; c += nt) {
-            T ul, ur;
-            weno53_cell<T>(v[c], a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
-                           a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, ul, ur);
-            a.UL[c] = ul;
-            a.UR[c] = ur;
+        for (int i = lo + tid; i < hi; i += nt) {
+            T acc = (a.T0[i + 2] + a.T1[i + 1]) + a.T2[i] + (a.T3[i - 1] + a.T4[i - 2]);
+            // wave-speed terms: face i-1/2 (cells i-1, i) and face i+1/2 (cells i, i+1)
+            const T gam = -(((w[i] - w[i - 1]) * dtdx) * p.hnu) * (a.UL[i] - a.UR[i - 1]);
+            const T gap = -(((w[i + 1] - w[i]) * dtdx) * p.hnu) * (a.UL[i + 1] - a.UR[i]);
+            acc = fma(gam, damax_dx<EQ>(v[i], v[i - 1], p.c), acc);
+            acc = fma(gap, damax_dx<EQ>(v[i], v[i + 1], p.c), acc);
+            z[i] = acc;
         }
         __syncthreads();
+        return;
     }
+    for (int c = lo - 5 + tid; c < hi + 4; c += nt) a.H[c] = T(0.5) * (v[c + 1] - v[c]);
+    __syncthreads();
+    for (int c = lo - 4 + tid; c < hi + 4; c += nt) {
+        const T d = a.H[c] - a.H[c - 1];
+        a.D[c] = d;
+        a.Q[c] = (T(13.0 / 3.0) * d) * d;
+    }
+    __syncthreads();
+    for (int c = lo - 3 + tid; c < hi + 3; c += nt) {
+        T ul, ur;
+        weno53_cell<T>(v[c], a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
+                       a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, ul, ur);
+        a.UL[c] = ul;
+        a.UR[c] = ur;
+    }
+    __syncthreads();
     // face j+1/2: F = 1/2 (f(L) + f(R)) - nu/2 a (L - R), L = ul_{j+1}, R = ur_j
     for (int j = lo - 3 + tid; j < hi + 2; j += nt) {
         const T fb = (w[j + 1] - w[j]) * dtdx;
@@ -212,38 +264,12 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
         a.GA[j] = -(fb * p.hnu) * (L - R);
     }
     __syncthreads();
-    if constexpr (REC == SHK_REC_LEARNED) {
-        // one cell per lane, 32 cells per warp iteration (tensor-core network
-        // backward); the cell's stencil relative to v_c from the float cell
-        // differences, as the forward (learned_phase left them in H)
-        const float* db = reinterpret_cast<const float*>(a.H);
-        MlpFrags f;
-        mlp_load_frags(p.lp.mlp, f);
-        MlpBackFrags bk;
-        mlp_load_back_frags(p.lp.mlp, bk);
-        const int lane = tid & 31, g = lane >> 2, tq = lane & 3;
-        const int myrow = 16 * (tq >> 1) + 8 * (tq & 1) + g;
-        const int c0 = lo - 2, ncell = hi + 2 - c0;
-        for (int qb = tid >> 5; qb * 32 < ncell; qb += nt >> 5) {
-            const int r = qb * 32 + myrow;
-            const int c = c0 + min(r, ncell - 1);
-            const float dm2 = db[c - 2], dm1 = db[c - 1], d0 = db[c], dp1 = db[c + 1];
-            const float sc[5] = {-(dm1 + dm2), -dm1, 0.0f, d0, d0 + dp1};
-            float dd[5];
-            learned_cell_vjp32(f, bk, sc, static_cast<float>(a.GR[c]), static_cast<float>(a.GL[c - 1]),
-                               p.lp, dd);
-            if (r < ncell) {
-                a.T0[c] = dd[0]; a.T1[c] = dd[1]; a.T2[c] = dd[2]; a.T3[c] = dd[3]; a.T4[c] = dd[4];
-            }
-        }
-    } else {
-        for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
-            T t0, t1, t2, t3, t4;
-            weno53_cell_vjp<T>(a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
-                               a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, a.GR[c],
-                               a.GL[c - 1], t0, t1, t2, t3, t4);
-            a.T0[c] = t0; a.T1[c] = t1; a.T2[c] = t2; a.T3[c] = t3; a.T4[c] = t4;
-        }
+    for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
+        T t0, t1, t2, t3, t4;
+        weno53_cell_vjp<T>(a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
+                           a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, a.GR[c],
+                           a.GL[c - 1], t0, t1, t2, t3, t4);
+        a.T0[c] = t0; a.T1[c] = t1; a.T2[c] = t2; a.T3[c] = t3; a.T4[c] = t4;
     }
     __syncthreads();
     for (int i = lo + tid; i < hi; i += nt) {

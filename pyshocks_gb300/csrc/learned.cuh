@@ -423,10 +423,14 @@ __device__ __forceinline__ void mlp_tile_back(const MlpBackFrags& b, uint32_t d0
 // gR d(u_R)/ds + gL d(u_L)/ds of this lane's cell (right and left face values)
 // with respect to its stencil s = v_{c-2..c+2}, given shifted by the cell
 // value as the forward evaluates it (ds[2] = 0; the gradient of a
-// shift-equivariant value does not depend on the shift). All 32 lanes must
-// call it (shuffles, mma) with finite stencils; returns dsum[5].
+// shift-equivariant value does not depend on the shift). The cotangents come
+// from seed(cr, cl, gR, gL), called once the forward has produced the face
+// corrections cr = u_R - v_c and cl = u_L - v_c (the seeds of a flux VJP
+// depend on the face values). All 32 lanes must call it (shuffles, mma) with
+// finite stencils; returns dsum[5].
+template <class Seed>
 __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpBackFrags& bk,
-                                                   const float s[5], float gR, float gL,
+                                                   const float s[5], Seed&& seed,
                                                    const LearnedParams& lp, float dsum[5]) {
     const int lane = threadIdx.x & 31, t = lane & 3, base = lane & ~3;
     // ---- forward (as learned_cell32), keeping the activations
@@ -470,6 +474,10 @@ __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpB
     const bool fbr = outside_band(wr, jr, lp), fbl = outside_band(wl, jl, lp);
     const float* tr = fbr ? jr : wr;
     const float* tl = fbl ? jl : wl;
+    const float uR = tr[0] * hr[0] + tr[1] * hr[1] + tr[2] * hr[2];
+    const float uL = tl[0] * hl[0] + tl[1] * hl[1] + tl[2] * hl[2];
+    float gR, gL;
+    seed(uR, uL, gR, gL);
     // direct parts: sum_k omega_k d uhat_k / ds; 6 uhat taps, right face
     // (2,-7,11,0,0) (0,-1,5,2,0) (0,0,2,5,-1), left face mirrored
     const float cR = gR * (1.0f / 6.0f), cL = gL * (1.0f / 6.0f);
@@ -482,8 +490,6 @@ __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpB
     if (fbr || fbl) {
         // WENO-JS faces: d u / d beta_l = -2 omega_l (uhat_l - u) / (eps + beta_l);
         // the left face's sub-stencil k sees beta_{2-k}
-        const float uR = tr[0] * hr[0] + tr[1] * hr[1] + tr[2] * hr[2];
-        const float uL = tl[0] * hl[0] + tl[1] * hl[1] + tl[2] * hl[2];
         float bb[3] = {0.0f, 0.0f, 0.0f};
         if (fbr)
             for (int l = 0; l < 3; ++l) bb[l] += -2.0f * gR * jr[l] * (hr[l] - uR) / (lp.eps + be[l]);
