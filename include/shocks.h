@@ -211,6 +211,38 @@ int shk_plan_copy_dt_history(shk_plan* plan, double* out, void* stream);
 /* copy the device status word to *h_status (synchronises `stream`). */
 int shk_plan_status(shk_plan* plan, int32_t* h_status, void* stream);
 
+/* ---- host-resident batches ---------------------------------------------- */
+
+/* A batch whose state lives in host memory, as the reference's arrays do (the
+ * step() loop of timestepping.py:89-152 runs on numpy / JAX CPU arrays). The
+ * stepper splits the batch by instance into `nchunks` chunks of about equal
+ * cell counts (0: one per 512 Ki cells, at most 32; never more than one per
+ * instance), each with its own plan and device buffers, and
+ * pipelines them: host-to-device copy of chunk c+1 and device-to-host copy of
+ * chunk c-1 overlap the steps of chunk c. Arguments as shk_plan_create
+ * (opts->max_steps must be 0: forward only). */
+typedef struct shk_host_stepper shk_host_stepper;
+
+int shk_host_stepper_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_offsets,
+                            const double* h_dx, const double* h_cfl, double theta,
+                            const shk_plan_opts* opts, int32_t nchunks, shk_host_stepper** out);
+int shk_host_stepper_destroy(shk_host_stepper* hs);
+/* number of chunks actually used (at most the number of instances) */
+int shk_host_stepper_num_chunks(const shk_host_stepper* hs);
+
+/* h_out = the packed host state h_in (plan layout, double or float as the
+ * opts' dtype) advanced by `nsteps` SSPRK33 CFL steps from t = 0 with no final
+ * time: the same kernels, dt and result, bit for bit, as shk_plan_reset +
+ * shk_plan_step over the whole batch. h_in may equal h_out. Asynchronous with
+ * respect to the host: the results are in h_out once `stream` has reached
+ * the point of the call. Overlap needs pinned host buffers (cudaHostAlloc or
+ * cudaHostRegister). */
+int shk_host_stepper_advance(shk_host_stepper* hs, const void* h_in, void* h_out, int32_t nsteps,
+                             void* stream);
+
+/* OR of the chunks' status words (synchronises `stream`) */
+int shk_host_stepper_status(shk_host_stepper* hs, int32_t* h_status, void* stream);
+
 /* ---- discrete adjoint (dt frozen, as adjoint_step: timestepping.py:155-215) -- */
 
 /* p_out = (d advance(u) / d u)^T p_next for one SSPRK33 step of a ghosted single

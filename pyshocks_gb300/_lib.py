@@ -110,6 +110,14 @@ SIGNATURES: dict[str, tuple] = {
     "shk_plan_copy_dt_history": (ctypes.c_int, [_P, _P, _P]),
     "shk_plan_status": (ctypes.c_int, [_P, ctypes.POINTER(_I32), _P]),
     "shk_plan_reduce": (ctypes.c_int, [_P, _P, _I32, _P, _P]),
+    "shk_host_stepper_create": (
+        ctypes.c_int,
+        [_SCH, _I32, _P, _P, _P, _D, ctypes.POINTER(ShkPlanOpts), _I32, ctypes.POINTER(_P)],
+    ),
+    "shk_host_stepper_destroy": (ctypes.c_int, [_P]),
+    "shk_host_stepper_num_chunks": (ctypes.c_int, [_P]),
+    "shk_host_stepper_advance": (ctypes.c_int, [_P, _P, _P, _I32, _P]),
+    "shk_host_stepper_status": (ctypes.c_int, [_P, ctypes.POINTER(_I32), _P]),
     "shk_ssprk33_vjp_f64": (ctypes.c_int, [_SCH, _P, _P, _P, _I64, _I32, _D, _D, _P]),
     "shk_ssprk33_vjp_bc_f64": (ctypes.c_int, [_SCH, ctypes.POINTER(ShkBoundary), _P, _P, _P, _I64,
                                               _I32, _D, _D, _P]),

@@ -46,6 +46,75 @@ def pack_offsets(sizes: Sequence[int]) -> np.ndarray:
     return off
 
 
+class HostStepper:
+    """A batch whose state lives in host memory (``shk_host_stepper``).
+
+    :meth:`advance` copies the packed host state in, takes ``nsteps`` CFL
+    steps from t = 0 and copies the result out, with the batch split by
+    instance into *chunks* pipelined over copy and compute streams: the copies
+    of one chunk overlap the steps of the others. The result is bit-identical
+    to a :class:`BatchedSolver` over the whole batch. Host tensors should be
+    pinned (``pin_memory()``) for the copies to overlap.
+    """
+
+    def __init__(self, scheme, sizes: Sequence[int], dx: float | Sequence[float], *,
+                 theta: float = 1.0, dtype: torch.dtype = torch.float64, tile: int = 0,
+                 ctas_per_sm: int = 0, chunks: int = 0):
+        if dtype not in _DTYPES:
+            raise TypeError(f"unsupported dtype {dtype}")
+        self.lib = L.lib()
+        self.sizes = np.asarray(sizes, dtype=np.int64)
+        self.B = int(self.sizes.size)
+        self.offsets = pack_offsets(self.sizes)
+        self.total = int(self.offsets[-1])
+        self.dtype = dtype
+        dxs = np.broadcast_to(np.asarray(dx, dtype=np.float64), (self.B,)).copy()
+        self.cfl = np.array([scheme.cfl_constant(float(h)) for h in dxs], dtype=np.float64)
+        cs = scheme.c_scheme(float(dxs[0]))
+        opts = L.ShkPlanOpts(dtype=_DTYPES[dtype], tile=int(tile), max_steps=0,
+                             ctas_per_sm=int(ctas_per_sm))
+        hs = ctypes.c_void_p()
+        L.check(self.lib.shk_host_stepper_create(cs, self.B, self.offsets.ctypes.data,
+                                                 dxs.ctypes.data, self.cfl.ctypes.data,
+                                                 float(theta), ctypes.byref(opts), int(chunks),
+                                                 ctypes.byref(hs)), "host_stepper_create")
+        self._hs = hs
+        self.chunks = int(self.lib.shk_host_stepper_num_chunks(hs))
+
+    def __del__(self):
+        hs = getattr(self, "_hs", None)
+        if hs is not None and hs.value:
+            try:
+                torch.cuda.synchronize()
+                self.lib.shk_host_stepper_destroy(hs)
+            except Exception:
+                pass
+            self._hs = None
+
+    def advance(self, u_in: torch.Tensor, u_out: torch.Tensor | None = None,
+                nsteps: int = 1) -> torch.Tensor:
+        """``u_out`` = ``u_in`` advanced by *nsteps* steps (CPU tensors of the
+        stepper's dtype, packed layout; ``u_out`` may be ``u_in``). The call
+        does not block: ``u_out`` holds the result once the current stream has
+        passed it (``torch.cuda.current_stream().synchronize()``)."""
+        for t in (u_in,) if u_out is None else (u_in, u_out):
+            if t.device.type != "cpu" or t.dtype != self.dtype or not t.is_contiguous() \
+                    or t.numel() != self.total:
+                raise ValueError("host state must be a contiguous CPU tensor of the "
+                                 "stepper's dtype and packed size")
+        if u_out is None:
+            u_out = torch.empty(u_in.shape, dtype=self.dtype, pin_memory=u_in.is_pinned())
+        L.check(self.lib.shk_host_stepper_advance(self._hs, u_in.data_ptr(), u_out.data_ptr(),
+                                                  int(nsteps), L.stream_handle()),
+                "host_stepper_advance")
+        return u_out
+
+    def status(self) -> int:
+        st = ctypes.c_int32()
+        L.check(self.lib.shk_host_stepper_status(self._hs, ctypes.byref(st), L.stream_handle()))
+        return int(st.value)
+
+
 class BatchedSolver:
     """Persistent batched SSPRK33 solver for one scheme on periodic domains.
 

@@ -126,6 +126,11 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
     }
 }
 
+__global__ void fill_kernel(double* x, int n, double v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = v;
+}
+
 // max |f'(u)| per instance into amax[cur] (plan reset / priming)
 template <class T, int EQ>
 __global__ void __launch_bounds__(kThreads) batched_max_kernel(PlanDev P, const T* __restrict__ u, T c,
@@ -858,10 +863,9 @@ int shk_plan_reset(shk_plan* plan, const void* u, const double* t0, const double
     else SHK_CUDA(cudaMemsetAsync(plan->t, 0, sizeof(double) * B, st));
     if (tfinal) {
         SHK_CUDA(cudaMemcpyAsync(plan->tfinal, tfinal, sizeof(double) * B, cudaMemcpyDeviceToDevice, st));
-    } else {
-        std::vector<double> inf(B, DBL_MAX);
-        SHK_CUDA(cudaMemcpyAsync(plan->tfinal, inf.data(), sizeof(double) * B, cudaMemcpyHostToDevice, st));
-        SHK_CUDA(cudaStreamSynchronize(st));
+    } else {  // no final time; a kernel, so that a reset never waits on the host
+        fill_kernel<<<(B + kThreads - 1) / kThreads, kThreads, 0, st>>>(plan->tfinal, B, DBL_MAX);
+        SHK_CUDA(cudaGetLastError());
     }
     if (plan->dt_hist)
         SHK_CUDA(cudaMemsetAsync(plan->dt_hist, 0, sizeof(double) * size_t(plan->max_steps) * B, st));

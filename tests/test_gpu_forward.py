@@ -226,6 +226,37 @@ def test_batched_graph_equals_stream(gb):
     assert torch.equal(s1.time(), s2.time())
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("chunks", [1, 3, 16])
+def test_host_stepper_equals_device_plan(gb, dtype, chunks):
+    """The pipelined host-buffer stepper gives the device plan's result bit for
+    bit (every instance is independent), in place or not, over repeated calls."""
+    from pyshocks_gb300.batched import BatchedSolver, HostStepper
+
+    sizes = [1024, 2048, 512, 4096, 96, 3000, 1536]
+    rng = np.random.default_rng(13)
+    u0 = np.concatenate([R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes])
+    scheme = _scheme(gb, "rusanov")
+    dx = [2.0 / n for n in sizes]
+    ref = BatchedSolver(scheme, sizes, dx, theta=0.9, dtype=dtype)
+    ref.reset(torch.tensor(u0, device="cuda"))
+    ref.step(3)
+    hs = HostStepper(scheme, sizes, dx, theta=0.9, dtype=dtype, chunks=chunks)
+    # chunks of about equal cell counts: at most one per instance
+    assert 1 <= hs.chunks <= min(chunks, len(sizes))
+    host = torch.tensor(u0).to(dtype).pin_memory()
+    out = hs.advance(host, nsteps=3)
+    torch.cuda.current_stream().synchronize()
+    assert torch.equal(out, ref.u.cpu())
+    # in place, twice: 2 x (3 steps from t = 0) equals 6 steps (no final time)
+    hs.advance(host, host, nsteps=3)
+    hs.advance(host, host, nsteps=3)
+    ref.step(3)
+    torch.cuda.current_stream().synchronize()
+    assert torch.equal(host, ref.u.cpu())
+    assert hs.status() == 0
+
+
 def test_batched_float32_error_and_conservation(gb):
     """FP32 state: error against the FP64 oracle reported/bounded; the FP64
     conserved-mass sums drift only by rounding."""
