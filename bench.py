@@ -248,7 +248,8 @@ def bench_reference(args, rank: int) -> None:
 
 
 def _config(args) -> dict:
-    what = {"plain": "plain WENO-JS5", "learned": "learned-weight WENO (float64 state)",
+    what = {"plain": "plain WENO-JS5", "plain32": "plain WENO-JS5 (float32 state)",
+            "learned": "learned-weight WENO (float64 state)",
             "learned32": "learned-weight WENO (float32 state)"}[getattr(args, "scheme", "plain")]
     return {
         "workload": f"batched {what}+Rusanov+SSPRK33 Burgers, B={args.batch}, "
@@ -280,7 +281,7 @@ def bench_gpu(args, rank: int, world: int) -> None:
     rec = gb.reconstruction.make_reconstruction_from_name("wenojs53", eps=EPS)
     scheme = gb.burgers.make_scheme_from_name("rusanov", rec=rec)
     u0 = initial_state(sizes, params, dev)
-    if args.scheme != "plain":
+    if args.scheme.startswith("learned"):
         # profiling aid: the learned-weight step on the same batch (float64
         # state with the float operator, or float32 state)
         from pyshocks_gb300 import learned
@@ -291,6 +292,7 @@ def bench_gpu(args, rank: int, world: int) -> None:
                                tile=args.tile)
     else:
         solver = BatchedSolver(scheme, sizes, 2.0 / sizes.astype(np.float64), theta=THETA,
+                               dtype=torch.float32 if args.scheme == "plain32" else torch.float64,
                                tile=args.tile)
     stream = torch.cuda.Stream(device=dev)
     dist = None
@@ -375,6 +377,8 @@ def bench_gpu(args, rank: int, world: int) -> None:
     if hbm_peak is None:
         hbm_peak, peak_src = 6800.0, "profiling-recipe fallback 6.8 TB/s (of fallback)"
     algo_bytes = BYTES_PER_CELL_STEP_F64 * cells
+    if solver.dtype == torch.float32:  # profiling aid: float32 state, 8 B per cell-step
+        algo_bytes //= 2
     achieved = algo_bytes / per_launch_s / 1e9
     traffic = None
     if "dram_bytes_per_cell_step" in consts:
@@ -425,8 +429,9 @@ def bench_gpu(args, rank: int, world: int) -> None:
             "gpu_launches": k,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
-                         "kernel": ("batched_step_kernel<double,Burgers,WENOJS53,Rusanov>"
-                                    if args.scheme == "plain" else
+                         "kernel": (f"batched_step_kernel<{'float' if args.scheme == 'plain32' else 'double'},"
+                                    "Burgers,WENOJS53,Rusanov>"
+                                    if args.scheme.startswith("plain") else
                                     f"batched_step_kernel<{'float' if args.scheme == 'learned32' else 'double'},"
                                     "Burgers,LEARNED,Rusanov>"),
                          "algo_bytes_per_launch": algo_bytes, "peak_source": peak_src},
@@ -466,9 +471,9 @@ def bench_fp32(scheme, sizes, u0, stream, args) -> dict:
     dx = 2.0 / sizes.astype(np.float64)
     k = args.steps + (args.steps % 2)
     s32 = BatchedSolver(scheme, sizes, dx, dtype=torch.float32)
-    ms = _timed_steps(s32, u0, k, stream)
+    ms = _timed_steps(s32, u0, k, stream)  # ms per step
     cells = int(np.sum(sizes))
-    rate = cells * k / (ms * 1e-3)
+    rate = cells / (ms * 1e-3)
     # error and drift after 4 + k steps from u0 (the timed run's state)
     s64 = BatchedSolver(scheme, sizes, dx)
     with torch.cuda.stream(stream):
@@ -651,11 +656,11 @@ def profile_adjoint(args) -> None:
     from pyshocks_gb300 import learned
 
     dev = torch.device("cuda", 0)
-    if args.scheme == "plain":
+    if args.scheme.startswith("plain"):
         sch = gb.burgers.Rusanov(rec=gb.reconstruction.make_reconstruction_from_name("wenojs53", eps=EPS))
     else:
         sch = gb.burgers.Rusanov(rec=learned.LearnedWENO(params=learned.load_default_params(device=dev)))
-    dtype = torch.float32 if args.scheme == "learned32" else torch.float64
+    dtype = torch.float32 if args.scheme.endswith("32") else torch.float64
     r = _adjoint_rate(sch, dev, args.adjoint_steps, dtype, B=args.batch)
     print(json.dumps({"profile_adjoint": args.scheme, **r}), flush=True)
 
@@ -687,9 +692,10 @@ def main() -> None:
                     help="timed gradient-descent iterations of the inverse-problem leg (full: 50)")
     ap.add_argument("--inverse-only", action="store_true",
                     help="run only the inverse-problem leg (one JSON line)")
-    ap.add_argument("--scheme", choices=["plain", "learned", "learned32"], default="plain",
-                    help="profiling aid: time the learned-weight step (float64 state with the "
-                         "float operator, or float32 state) instead of the plain one")
+    ap.add_argument("--scheme", choices=["plain", "plain32", "learned", "learned32"], default="plain",
+                    help="profiling aid: time the plain step with float32 state, or the "
+                         "learned-weight step (float64 state with the float operator, or "
+                         "float32 state), instead of the plain float64 one")
     ap.add_argument("--tile", default="auto",
                     help="cells per work item of the batched plans, or 'auto' (autotuner: tile "
                          "and CTAs/SM timed on the batch); 0 = library default")

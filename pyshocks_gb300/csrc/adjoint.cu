@@ -108,8 +108,8 @@ __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1
     T P0, P1, P2;
     if constexpr (sizeof(T) == 8) {
         P0 = s1 * s2; P1 = s0 * s2; P2 = s0 * s1;
-    } else {
-        P0 = T(1) / s0; P1 = T(1) / s1; P2 = T(1) / s2;
+    } else {  // the forward's approximate reciprocals
+        P0 = rcp_approx_f32(s0); P1 = rcp_approx_f32(s1); P2 = rcp_approx_f32(s2);
     }
     const T cr0 = fma(T(10), Hm1, T(-4) * Hm2);
     const T cr1 = fma(T(24), H0, T(12) * Hm1);
@@ -136,14 +136,14 @@ __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1
         ie1 = (e0 * e2) * q;
         ie2 = e01 * q;
     } else {
-        const T ird = T(1) / dr, ild = T(1) / dl;
+        const T ird = rcp_approx_f32(dr), ild = rcp_approx_f32(dl);
         gR = urb * ird;
         gL = ulb * ild;
         dR = nr * ird;
         dL = nl * ild;
-        ie0 = T(1) / e0;
-        ie1 = T(1) / e1;
-        ie2 = T(1) / e2;
+        ie0 = rcp_approx_f32(e0);
+        ie1 = rcp_approx_f32(e1);
+        ie2 = rcp_approx_f32(e2);
     }
     // interpolation part (weights held fixed): d_k P_k / D folded with the
     // sub-stencil values 6 uhat_k

@@ -59,6 +59,14 @@ template <class T> struct Bits;
 template <> struct Bits<double> { using type = unsigned long long; };
 template <> struct Bits<float> { using type = unsigned int; };
 
+// 1/x to about 1 ulp in one instruction (rcp.approx.ftz.f32; subnormal inputs
+// flush to zero) for float paths where a correctly rounded division buys nothing
+__device__ __forceinline__ float rcp_approx_f32(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // max(|a|, |b|) without the FP pipe (NaN-free inputs)
 template <class T>
 __device__ __forceinline__ T absmax(T a, T b) {
@@ -121,12 +129,14 @@ __device__ __forceinline__ void weno53_cell(T v, T Hm2, T Hm1, T H0, T Hp1, T Dm
     T s2 = eps + b2; s2 = s2 * s2;
     // alpha_k = d_k / s_k (weno.py:254). f64: product form P_k = prod_{j!=k} s_j
     // (proportional to 1/s_k, no reciprocal); f32: P_k = 1/s_k, which cannot
-    // underflow when eps^4 is below the float range.
+    // underflow when eps^4 is below the float range. The float reciprocals are
+    // the one-instruction approximate ones (about 1 ulp): the float state
+    // itself carries 2^-24 relative rounding per stage.
     T P0, P1, P2;
     if constexpr (sizeof(T) == 8) {
         P0 = s1 * s2; P1 = s0 * s2; P2 = s0 * s1;
     } else {
-        P0 = T(1) / s0; P1 = T(1) / s1; P2 = T(1) / s2;
+        P0 = rcp_approx_f32(s0); P1 = rcp_approx_f32(s1); P2 = rcp_approx_f32(s2);
     }
     // 6 (uhat_k - v) of the right side (weno.py:231-239), d_k folded (1, 6, 3):
     //   uhat_0: -2 d_{c-2} + 5 d_{c-1}       -> -4 H_{c-2} + 10 H_{c-1}
@@ -149,8 +159,8 @@ __device__ __forceinline__ void weno53_cell(T v, T Hm2, T Hm1, T H0, T Hp1, T Dm
         ur = fma(nr * dl, r, v);
         ul = fma(nl * dr, r, v);
     } else {
-        ur = v + nr / dr;
-        ul = v + nl / dl;
+        ur = fma(nr, rcp_approx_f32(dr), v);
+        ul = fma(nl, rcp_approx_f32(dl), v);
     }
 }
 

@@ -51,12 +51,14 @@ __device__ void finalize_step(const PlanDev& P, int64_t k) {
 }
 
 template <class T, int EQ, int REC, int FLUX>
-__global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC == SHK_REC_WENOJS53 && sizeof(T) == 8 ? 3 : 1)) batched_step_kernel(PlanDev P, const T* __restrict__ uin,
+__global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC == SHK_REC_WENOJS53 ? (sizeof(T) == 8 ? 3 : 4) : 1)) batched_step_kernel(PlanDev P, const T* __restrict__ uin,
                                                                 T* __restrict__ uout, OpParams<T> p) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ unsigned long long red[32];
     __shared__ int is_last;
+    __shared__ DtState item_dt;  // the item's step, computed once per CTA
+    __shared__ double item_dx;
     constexpr int HL = step_halo<T>();
     using B = typename Bits<T>::type;
 
@@ -78,7 +80,15 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
         const int64_t n = P.offsets[b + 1] - off;
         const int64_t s0 = int64_t(P.item_tile[item]) * P.tile;
         const int te = static_cast<int>(imin64(P.tile, n - s0));
-        const DtState ds = plan_dt(P, k, b, from_bits(P.amax[size_t(cur) * P.B + b]));
+        // one thread evaluates the step (double divisions: a 1/64-rate pipe on
+        // this GPU) and shares it; the previous item's readers are past the
+        // barrier that ended that item
+        if (threadIdx.x == 0) {
+            item_dt = plan_dt(P, k, b, from_bits(P.amax[size_t(cur) * P.B + b]));
+            item_dx = 1.0 / P.inv_dx[b];
+        }
+        __syncthreads();
+        const DtState ds = item_dt;
         B mx = 0;
         if (!(ds.active && ds.finite)) {
             // instance finished or frozen: copy the tile through
@@ -96,7 +106,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
             }
             const T dtdx = static_cast<T>(ds.dt * P.inv_dx[b]);
             OpParams<T> pb = p;
-            pb.dx = static_cast<T>(1.0 / P.inv_dx[b]);
+            pb.dx = static_cast<T>(item_dx);
             mx = step_tile<T, EQ, REC, FLUX>(sm, uout + off + s0, te, dtdx, pb, plan_bc(P, b),
                                              s0 - HL, n);
         }
