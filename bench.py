@@ -470,7 +470,7 @@ def bench_fp32(scheme, sizes, u0, stream, args) -> dict:
 
     dx = 2.0 / sizes.astype(np.float64)
     k = args.steps + (args.steps % 2)
-    s32 = BatchedSolver(scheme, sizes, dx, dtype=torch.float32)
+    s32 = BatchedSolver(scheme, sizes, dx, dtype=torch.float32, tile=args.tile)
     ms = _timed_steps(s32, u0, k, stream)  # ms per step
     cells = int(np.sum(sizes))
     rate = cells / (ms * 1e-3)
@@ -490,6 +490,7 @@ def bench_fp32(scheme, sizes, u0, stream, args) -> dict:
         stream.synchronize()
     return {"metric": "WENO5 cell-steps/s (float32 state)", "value": rate, "unit": "cell-steps/s",
             "ms_per_step": ms, "algo_gb_per_s": 8 * rate / 1e9,
+            "launch_shape": {"tile": s32.tile, "ctas_per_sm": s32.ctas_per_sm},
             "vs_float64_after_steps": 4 + k,
             "l1_mean": float(l1.mean()), "linf": float(diff.max()),
             "mass_drift_per_cell_max": {"float64": float(drift64), "float32": float(drift32)}}

@@ -61,13 +61,13 @@ def shape_key(scheme, sizes: Sequence[int], dtype: torch.dtype, device) -> str:
                        str(dtype), int(sizes.size), hist], sort_keys=True)
 
 
-def _smem_bytes(tile: int, dtype: torch.dtype, learned: bool = False) -> int:
+def _smem_bytes(tile: int, dtype: torch.dtype, learned: bool = False, weno5: bool = False) -> int:
     # the step tile's shared memory: 7 double arrays of the window (halo 10),
     # or for the learned reconstruction the double window plus 7 float arrays;
-    # 8 float arrays for float32 states (halo 12)
+    # for float32 states (halo 12) 6 float arrays with WENO-JS5, else 8
     if dtype == torch.float64:
         return (tile + 20) * (8 + 7 * 4 if learned else 7 * 8)
-    return 8 * (tile + 24) * 4
+    return (6 if weno5 else 8) * (tile + 24) * 4
 
 
 def _adjoint_smem_bytes(tile: int, dtype: torch.dtype, learned: bool = False) -> int:
@@ -80,7 +80,7 @@ def _adjoint_smem_bytes(tile: int, dtype: torch.dtype, learned: bool = False) ->
 
 
 def candidates(dtype: torch.dtype, max_cells: int, learned: bool = False,
-               adjoint: bool = False) -> list[tuple[int, int]]:
+               adjoint: bool = False, weno5: bool = False) -> list[tuple[int, int]]:
     """(tile, ctas_per_sm) pairs whose shared memory fits one SM; tiles longer
     than twice the largest instance are skipped (they only add idle lanes);
     with ``adjoint`` only tiles whose reverse step fits too."""
@@ -90,7 +90,7 @@ def candidates(dtype: torch.dtype, max_cells: int, learned: bool = False,
             continue
         if adjoint and _adjoint_smem_bytes(tile, dtype, learned) > SMEM_PER_SM:
             continue
-        per = _smem_bytes(tile, dtype, learned)
+        per = _smem_bytes(tile, dtype, learned, weno5)
         if per > SMEM_PER_SM:
             continue
         for c in CTAS_PER_SM:
@@ -153,7 +153,8 @@ def tune(scheme, sizes: Sequence[int], dx, *, dtype: torch.dtype = torch.float64
     table = []
     k = 2 * max(1, steps // 2)
     learned = type(getattr(scheme, "rec", None)).__name__ == "LearnedWENO"
-    for tile, cps in candidates(dtype, int(sizes.max()), learned, adjoint):
+    weno5 = type(getattr(scheme, "rec", None)).__name__ == "WENOJS53"
+    for tile, cps in candidates(dtype, int(sizes.max()), learned, adjoint, weno5):
         solver = BatchedSolver(scheme, sizes, dx, theta=theta, dtype=dtype, tile=tile,
                                ctas_per_sm=cps, device=device)
         with torch.cuda.stream(stream):

@@ -50,7 +50,16 @@ struct Smem {
     // mixed precision (step_tile_mixed) on the double window and 7 float arrays
     __host__ static size_t step_bytes(int W, int rec) {
         if (sizeof(T) == 8 && rec == SHK_REC_LEARNED) return size_t(W) * (sizeof(double) + 7 * sizeof(float));
+        if (sizeof(T) == 4 && rec == SHK_REC_WENOJS53) return size_t(6) * W * sizeof(T);
         return host_bytes(W);
+    }
+    // float state with WENO-JS5: the reconstruction works from the window
+    // values directly, so H and Q are not needed (6 arrays)
+    __device__ void carve_compact(unsigned char* base, int W) {
+        T* p = reinterpret_cast<T*>(base);
+        U = p; S = p + W; D = p + 2 * W; UL = p + 3 * W; UR = p + 4 * W; I = p + 5 * W;
+        H = Q = nullptr;
+        this->W = W;
     }
     // compact layout of that mixed step: U (double window), then as float
     // arrays S (2W: uf, k), H (2W: cell differences, increments), D, UL, UR;
@@ -92,6 +101,7 @@ struct OpParams {
 template <class T, int REC>
 __device__ __forceinline__ void carve_step(Smem<T>& sm, unsigned char* base, int W) {
     if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED) sm.carve_mixed(base, W);
+    else if constexpr (sizeof(T) == 4 && REC == SHK_REC_WENOJS53) sm.carve_compact(base, W);
     else sm.carve(base, W);
 }
 
@@ -254,24 +264,19 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
             sm.UR[c] = ur;
         }
         __syncthreads();
-    } else if constexpr (REC == SHK_REC_WENOJS53) {
-        // phase A: H_c = (v_{c+1} - v_c)/2, c in [lo-3, hi+2)
-        for (int c = lo - 3 + tid; c < hi + 2; c += nt) sm.H[c] = T(0.5) * (v[c + 1] - v[c]);
-        __syncthreads();
-        // phase B: D_c = H_c - H_{c-1}, Q_c = 13/12 (2 D_c)^2, c in [lo-2, hi+2)
-        for (int c = lo - 2 + tid; c < hi + 2; c += nt) {
-            const T d = sm.H[c] - sm.H[c - 1];
-            sm.D[c] = d;
-            sm.Q[c] = (T(13.0 / 3.0) * d) * d;
-        }
-        __syncthreads();
-        // phase C: ul, ur of cells [lo-1, hi+1)
+    } else if constexpr (REC == SHK_REC_WENOJS53 && sizeof(T) == 4) {
+        // float: each cell's differences straight from its five values (a few
+        // more float operations, two fewer barriers and about half the
+        // shared-memory traffic of the staged phases below)
 #pragma unroll 2
         for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
+            const T vm2 = v[c - 2], vm1 = v[c - 1], v0 = v[c], vp1 = v[c + 1], vp2 = v[c + 2];
+            const T hm2 = T(0.5) * (vm1 - vm2), hm1 = T(0.5) * (v0 - vm1);
+            const T h0 = T(0.5) * (vp1 - v0), hp1 = T(0.5) * (vp2 - vp1);
+            const T dm1 = hm1 - hm2, d0 = h0 - hm1, dp1 = hp1 - h0;
             T ul, ur;
-            weno53_cell<T>(v[c], sm.H[c - 2], sm.H[c - 1], sm.H[c], sm.H[c + 1], sm.D[c - 1],
-                           sm.D[c], sm.D[c + 1], sm.Q[c - 1], sm.Q[c], sm.Q[c + 1], p.eps, ul,
-                           ur);
+            weno53_cell<T>(v0, hm2, hm1, h0, hp1, dm1, d0, dp1, (T(13.0 / 3.0) * dm1) * dm1,
+                           (T(13.0 / 3.0) * d0) * d0, (T(13.0 / 3.0) * dp1) * dp1, p.eps, ul, ur);
             sm.UL[c] = ul;
             sm.UR[c] = ur;
         }
@@ -354,34 +359,44 @@ template <class T>
 __device__ bool load_window(T* dst, const T* base, int64_t n, int64_t g0, int W,
                             uint64_t* bar, uint32_t& phase) {
     const size_t sz = sizeof(T);
-    bool bulk = (reinterpret_cast<uintptr_t>(base) % 16 == 0) &&
-                (reinterpret_cast<uintptr_t>(dst) % 16 == 0);
-    {
+    // a window no longer than its instance wraps at most once: one compare
+    // instead of a 64-bit remainder per position
+    const bool once = g0 >= -n && g0 + W <= 2 * n;
+    auto wrap = [&](int64_t pos) -> int64_t {
+        if (once) return pos < 0 ? pos + n : (pos >= n ? pos - n : pos);
+        return imod(pos, n);
+    };
+    // order earlier generic-proxy accesses of dst before the async-proxy writes
+    fence_proxy_async();
+    // thread 0 decides between bulk copies and plain loads; the barrier that
+    // broadcasts the decision also orders the fences before the copies
+    bool bulk = false;
+    if (threadIdx.x == 0) {
+        bulk = (reinterpret_cast<uintptr_t>(base) % 16 == 0) &&
+               (reinterpret_cast<uintptr_t>(dst) % 16 == 0);
         int64_t pos = g0;
         const int64_t end = g0 + W;
         int npieces = 0;
         while (pos < end && bulk) {
-            const int64_t src = imod(pos, n);
+            const int64_t src = wrap(pos);
             const int64_t len = min(end - pos, n - src);
             if ((src * sz) % 16 || (len * sz) % 16 || ((pos - g0) * sz) % 16) bulk = false;
             pos += len;
             if (++npieces > 8) bulk = false;  // tiny instances: plain loads
         }
     }
+    bulk = __syncthreads_or(bulk);
     if (!bulk) {
-        for (int w = threadIdx.x; w < W; w += blockDim.x) dst[w] = base[imod(g0 + w, n)];
+        for (int w = threadIdx.x; w < W; w += blockDim.x) dst[w] = base[wrap(g0 + w)];
         __syncthreads();
         return true;
     }
-    // order earlier generic-proxy accesses of dst before the async-proxy writes
-    fence_proxy_async();
-    __syncthreads();
     if (threadIdx.x == 0) {
         mbar_expect_tx(bar, static_cast<uint32_t>(W * sz));
         int64_t pos = g0;
         const int64_t end = g0 + W;
         while (pos < end) {
-            const int64_t src = imod(pos, n);
+            const int64_t src = wrap(pos);
             const int64_t len = min(end - pos, n - src);
             bulk_g2s(dst + (pos - g0), base + src, static_cast<uint32_t>(len * sz), bar);
             pos += len;
