@@ -155,6 +155,11 @@ class BatchedSolver:
         dxs = np.broadcast_to(np.asarray(dx, dtype=np.float64), (self.B,)).copy()
         self.dx = dxs
         self.cfl = np.array([scheme.cfl_constant(float(h)) for h in dxs], dtype=np.float64)
+        nu_for = getattr(scheme, "nu_for", None)
+        if nu_for is not None and len({nu_for(float(h)) for h in np.unique(dxs)}) > 1:
+            # Rusanov(alpha != 1): nu = dx^(alpha - 1) (scalar.py:231-234)
+            raise ValueError("the scheme's dissipation depends on dx and a plan takes one "
+                             "value: instances of Rusanov(alpha != 1) must share dx")
         self.theta = float(theta)
         self.dtype = dtype
         self.device = torch.device(device)
