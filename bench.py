@@ -381,8 +381,8 @@ def bench_gpu(args, rank: int, world: int) -> None:
         algo_bytes //= 2
     achieved = algo_bytes / per_launch_s / 1e9
     traffic = None
-    if "dram_bytes_per_cell_step" in consts:
-        traffic = consts["dram_bytes_per_cell_step"] * cells
+    if "dram_bytes_per_cell_step" in consts and args.scheme == "plain":
+        traffic = consts["dram_bytes_per_cell_step"] * cells  # measured on the plain FP64 step
     fp64_peak = None if args.profile else ctypes_fp_peak(L)
     fp64 = None
     if "fp64_flop_per_cell_step" in consts and fp64_peak:
@@ -421,7 +421,7 @@ def bench_gpu(args, rank: int, world: int) -> None:
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64",
+            "dtype": "f32" if solver.dtype == torch.float32 else "f64",
             "data": "synthetic",
             "config": _config(args),
             "clocks": clk.summary(),

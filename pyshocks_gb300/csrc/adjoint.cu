@@ -190,22 +190,19 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
         //   gR_j = fb_j (f'(R)/2 + a_j), and cell j+1 with gL = fb_j (f'(L)/2 - a_j),
         // fb_j = dt/dx (w_{j+1} - w_j), a_j = nu/2 max(|f'(v_j)|, |f'(v_{j+1})|).
         // The face values are kept for the wave-speed terms below.
-        float* db = reinterpret_cast<float*>(a.H);
-        for (int c = lo - 4 + tid; c < hi + 2; c += nt) db[c] = v[c + 1] - v[c];
         MlpFrags f;
         mlp_load_frags(p.lp.mlp, f);
         MlpBackFrags bk;
         mlp_load_back_frags(p.lp.mlp, bk);
-        __syncthreads();
         const int lane = tid & 31, g = lane >> 2, tq = lane & 3;
         const int myrow = 16 * (tq >> 1) + 8 * (tq & 1) + g;
         const int c0 = lo - 2, ncell = hi + 2 - c0;
         for (int qb = tid >> 5; qb * 32 < ncell; qb += nt >> 5) {
             const int r = qb * 32 + myrow;
             const int c = c0 + min(r, ncell - 1);
-            const float dm2 = db[c - 2], dm1 = db[c - 1], d0 = db[c], dp1 = db[c + 1];
-            const float sc[5] = {-(dm1 + dm2), -dm1, 0.0f, d0, d0 + dp1};
+            // the stencil relative to v_c as the forward forms it (learned_phase)
             const float vm = v[c - 1], vc = v[c], vp = v[c + 1];
+            const float sc[5] = {v[c - 2] - vc, vm - vc, 0.0f, vp - vc, v[c + 2] - vc};
             const float wm = w[c - 1], wc = w[c], wp = w[c + 1];
             float ul = 0.0f, ur = 0.0f;
             auto seed = [&](float cr, float cl, float& gR, float& gL) {

@@ -200,19 +200,15 @@ __host__ __device__ inline OpParams<float> float_params(const OpParams<T>& p) {
 }
 
 // learned reconstruction of cells [clo, chi): one cell per lane, 32 cells per
-// warp iteration, both faces of a cell from one network evaluation. The cell
-// differences d_k = v_{k+1} - v_k are formed once, in the state precision, and
-// stored as float in `dbuf`; a cell's stencil relative to v_c is a float sum
-// of them, and the face values are v_c + correction in the state precision, so
-// double states spend three double operations per cell here.
+// warp iteration, both faces of a cell from one network evaluation. A cell's
+// stencil relative to v_c is formed in the state precision straight from the
+// window (v_{c+o} - v_c, o = -2..2) and rounded to float; the face values are
+// v_c + correction in the state precision.
 template <class T>
 __device__ __forceinline__ void learned_phase(const T* v, int clo, int chi, T* UL, T* UR,
-                                              float* dbuf, const LearnedParams& lp) {
-    for (int c = clo - 2 + threadIdx.x; c < chi + 1; c += blockDim.x)
-        dbuf[c] = static_cast<float>(v[c + 1] - v[c]);
+                                              const LearnedParams& lp) {
     MlpFrags f;
     mlp_load_frags(lp.mlp, f);
-    __syncthreads();
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int ncell = chi - clo;
@@ -220,13 +216,13 @@ __device__ __forceinline__ void learned_phase(const T* v, int clo, int chi, T* U
     for (int q = warp; q * 32 < ncell; q += nw) {
         const int r = q * 32 + myrow;
         const int c = clo + min(r, ncell - 1);
-        const float dm2 = dbuf[c - 2], dm1 = dbuf[c - 1], d0 = dbuf[c], dp1 = dbuf[c + 1];
-        // v_{c+o} - v_c for o = -2..2
-        const float ds[5] = {-(dm1 + dm2), -dm1, 0.0f, d0, d0 + dp1};
+        const T vc = v[c];
+        const float ds[5] = {static_cast<float>(v[c - 2] - vc), static_cast<float>(v[c - 1] - vc),
+                             0.0f, static_cast<float>(v[c + 1] - vc),
+                             static_cast<float>(v[c + 2] - vc)};
         float cr, cl;
         learned_cell32(f, ds, lp, cr, cl);
         if (r < ncell) {
-            const T vc = v[c];
             UR[c] = vc + static_cast<T>(cr);
             UL[c] = vc + static_cast<T>(cl);
         }
@@ -282,7 +278,7 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
         }
         __syncthreads();
     } else if constexpr (REC == SHK_REC_LEARNED) {
-        learned_phase<T>(v, lo - 1, hi + 1, sm.UL, sm.UR, reinterpret_cast<float*>(sm.H), p.lp);
+        learned_phase<T>(v, lo - 1, hi + 1, sm.UL, sm.UR, p.lp);
         __syncthreads();
     } else if constexpr (REC == SHK_REC_CONSTANT) {
         // reconstruction.py:153-163: ul = ur = u

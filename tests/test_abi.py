@@ -65,6 +65,49 @@ def test_invalid_arguments_rejected_on_host(cdll):
     assert cdll.shk_plan_step(None, None, None, 1, None) == _lib.SHK_EINVAL
 
 
+def test_plan_arguments_rejected_on_host(cdll):
+    """Empty batches, degenerate instances, bad cell sizes and tiles are refused
+    before any device memory is touched (plans and host-buffer steppers)."""
+    import ctypes
+
+    import numpy as np
+
+    from pyshocks_gb300 import _lib
+
+    s = _lib.ShkScheme(flux=0, rec=0, equation=0, eps=1e-6, delta=0.0, nu=1.0, speed=1.0)
+    out = ctypes.c_void_p()
+
+    def create(offsets, dx, opts=None, *, chunks=None):
+        off = np.asarray(offsets, dtype=np.int64)
+        dxa = np.asarray(dx, dtype=np.float64)
+        cfl = 0.5 * dxa
+        B = len(off) - 1
+        o = ctypes.byref(opts) if opts is not None else None
+        if chunks is None:
+            return cdll.shk_plan_create(s, B, off.ctypes.data, dxa.ctypes.data, cfl.ctypes.data,
+                                        1.0, o, ctypes.byref(out))
+        return cdll.shk_host_stepper_create(s, B, off.ctypes.data, dxa.ctypes.data,
+                                            cfl.ctypes.data, 1.0, o, chunks, ctypes.byref(out))
+
+    for chunks in (None, 4):
+        assert create([0], [], chunks=chunks) == _lib.SHK_EINVAL  # no instance
+        assert create([0, 2], [0.1], chunks=chunks) == _lib.SHK_EINVAL  # n < 3
+        assert create([0, 64], [0.0], chunks=chunks) == _lib.SHK_EINVAL  # dx <= 0
+        assert create([0, 64], [-0.1], chunks=chunks) == _lib.SHK_EINVAL
+        for tile in (7, 8, 8200):  # not a multiple of 16 bytes, too short, too long
+            opts = _lib.ShkPlanOpts(dtype=_lib.SHK_F64, tile=tile, max_steps=0, ctas_per_sm=0)
+            assert create([0, 64], [0.1], opts, chunks=chunks) == _lib.SHK_EINVAL, tile
+        opts = _lib.ShkPlanOpts(dtype=7, tile=0, max_steps=0, ctas_per_sm=0)
+        assert create([0, 64], [0.1], opts, chunks=chunks) == _lib.SHK_EINVAL  # dtype
+    assert out.value is None
+    # host steppers step forward only and take a non-negative chunk count
+    opts = _lib.ShkPlanOpts(dtype=_lib.SHK_F64, tile=0, max_steps=10, ctas_per_sm=0)
+    assert create([0, 64], [0.1], opts, chunks=4) == _lib.SHK_EINVAL
+    assert create([0, 64], [0.1], chunks=-1) == _lib.SHK_EINVAL
+    assert cdll.shk_host_stepper_advance(None, None, None, 1, None) == _lib.SHK_EINVAL
+    assert cdll.shk_host_stepper_num_chunks(None) == 0
+
+
 def test_product_path_never_imports_the_oracle():
     """The package must not import, call or link anything under oracle/."""
     pkg = ROOT / "pyshocks_gb300"

@@ -117,3 +117,26 @@ def test_rusanov_alpha_plan_needs_one_dx():
     with pytest.raises(ValueError, match="share dx"):
         BatchedSolver(scheme, [64, 128], [2.0 / 64, 2.0 / 128])
     BatchedSolver(scheme, [64, 64], 2.0 / 64)  # one dx: fine
+
+
+def test_ssprk33_time_order_gpu():
+    """``tests/test_timestepping.py:26-99`` on the GPU path: SSPRK33 is third
+    order in time. One batch of the same grid (periodic advection, N = 256,
+    WENOJS53) stepped to t = 1 with Courant numbers 0.8, 0.4, 0.2, 0.1 and a
+    reference at 0.0125: the spatial error is common to all instances, so the
+    differences to the reference are the temporal errors."""
+    from pyshocks_gb300 import burgers, grid as G, reconstruction
+
+    n, tfinal = 256, 1.0
+    h = 2.0 / n
+    scheme = burgers.AdvectionRusanov(rec=reconstruction.WENOJS53(eps=1.0e-6))
+    g = G.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
+    q = G.make_leggauss_quadrature(g, order=5)
+    v0 = G.cell_average(q, lambda x: np.sin(np.pi * x))[3:-3]
+    courant = [0.8, 0.4, 0.2, 0.1, 0.0125]
+    maxits = [int(np.ceil(tfinal / (c * h))) for c in courant]
+    dts = [tfinal / m for m in maxits]
+    out = _run(scheme, [n] * len(courant), -1.0, 1.0, [v0] * len(courant), _dt_table(dts, maxits))
+    ref = out[-1]
+    errs = [np.sum(np.abs(u - ref)) * h for u in out[:-1]]
+    assert _eoc(dts[:-1], errs) >= 3 - 0.1, errs
