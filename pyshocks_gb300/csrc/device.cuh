@@ -200,6 +200,36 @@ __device__ __forceinline__ void weno53_cell_d(double v, double dm1, double d0, d
     ul = fma(nl * dr, r, v);
 }
 
+// Float variant of weno53_cell_d for the one-pass float reconstruction: the
+// same unscaled differences (d_{c-2} .. d_{c+1} from the window, E and G formed
+// here) and folded corrections, with the weights P_k = 1/s_k and the two
+// normalisations as one-instruction approximate reciprocals (a product form
+// could underflow in float).
+__device__ __forceinline__ void weno53_cell_f(float v, float dm2, float dm1, float d0, float dp1,
+                                              float eps4, float& ul, float& ur) {
+    const float Em1 = dm1 - dm2, E0 = d0 - dm1, Ep1 = dp1 - d0;
+    const float h0 = fmaf(2.0f, dm1, Em1);
+    const float h1 = d0 + dm1;
+    const float h2 = fmaf(-2.0f, d0, Ep1);
+    float s0 = fmaf(h0, h0, fmaf((13.0f / 3.0f) * Em1, Em1, eps4)); s0 = s0 * s0;
+    float s1 = fmaf(h1, h1, fmaf((13.0f / 3.0f) * E0, E0, eps4)); s1 = s1 * s1;
+    float s2 = fmaf(h2, h2, fmaf((13.0f / 3.0f) * Ep1, Ep1, eps4)); s2 = s2 * s2;
+    const float P0 = rcp_approx_f32(s0), P1 = rcp_approx_f32(s1), P2 = rcp_approx_f32(s2);
+    const float cr0 = fmaf(2.0f, h0, -dm1);
+    const float cr1 = fmaf(12.0f, d0, 6.0f * dm1);
+    const float cr2 = 3.0f * (d0 - h2);
+    const float cl0 = fmaf(2.0f, h2, d0);
+    const float cl1 = fmaf(6.0f, E0, -cr1);
+    const float cl2 = -3.0f * (h0 + dm1);
+    const float nr = fmaf(P0, cr0, fmaf(P1, cr1, P2 * cr2));
+    const float nl = fmaf(P2, cl0, fmaf(P1, cl1, P0 * cl2));
+    const float m = 36.0f * P1;
+    const float dr = fmaf(6.0f, P0, fmaf(18.0f, P2, m));
+    const float dl = fmaf(6.0f, P2, fmaf(18.0f, P0, m));
+    ur = fmaf(nr, rcp_approx_f32(dr), v);
+    ul = fmaf(nl, rcp_approx_f32(dl), v);
+}
+
 // 2|x| from the bit pattern of |x| (integer exponent increment, exact for
 // normal numbers; zero and subnormals take the FP path)
 __device__ __forceinline__ double twice_abs_bits(unsigned long long b) {

@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
     __shared__ unsigned long long red[32];
     __shared__ int is_last;
     __shared__ DtState item_dt;  // the item's step, computed once per CTA
-    __shared__ double item_dx;
+    __shared__ T item_dtdx, item_dx;
     constexpr int HL = step_halo<T>();
     using B = typename Bits<T>::type;
 
@@ -84,8 +84,10 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
         // this GPU) and shares it; the previous item's readers are past the
         // barrier that ended that item
         if (threadIdx.x == 0) {
-            item_dt = plan_dt(P, k, b, from_bits(P.amax[size_t(cur) * P.B + b]));
-            item_dx = 1.0 / P.inv_dx[b];
+            const DtState d = plan_dt(P, k, b, from_bits(P.amax[size_t(cur) * P.B + b]));
+            item_dt = d;
+            item_dtdx = static_cast<T>(d.dt * P.inv_dx[b]);
+            item_dx = static_cast<T>(1.0 / P.inv_dx[b]);
         }
         __syncthreads();
         const DtState ds = item_dt;
@@ -104,9 +106,9 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
                 if (threadIdx.x == 0) atomicOr(P.status, ERR_TIMEOUT);
                 break;
             }
-            const T dtdx = static_cast<T>(ds.dt * P.inv_dx[b]);
+            const T dtdx = item_dtdx;
             OpParams<T> pb = p;
-            pb.dx = static_cast<T>(item_dx);
+            pb.dx = item_dx;
             mx = step_tile<T, EQ, REC, FLUX>(sm, uout + off + s0, te, dtdx, pb, plan_bc(P, b),
                                              s0 - HL, n);
         }

@@ -262,17 +262,14 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
         __syncthreads();
     } else if constexpr (REC == SHK_REC_WENOJS53 && sizeof(T) == 4) {
         // float: each cell's differences straight from its five values (a few
-        // more float operations, two fewer barriers and about half the
-        // shared-memory traffic of the staged phases below)
+        // more float operations, no barriers and about half the shared-memory
+        // traffic of staged difference arrays)
+        const float eps4 = 4.0f * p.eps;
 #pragma unroll 2
         for (int c = lo - 1 + tid; c < hi + 1; c += nt) {
             const T vm2 = v[c - 2], vm1 = v[c - 1], v0 = v[c], vp1 = v[c + 1], vp2 = v[c + 2];
-            const T hm2 = T(0.5) * (vm1 - vm2), hm1 = T(0.5) * (v0 - vm1);
-            const T h0 = T(0.5) * (vp1 - v0), hp1 = T(0.5) * (vp2 - vp1);
-            const T dm1 = hm1 - hm2, d0 = h0 - hm1, dp1 = hp1 - h0;
             T ul, ur;
-            weno53_cell<T>(v0, hm2, hm1, h0, hp1, dm1, d0, dp1, (T(13.0 / 3.0) * dm1) * dm1,
-                           (T(13.0 / 3.0) * d0) * d0, (T(13.0 / 3.0) * dp1) * dp1, p.eps, ul, ur);
+            weno53_cell_f(v0, vm1 - vm2, v0 - vm1, vp1 - v0, vp2 - vp1, eps4, ul, ur);
             sm.UL[c] = ul;
             sm.UR[c] = ur;
         }
