@@ -510,7 +510,8 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
     }
     __syncthreads();
     uint32_t phase = 0;
-    for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
+    __shared__ int s_item;
+    for (int item = next_item(P, 2, &s_item); item >= 0; item = next_item(P, 2, &s_item)) {
         const int b = P.item_inst[item];
         const int64_t off = P.offsets[b];
         const int64_t n = P.offsets[b + 1] - off;
@@ -524,7 +525,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
         }
         if (!adjoint_load<T>(a, um + off, pnext + off, n, s0, te, &bar, phase)) {
             if (threadIdx.x == 0) atomicOr(P.status, ERR_TIMEOUT);
-            return;
+            break;
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
         const BcView bc = plan_bc(P, b);
@@ -533,6 +534,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
         else adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p, bc, g0, n);
         __syncthreads();
     }
+    finish_items(P, 2);
 }
 
 // forward step with a recorded dt (no CFL, no time update): recompute of the
@@ -553,7 +555,8 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
     }
     __syncthreads();
     uint32_t phase = 0;
-    for (int item = blockIdx.x; item < P.nitems; item += gridDim.x) {
+    __shared__ int s_item;
+    for (int item = next_item(P, 4, &s_item); item >= 0; item = next_item(P, 4, &s_item)) {
         const int b = P.item_inst[item];
         const int64_t off = P.offsets[b];
         const int64_t n = P.offsets[b + 1] - off;
@@ -567,13 +570,14 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
         }
         if (!load_window<T>(sm.U, uin + off, n, s0 - HL, te + 2 * HL, &bar, phase)) {
             if (threadIdx.x == 0) atomicOr(P.status, ERR_TIMEOUT);
-            return;
+            break;
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
         step_tile<T, EQ, REC, SHK_FLUX_RUSANOV>(sm, uout + off + s0, te, dtdx, p, plan_bc(P, b),
                                                 s0 - HL, n);
         __syncthreads();
     }
+    finish_items(P, 4);
 }
 
 // single instance on the reference's ghosted layout (drop-in adjoint_step)

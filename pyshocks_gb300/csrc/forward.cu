@@ -74,7 +74,8 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
     const int cur = static_cast<int>(k & 1), nxt = cur ^ 1;
     bool ok = true;
 
-    for (int item = blockIdx.x; item < P.nitems && ok; item += gridDim.x) {
+    __shared__ int s_item;
+    for (int item = next_item(P, 0, &s_item); item >= 0 && ok; item = next_item(P, 0, &s_item)) {
         const int b = P.item_inst[item];
         const int64_t off = P.offsets[b];
         const int64_t n = P.offsets[b + 1] - off;
@@ -132,6 +133,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
         __syncthreads();
         if (threadIdx.x == 0) {
             *reinterpret_cast<volatile unsigned*>(P.done) = 0u;
+            atomicExch(P.sched, 0u);  // every CTA has taken its last item
             *reinterpret_cast<volatile int64_t*>(P.step) = k + 1;
             __threadfence();
         }
@@ -574,6 +576,8 @@ struct shk_plan {
     int bc_left = SHK_BC_PERIODIC, bc_right = SHK_BC_PERIODIC;
     double* bc_dir = nullptr;  // [B][2][3]
     double* bc_neu = nullptr;  // [B][2]
+    int32_t* item_order = nullptr;  // [nitems] longest first
+    unsigned int* sched = nullptr;  // [8] scheduling counters
     // host mirror of the number of steps launched since reset
     int64_t host_steps = 0;
     // captured two-step graph
@@ -589,6 +593,7 @@ struct shk_plan {
         P.partial = partial; P.B = B;
         P.dt_fixed = fixed_steps > 0 ? dt_fixed : nullptr; P.fixed_steps = fixed_steps;
         P.bc_left = bc_left; P.bc_right = bc_right; P.bc_dir = bc_dir; P.bc_neu = bc_neu; P.nitems = nitems; P.tile = tile; P.max_steps = max_steps;
+        P.item_order = item_order; P.sched = sched;
         return P;
     }
 };
@@ -735,7 +740,7 @@ int shk_plan_destroy(shk_plan* plan) {
     void* ptrs[] = {plan->item_inst, plan->item_tile, plan->item_first, plan->offsets, plan->cfl,
                     plan->inv_dx, plan->tfinal, plan->amax, plan->t, plan->dt_hist, plan->step,
                     plan->done, plan->status, plan->partial, plan->dt_fixed, plan->bc_dir,
-                    plan->bc_neu};
+                    plan->bc_neu, plan->item_order, plan->sched};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete plan;
@@ -766,6 +771,16 @@ int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_of
         }
     }
     first[batch] = static_cast<int32_t>(inst.size());
+    // scheduling order: longest items first (full tiles, then partial tiles
+    // by decreasing length), ties in packing order
+    std::vector<int32_t> order(inst.size());
+    std::vector<int64_t> len(inst.size());
+    for (size_t i = 0; i < inst.size(); ++i) {
+        order[i] = static_cast<int32_t>(i);
+        const int64_t n = h_offsets[inst[i] + 1] - h_offsets[inst[i]];
+        len[i] = std::min<int64_t>(tile, n - int64_t(tl[i]) * tile);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return len[x] > len[y]; });
     auto* P = new (std::nothrow) shk_plan();
     if (!P) return SHK_ENOMEM;
     P->scheme = *scheme;
@@ -790,7 +805,9 @@ int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_of
               alloc((void**)&P->t, sizeof(double) * batch) &&
               alloc((void**)&P->step, sizeof(int64_t)) && alloc((void**)&P->done, sizeof(unsigned)) &&
               alloc((void**)&P->status, sizeof(int32_t)) &&
-              alloc((void**)&P->partial, sizeof(double) * P->nitems);
+              alloc((void**)&P->partial, sizeof(double) * P->nitems) &&
+              alloc((void**)&P->item_order, sizeof(int32_t) * P->nitems) &&
+              alloc((void**)&P->sched, sizeof(unsigned) * 8);
     if (ok && P->max_steps > 0)
         ok = alloc((void**)&P->dt_hist, sizeof(double) * size_t(P->max_steps) * batch);
     if (!ok) {
@@ -799,6 +816,8 @@ int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_of
     }
     ok = cudaMemcpy(P->item_inst, inst.data(), sizeof(int32_t) * P->nitems, cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(P->item_tile, tl.data(), sizeof(int32_t) * P->nitems, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemcpy(P->item_order, order.data(), sizeof(int32_t) * P->nitems, cudaMemcpyHostToDevice) == cudaSuccess &&
+         cudaMemset(P->sched, 0, sizeof(unsigned) * 8) == cudaSuccess &&
          cudaMemcpy(P->item_first, first.data(), sizeof(int32_t) * (batch + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(P->offsets, h_offsets, sizeof(int64_t) * (batch + 1), cudaMemcpyHostToDevice) == cudaSuccess &&
          cudaMemcpy(P->cfl, h_cfl, sizeof(double) * batch, cudaMemcpyHostToDevice) == cudaSuccess &&
@@ -870,6 +889,7 @@ int shk_plan_reset(shk_plan* plan, const void* u, const double* t0, const double
     SHK_CUDA(cudaMemsetAsync(plan->amax, 0, sizeof(unsigned long long) * 2 * B, st));
     SHK_CUDA(cudaMemsetAsync(plan->step, 0, sizeof(int64_t), st));
     SHK_CUDA(cudaMemsetAsync(plan->done, 0, sizeof(unsigned), st));
+    SHK_CUDA(cudaMemsetAsync(plan->sched, 0, sizeof(unsigned) * 8, st));
     SHK_CUDA(cudaMemsetAsync(plan->status, 0, sizeof(int32_t), st));
     if (t0) SHK_CUDA(cudaMemcpyAsync(plan->t, t0, sizeof(double) * B, cudaMemcpyDeviceToDevice, st));
     else SHK_CUDA(cudaMemsetAsync(plan->t, 0, sizeof(double) * B, st));

@@ -610,8 +610,37 @@ struct PlanDev {
     int bc_left, bc_right;   // SHK_BC_* of every instance
     const double* bc_dir;    // [B][2][3] Dirichlet ghost values
     const double* bc_neu;    // [B][2] Neumann gradients
+    const int32_t* item_order;  // [nitems] items longest first (dynamic scheduling)
+    unsigned int* sched;        // [8] item counters of the scheduled kernels
     int32_t B, nitems, tile, max_steps;
 };
+
+// Dynamic item scheduling. A CTA takes the next item of the plan's
+// longest-first order from the counter sched[slot]; uneven items (partial
+// tiles, copied-through instances) then balance over the persistent grid,
+// where a fixed stride would hand some CTAs only long items. Returns the item,
+// or -1 when none is left. Every caller's loop body ends with a barrier, which
+// orders the read of *s_item before thread 0 overwrites it.
+__device__ __forceinline__ int next_item(const PlanDev& P, int slot, int* s_item) {
+    if (threadIdx.x == 0) *s_item = static_cast<int>(atomicAdd(P.sched + slot, 1u));
+    __syncthreads();
+    const int q = *s_item;
+    return q < P.nitems ? P.item_order[q] : -1;
+}
+
+// end of a scheduled launch: the CTA that finishes last (counter
+// sched[slot + 1]) resets both counters for the next launch
+__device__ __forceinline__ void finish_items(const PlanDev& P, int slot) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(P.sched + slot + 1, 1u) == gridDim.x - 1) {
+            atomicExch(P.sched + slot, 0u);
+            atomicExch(P.sched + slot + 1, 0u);
+            __threadfence();
+        }
+    }
+}
 
 // the boundary of instance b (time-independent data: one stage for all three)
 __device__ __forceinline__ BcView plan_bc(const PlanDev& P, int b) {
