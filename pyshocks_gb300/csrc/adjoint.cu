@@ -194,6 +194,8 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
         mlp_load_frags(p.lp.mlp, f);
         MlpBackFrags bk;
         mlp_load_back_frags(p.lp.mlp, bk);
+        // warp scratch: GL, GR, GA (3W floats, unused by this branch)
+        float* scr = learned_scratch(a.GL) + (tid >> 5) * kWarpScratchVjp;
         const int lane = tid & 31, g = lane >> 2, tq = lane & 3;
         const int myrow = 16 * (tq >> 1) + 8 * (tq & 1) + g;
         const int c0 = lo - 2, ncell = hi + 2 - c0;
@@ -215,7 +217,7 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
                 gL = ((wc - wm) * dtdx) * fmaf(0.5f, flux_prime<EQ>(ul, p.c), -hm);
             };
             float dd[5];
-            learned_cell_vjp32(f, bk, sc, seed, p.lp, dd);
+            learned_cell_vjp32(f, bk, sc, seed, p.lp, scr, dd);
             if (r < ncell) {
                 a.T0[c] = dd[0]; a.T1[c] = dd[1]; a.T2[c] = dd[2]; a.T3[c] = dd[3]; a.T4[c] = dd[4];
                 a.UL[c] = ul;

@@ -759,6 +759,8 @@ int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_of
     int tile = (opts && opts->tile > 0) ? opts->tile : kDefaultTile;
     const int align = dtype == SHK_F64 ? 2 : 4;
     if (tile % align || tile < 16 || tile > 8192) return SHK_EINVAL;
+    // the learned phase's warp scratch lives in the window's free arrays
+    if (scheme->rec == SHK_REC_LEARNED && tile < kLearnedMinTile) return SHK_EINVAL;
     std::vector<int32_t> inst, tl, first(batch + 1, 0);
     for (int b = 0; b < batch; ++b) {
         const int64_t n = h_offsets[b + 1] - h_offsets[b];

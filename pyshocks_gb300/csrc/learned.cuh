@@ -206,6 +206,50 @@ __device__ __forceinline__ uint32_t tanh_bf16x2(uint32_t x) {
     return y;
 }
 
+// ---- warp exchanges through shared memory ------------------------------------
+// Rows of the warp's 32-cell block go through a per-warp scratch area (16-byte
+// aligned): row r at scr + 4 r (16 B) for fragment rows, or scr + 6 r for the
+// input cotangents. An A fragment is then one ldmatrix.x4 instead of twelve
+// shuffles and selects, and a lane's row of an accumulator tile one vector
+// load. Every exchange begins with __syncwarp, so a lane never overwrites
+// scratch that another lane of the warp is still to read.
+constexpr int kWarpScratch = 128;      // floats per warp, forward
+constexpr int kWarpScratchVjp = 192;   // floats per warp, backward
+
+__device__ __forceinline__ void ldmatrix_x4(const float* row, uint32_t a[4]) {
+    const uint32_t addr = static_cast<uint32_t>(__cvta_generic_to_shared(row));
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3])
+                 : "r"(addr)
+                 : "memory");
+}
+
+// A fragments (rows g, g+8 of tiles A and B; columns 2t, 2t+1) of the block
+// whose row `myrow` holds this lane's 8 b16 values (w0..w3)
+__device__ __forceinline__ void rows_to_afrags(float* scr, int myrow, uint32_t w0, uint32_t w1,
+                                               uint32_t w2, uint32_t w3, uint32_t a[4]) {
+    __syncwarp();
+    *reinterpret_cast<uint4*>(scr + 4 * myrow) = make_uint4(w0, w1, w2, w3);
+    __syncwarp();
+    ldmatrix_x4(scr + 4 * (threadIdx.x & 31), a);
+}
+
+// columns 0..3 of the lane's row `myrow` from the accumulators of tiles A
+// (c[0..3]: rows g, g+8) and B (d[0..3]); lanes t = 0, 1 hold columns 0..3
+__device__ __forceinline__ float4 accum_row4(float* scr, int myrow, const float c[4],
+                                             const float d[4]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    __syncwarp();
+    if (t < 2) {
+        *reinterpret_cast<float2*>(scr + 4 * g + 2 * t) = make_float2(c[0], c[1]);
+        *reinterpret_cast<float2*>(scr + 4 * (g + 8) + 2 * t) = make_float2(c[2], c[3]);
+        *reinterpret_cast<float2*>(scr + 4 * (g + 16) + 2 * t) = make_float2(d[0], d[1]);
+        *reinterpret_cast<float2*>(scr + 4 * (g + 24) + 2 * t) = make_float2(d[2], d[3]);
+    }
+    __syncwarp();
+    return *reinterpret_cast<const float4*>(scr + 4 * myrow);
+}
+
 // hidden layers + output of one m16 tile; a0/a1: layer-1 A registers (rows g, g+8)
 __device__ __forceinline__ void mlp_tile(const MlpFrags& f, uint32_t a0, uint32_t a1, float& z0,
                                          float& z1, float& z2, float& z3) {
@@ -238,38 +282,25 @@ __device__ __forceinline__ void mlp_tile(const MlpFrags& f, uint32_t a0, uint32_
 // face cr, left face cl) from its shifted stencil ds (ds[2] = 0), with the
 // WENO-JS trust band per face. All 32 lanes must call it (shuffles) with
 // finite stencils.
+// scr: the warp's kWarpScratch floats of shared memory (16-byte aligned).
 __device__ __forceinline__ void learned_cell32(const MlpFrags& f, const float ds[5],
-                                               const LearnedParams& lp, float& cr, float& cl) {
-    const int lane = threadIdx.x & 31, t = lane & 3, base = lane & ~3;
-    // normalised input and its packed column pairs (x0,x1) (x2,x3) (x4,1)
+                                               const LearnedParams& lp, float* scr, float& cr,
+                                               float& cl) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int myrow = 16 * (t >> 1) + 8 * (t & 1) + g;
+    // normalised input, its row (x0,x1) (x2,x3) (x4,1) (0,0) of the layer-1
+    // A operand, and the A fragments of both tiles
     float x[5];
     mlp_normalise(ds, x, lp.norm_eps);
-    const uint32_t p0 = pack_bf16(x[0], x[1]), p1 = pack_bf16(x[2], x[3]), p2 = pack_bf16(x[4], 1.0f);
-    // A registers of lane (g, t): columns 2t, 2t+1 of rows g and g+8 of each tile,
-    // owned by lanes base+0 (A, g), base+1 (A, g+8), base+2 (B, g), base+3 (B, g+8)
     uint32_t a[4];
-#pragma unroll
-    for (int o = 0; o < 4; ++o) {
-        const uint32_t q0 = __shfl_sync(0xffffffffu, p0, base + o);
-        const uint32_t q1 = __shfl_sync(0xffffffffu, p1, base + o);
-        const uint32_t q2 = __shfl_sync(0xffffffffu, p2, base + o);
-        a[o] = t == 0 ? q0 : (t == 1 ? q1 : (t == 2 ? q2 : 0u));
-    }
-    float zA0, zA1, zA2, zA3, zB0, zB1, zB2, zB3;
-    mlp_tile(f, a[0], a[1], zA0, zA1, zA2, zA3);
-    mlp_tile(f, a[2], a[3], zB0, zB1, zB2, zB3);
-    // logits of the owned row: z[0], z[1] from lane base+0, z[2] from lane base+1
-    const float u0 = __shfl_sync(0xffffffffu, zA0, base), u1 = __shfl_sync(0xffffffffu, zA1, base);
-    const float u2 = __shfl_sync(0xffffffffu, zA2, base), u3 = __shfl_sync(0xffffffffu, zA3, base);
-    const float v0 = __shfl_sync(0xffffffffu, zB0, base), v1 = __shfl_sync(0xffffffffu, zB1, base);
-    const float v2 = __shfl_sync(0xffffffffu, zB2, base), v3 = __shfl_sync(0xffffffffu, zB3, base);
-    const float w0 = __shfl_sync(0xffffffffu, zA0, base + 1), w1 = __shfl_sync(0xffffffffu, zA2, base + 1);
-    const float y0 = __shfl_sync(0xffffffffu, zB0, base + 1), y1 = __shfl_sync(0xffffffffu, zB2, base + 1);
-    float z0, z1, z2;
-    if (t == 0) { z0 = u0; z1 = u1; z2 = w0; }
-    else if (t == 1) { z0 = u2; z1 = u3; z2 = w1; }
-    else if (t == 2) { z0 = v0; z1 = v1; z2 = y0; }
-    else { z0 = v2; z1 = v3; z2 = y1; }
+    rows_to_afrags(scr, myrow, pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], 1.0f),
+                   0u, a);
+    float zA[4], zB[4];
+    mlp_tile(f, a[0], a[1], zA[0], zA[1], zA[2], zA[3]);
+    mlp_tile(f, a[2], a[3], zB[0], zB[1], zB[2], zB[3]);
+    // logits of the owned row (columns 0..2 of the output tiles)
+    const float4 zr = accum_row4(scr, myrow, zA, zB);
+    const float z0 = zr.x, z1 = zr.y, z2 = zr.z;
     // softmax of both faces, trust band, corrections
     const float zm = fmaxf(fmaxf(z0, z1), z2);
     float wr[3], wl[3];
@@ -431,37 +462,22 @@ __device__ __forceinline__ void mlp_tile_back(const MlpBackFrags& b, uint32_t d0
 template <class Seed>
 __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpBackFrags& bk,
                                                    const float s[5], Seed&& seed,
-                                                   const LearnedParams& lp, float dsum[5]) {
-    const int lane = threadIdx.x & 31, t = lane & 3, base = lane & ~3;
+                                                   const LearnedParams& lp, float* scr,
+                                                   float dsum[5]) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int myrow = 16 * (t >> 1) + 8 * (t & 1) + g;
     // ---- forward (as learned_cell32), keeping the activations
     float x[5];
     mlp_normalise(s, x, lp.norm_eps);
-    const uint32_t p0 = pack_bf16(x[0], x[1]), p1 = pack_bf16(x[2], x[3]), p2 = pack_bf16(x[4], 1.0f);
     uint32_t a[4];
-#pragma unroll
-    for (int o = 0; o < 4; ++o) {
-        const uint32_t q0 = __shfl_sync(0xffffffffu, p0, base + o);
-        const uint32_t q1 = __shfl_sync(0xffffffffu, p1, base + o);
-        const uint32_t q2 = __shfl_sync(0xffffffffu, p2, base + o);
-        a[o] = t == 0 ? q0 : (t == 1 ? q1 : (t == 2 ? q2 : 0u));
-    }
+    rows_to_afrags(scr, myrow, pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], 1.0f),
+                   0u, a);
     uint32_t A2a[2][4], A3a[2][4], A2b[2][4], A3b[2][4];
-    float zA0, zA1, zA2, zA3, zB0, zB1, zB2, zB3;
-    mlp_tile_keep(f, a[0], a[1], A2a, A3a, zA0, zA1, zA2, zA3);
-    mlp_tile_keep(f, a[2], a[3], A2b, A3b, zB0, zB1, zB2, zB3);
-    float z0, z1, z2;
-    {
-        const float u0 = __shfl_sync(0xffffffffu, zA0, base), u1 = __shfl_sync(0xffffffffu, zA1, base);
-        const float u2 = __shfl_sync(0xffffffffu, zA2, base), u3 = __shfl_sync(0xffffffffu, zA3, base);
-        const float v0 = __shfl_sync(0xffffffffu, zB0, base), v1 = __shfl_sync(0xffffffffu, zB1, base);
-        const float v2 = __shfl_sync(0xffffffffu, zB2, base), v3 = __shfl_sync(0xffffffffu, zB3, base);
-        const float w0 = __shfl_sync(0xffffffffu, zA0, base + 1), w1 = __shfl_sync(0xffffffffu, zA2, base + 1);
-        const float y0 = __shfl_sync(0xffffffffu, zB0, base + 1), y1 = __shfl_sync(0xffffffffu, zB2, base + 1);
-        if (t == 0) { z0 = u0; z1 = u1; z2 = w0; }
-        else if (t == 1) { z0 = u2; z1 = u3; z2 = w1; }
-        else if (t == 2) { z0 = v0; z1 = v1; z2 = y0; }
-        else { z0 = v2; z1 = v3; z2 = y1; }
-    }
+    float zA[4], zB[4];
+    mlp_tile_keep(f, a[0], a[1], A2a, A3a, zA[0], zA[1], zA[2], zA[3]);
+    mlp_tile_keep(f, a[2], a[3], A2b, A3b, zB[0], zB[1], zB[2], zB[3]);
+    const float4 zr = accum_row4(scr, myrow, zA, zB);
+    const float z0 = zr.x, z1 = zr.y, z2 = zr.z;
     // ---- per-cell part: weights, fallback, direct terms, logit cotangents
     float hr[3], hl[3];
     cell_substencils(s, hr, hl);
@@ -525,34 +541,32 @@ __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpB
     ez = mz > 0.0f ? max(-100, min(100, ez)) : 0;
     const float up = __uint_as_float(static_cast<uint32_t>(127 - ez) << 23);  // 2^-ez
     const float down = __uint_as_float(static_cast<uint32_t>(127 + ez) << 23);  // 2^ez
-    const uint32_t e01 = pack_f16(dz[0] * up, dz[1] * up), e2 = pack_f16(dz[2] * up, 0.0f);
-    // ---- network backward on the tensor cores: A registers of the logit
-    // cotangents (columns 2t, 2t+1 of rows g, g+8 of each tile)
+    // ---- network backward on the tensor cores: the A fragments of the logit
+    // cotangents from the rows (dz0, dz1) (dz2, 0) (0, 0) (0, 0)
     uint32_t d[4];
-#pragma unroll
-    for (int o = 0; o < 4; ++o) {
-        const uint32_t q01 = __shfl_sync(0xffffffffu, e01, base + o);
-        const uint32_t q2 = __shfl_sync(0xffffffffu, e2, base + o);
-        d[o] = t == 0 ? q01 : (t == 1 ? q2 : 0u);
-    }
+    rows_to_afrags(scr, myrow, pack_f16(dz[0] * up, dz[1] * up), pack_f16(dz[2] * up, 0.0f), 0u,
+                   0u, d);
     float xa[4], xb[4];
     mlp_tile_back(bk, d[0], d[1], A2a, A3a, xa);
     mlp_tile_back(bk, d[2], d[3], A2b, A3b, xb);
-    // gather the owned row's dx[0..4] from lanes base+0 (columns 0, 1),
-    // base+1 (2, 3) and base+2 (4)
+    // the owned row's dx[0..5] (columns 0..5 of the input-gradient tiles, held
+    // by lanes t = 0, 1, 2), through rows of 6 floats
     float dx[6];
+    {
+        __syncwarp();
+        if (t < 3) {
+            *reinterpret_cast<float2*>(scr + 6 * g + 2 * t) = make_float2(xa[0], xa[1]);
+            *reinterpret_cast<float2*>(scr + 6 * (g + 8) + 2 * t) = make_float2(xa[2], xa[3]);
+            *reinterpret_cast<float2*>(scr + 6 * (g + 16) + 2 * t) = make_float2(xb[0], xb[1]);
+            *reinterpret_cast<float2*>(scr + 6 * (g + 24) + 2 * t) = make_float2(xb[2], xb[3]);
+        }
+        __syncwarp();
 #pragma unroll
-    for (int src = 0; src < 3; ++src) {
-        const float r0 = __shfl_sync(0xffffffffu, xa[0], base + src);
-        const float r1 = __shfl_sync(0xffffffffu, xa[1], base + src);
-        const float r2 = __shfl_sync(0xffffffffu, xa[2], base + src);
-        const float r3 = __shfl_sync(0xffffffffu, xa[3], base + src);
-        const float r4 = __shfl_sync(0xffffffffu, xb[0], base + src);
-        const float r5 = __shfl_sync(0xffffffffu, xb[1], base + src);
-        const float r6 = __shfl_sync(0xffffffffu, xb[2], base + src);
-        const float r7 = __shfl_sync(0xffffffffu, xb[3], base + src);
-        dx[2 * src] = t == 0 ? r0 : (t == 1 ? r2 : (t == 2 ? r4 : r6));
-        dx[2 * src + 1] = t == 0 ? r1 : (t == 1 ? r3 : (t == 2 ? r5 : r7));
+        for (int k = 0; k < 3; ++k) {
+            const float2 v = *reinterpret_cast<const float2*>(scr + 6 * myrow + 2 * k);
+            dx[2 * k] = v.x;
+            dx[2 * k + 1] = v.y;
+        }
     }
     // ---- normalisation x = (s - mean) / (max - min + norm_eps), unscaled
     const float m = (s[0] + s[1] + s[2] + s[3] + s[4]) * 0.2f;

@@ -15,6 +15,11 @@ namespace shk {
 
 constexpr int kThreads = 256;
 constexpr int kDefaultTile = 1024;
+// shortest tile of a plan with the learned reconstruction: its warp scratch
+// (8 warps x 128 floats forward, x 192 in the reverse step) lives in window
+// arrays that the learned phase leaves free (2W floats in the mixed step,
+// 3W in the float step and the reverse step)
+constexpr int kLearnedMinTile = 512;
 
 // halo of a window: 9 cells are needed for three fused stages, rounded up so
 // that the window start stays 16-byte aligned for cp.async.bulk
@@ -62,18 +67,19 @@ struct Smem {
         this->W = W;
     }
     // compact layout of that mixed step: U (double window), then as float
-    // arrays S (2W: uf, k), H (2W: cell differences, increments), D, UL, UR;
-    // Q aliases D (the learned reconstruction does not use it)
+    // arrays S (2W: uf, k), I (increments), H, D, UL, UR; H and D are
+    // contiguous (the learned phase's warp scratch, before D takes the face
+    // fluxes); Q aliases D (the learned reconstruction does not use it)
     __device__ void carve_mixed(unsigned char* base, int W) {
         U = reinterpret_cast<T*>(base);
         float* f = reinterpret_cast<float*>(base + size_t(W) * sizeof(double));
         S = reinterpret_cast<T*>(f);
-        H = reinterpret_cast<T*>(f + 2 * W);
+        I = reinterpret_cast<T*>(f + 2 * W);
+        H = reinterpret_cast<T*>(f + 3 * W);
         D = reinterpret_cast<T*>(f + 4 * W);
         UL = reinterpret_cast<T*>(f + 5 * W);
         UR = reinterpret_cast<T*>(f + 6 * W);
         Q = D;
-        I = nullptr;
         this->W = W;
     }
     __device__ void carve(unsigned char* base, int W) {
@@ -199,18 +205,27 @@ __host__ __device__ inline OpParams<float> float_params(const OpParams<T>& p) {
     return f;
 }
 
+// 16-byte aligned start of a shared-memory scratch region
+template <class P>
+__device__ __forceinline__ float* learned_scratch(P* region) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(region);
+    return reinterpret_cast<float*>((a + 15) & ~uintptr_t(15));
+}
+
 // learned reconstruction of cells [clo, chi): one cell per lane, 32 cells per
 // warp iteration, both faces of a cell from one network evaluation. A cell's
 // stencil relative to v_c is formed in the state precision straight from the
 // window (v_{c+o} - v_c, o = -2..2) and rounded to float; the face values are
 // v_c + correction in the state precision.
+// scratch: kWarpScratch floats per warp of shared memory (16-byte aligned).
 template <class T>
 __device__ __forceinline__ void learned_phase(const T* v, int clo, int chi, T* UL, T* UR,
-                                              const LearnedParams& lp) {
+                                              const LearnedParams& lp, float* scratch) {
     MlpFrags f;
     mlp_load_frags(lp.mlp, f);
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    float* scr = scratch + warp * kWarpScratch;
     const int ncell = chi - clo;
     const int myrow = 16 * (t >> 1) + 8 * (t & 1) + g;  // within the 32-cell block
     for (int q = warp; q * 32 < ncell; q += nw) {
@@ -221,7 +236,7 @@ __device__ __forceinline__ void learned_phase(const T* v, int clo, int chi, T* U
                              0.0f, static_cast<float>(v[c + 1] - vc),
                              static_cast<float>(v[c + 2] - vc)};
         float cr, cl;
-        learned_cell32(f, ds, lp, cr, cl);
+        learned_cell32(f, ds, lp, scr, cr, cl);
         if (r < ncell) {
             UR[c] = vc + static_cast<T>(cr);
             UL[c] = vc + static_cast<T>(cl);
@@ -275,7 +290,9 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
         }
         __syncthreads();
     } else if constexpr (REC == SHK_REC_LEARNED) {
-        learned_phase<T>(v, lo - 1, hi + 1, sm.UL, sm.UR, p.lp);
+        // warp scratch: H onward (free in this phase; every learned layout
+        // leaves at least 1027 floats there, see learned_scratch)
+        learned_phase<T>(v, lo - 1, hi + 1, sm.UL, sm.UR, p.lp, learned_scratch(sm.H));
         __syncthreads();
     } else if constexpr (REC == SHK_REC_CONSTANT) {
         // reconstruction.py:153-163: ul = ur = u
@@ -440,7 +457,7 @@ __host__ __device__ inline DtState compute_dt(double smax, double cfl, double th
 // the double pipe then carries three operations per cell and step instead of
 // the whole operator. Layout (Smem::carve_mixed, or the full double layout):
 // U is the loaded double window, S holds the float window uf and the float
-// stage state, H the float cell differences and the increments.
+// stage state, I the increments.
 template <int EQ, int FLUX>
 __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* gout, int te,
                                               double dtdx, const OpParams<double>& p,
@@ -456,7 +473,7 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
     fs.Q = reinterpret_cast<float*>(sm.Q);
     fs.UL = reinterpret_cast<float*>(sm.UL);
     fs.UR = reinterpret_cast<float*>(sm.UR);
-    fs.I = fs.H + W;
+    fs.I = reinterpret_cast<float*>(sm.I);
     fs.W = W;
     float* inc = fs.I;
     const float dtf = static_cast<float>(dtdx);

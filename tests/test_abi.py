@@ -99,6 +99,14 @@ def test_plan_arguments_rejected_on_host(cdll):
             assert create([0, 64], [0.1], opts, chunks=chunks) == _lib.SHK_EINVAL, tile
         opts = _lib.ShkPlanOpts(dtype=7, tile=0, max_steps=0, ctas_per_sm=0)
         assert create([0, 64], [0.1], opts, chunks=chunks) == _lib.SHK_EINVAL  # dtype
+    # the learned reconstruction needs tiles of at least 512 cells
+    s_learned = _lib.ShkScheme(flux=0, rec=_lib.SHK_REC_LEARNED, equation=0, eps=1e-6, delta=0.0,
+                               nu=1.0, speed=1.0, mlp=1)
+    off = np.array([0, 4096], dtype=np.int64)
+    dxa = np.array([0.1])
+    opts = _lib.ShkPlanOpts(dtype=_lib.SHK_F64, tile=256, max_steps=0, ctas_per_sm=0)
+    assert cdll.shk_plan_create(s_learned, 1, off.ctypes.data, dxa.ctypes.data, dxa.ctypes.data,
+                                1.0, ctypes.byref(opts), ctypes.byref(out)) == _lib.SHK_EINVAL
     assert out.value is None
     # host steppers step forward only and take a non-negative chunk count
     opts = _lib.ShkPlanOpts(dtype=_lib.SHK_F64, tile=0, max_steps=10, ctas_per_sm=0)
