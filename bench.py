@@ -496,7 +496,7 @@ def bench_fp32(scheme, sizes, u0, stream, args) -> dict:
             "mass_drift_per_cell_max": {"float64": float(drift64), "float32": float(drift32)}}
 
 
-def _adjoint_rate(scheme, dev, nsteps, dtype, B=256, n=4096) -> dict:
+def _adjoint_rate(scheme, dev, nsteps, dtype, B=256, n=4096, tile="auto") -> dict:
     """B Burgers instances, N=4096, config-1 initial condition,
     J = 1/2 |u(T) - u_target|^2, sqrt(n)-checkpointed reverse sweep. One
     gradient = one instance's full dJ/du0."""
@@ -509,7 +509,7 @@ def _adjoint_rate(scheme, dev, nsteps, dtype, B=256, n=4096) -> dict:
     f = np.linspace(-1.0, 1.0, n + 1)
     u1 = 0.5 + (np.cos(np.pi * f[:-1]) - np.cos(np.pi * f[1:])) / (np.pi * (2.0 / n))
     u0 = torch.tensor(np.tile(u1, B), device=dev, dtype=dtype)
-    solver = BatchedSolver(scheme, [n] * B, 2.0 / n, max_steps=nsteps, dtype=dtype)
+    solver = BatchedSolver(scheme, [n] * B, 2.0 / n, max_steps=nsteps, dtype=dtype, tile=tile)
     cs = CheckpointedSolve(solver, nsteps)
     rng = np.random.default_rng(SEED + 3)
     pert = torch.tensor(rng.standard_normal(u0.numel()), device=dev, dtype=dtype)
@@ -527,7 +527,8 @@ def _adjoint_rate(scheme, dev, nsteps, dtype, B=256, n=4096) -> dict:
         raise RuntimeError("adjoint run failed")
     return {"metric": "adjoint grads/s", "value": B / (t2 - t0), "unit": "gradients/s",
             "config": {"batch": B, "n": n, "steps": nsteps, "checkpoint_stride": cs.stride,
-                       "dtype": str(dtype).replace("torch.", "")},
+                       "dtype": str(dtype).replace("torch.", ""),
+                       "launch_shape": {"tile": solver.tile, "ctas_per_sm": solver.ctas_per_sm}},
             "forward_s": t1 - t0, "reverse_s": t2 - t1,
             "adjoint_cell_steps_per_s": n * B * nsteps / (t2 - t1)}
 
@@ -536,7 +537,7 @@ def bench_adjoint(scheme, dev, args) -> dict:
     """The adjoint configuration in float64 (B=256, N=4096, 4000 steps)."""
     import torch
 
-    return _adjoint_rate(scheme, dev, args.adjoint_steps, torch.float64)
+    return _adjoint_rate(scheme, dev, args.adjoint_steps, torch.float64, tile=args.tile)
 
 
 def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
@@ -591,14 +592,17 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
            "learned_f64": l1(run(lscheme, n, torch.float64)),
            "learned_f32": l1(run(lscheme, n, torch.float32)),
            "untrained_f64": l1(run(uscheme, n, torch.float64))}
-    adj = {"learned_f64": _adjoint_rate(lscheme, dev, args.adjoint_steps, torch.float64),
-           "learned_f32": _adjoint_rate(lscheme, dev, args.adjoint_steps, torch.float32)}
+    adj = {"learned_f64": _adjoint_rate(lscheme, dev, args.adjoint_steps, torch.float64, tile=args.tile),
+           "learned_f32": _adjoint_rate(lscheme, dev, args.adjoint_steps, torch.float32, tile=args.tile)}
     return {
         "forward": {"unit": "cell-steps/s", "config": {"batch": B, "n": n, "steps": k},
                     "launch_shapes": shapes, **rates,
                     "speedup_learned_f64": rates["learned_f64"] / rates["plain_f64"],
                     "speedup_learned_f32": rates["learned_f32"] / rates["plain_f64"]},
         "adjoint": {"unit": "gradients/s", "plain_f64": adjoint_plain["value"],
+                    "launch_shapes": {"plain_f64": adjoint_plain["config"]["launch_shape"],
+                                      "learned_f64": adj["learned_f64"]["config"]["launch_shape"],
+                                      "learned_f32": adj["learned_f32"]["config"]["launch_shape"]},
                     "learned_f64": adj["learned_f64"]["value"],
                     "learned_f32": adj["learned_f32"]["value"],
                     "speedup_learned_f64": adj["learned_f64"]["value"] / adjoint_plain["value"],
@@ -662,7 +666,7 @@ def profile_adjoint(args) -> None:
     else:
         sch = gb.burgers.Rusanov(rec=learned.LearnedWENO(params=learned.load_default_params(device=dev)))
     dtype = torch.float32 if args.scheme.endswith("32") else torch.float64
-    r = _adjoint_rate(sch, dev, args.adjoint_steps, dtype, B=args.batch)
+    r = _adjoint_rate(sch, dev, args.adjoint_steps, dtype, B=args.batch, tile=args.tile)
     print(json.dumps({"profile_adjoint": args.scheme, **r}), flush=True)
 
 

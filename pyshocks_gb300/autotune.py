@@ -38,7 +38,7 @@ _MEMO: dict[str, "TuneResult"] = {}
 class TuneResult:
     tile: int
     ctas_per_sm: int
-    ms_per_step: float
+    ms_per_step: float  # forward step, or forward + reverse step for adjoint plans
     table: list = field(default_factory=list)  # (tile, ctas_per_sm, ms) of every candidate
 
 
@@ -126,8 +126,10 @@ def tune(scheme, sizes: Sequence[int], dx, *, dtype: torch.dtype = torch.float64
          device="cuda", use_cache: bool = True, adjoint: bool = False) -> TuneResult:
     """Time every candidate shape on this batch and return the fastest.
 
-    :arg adjoint: keep to tiles the reverse step can run (plans that record a
-        dt history for the adjoint).
+    :arg adjoint: keep to tiles the reverse step can run and time a short
+        checkpointed forward solve plus its reverse sweep instead of forward
+        steps (plans that record a dt history for the adjoint, whose reverse
+        step dominates and prefers other shapes than the forward).
 
     :arg u0: packed state to step from (default: a smooth state of O(1)
         values); the step cost does not depend on the data except through the
@@ -155,17 +157,30 @@ def tune(scheme, sizes: Sequence[int], dx, *, dtype: torch.dtype = torch.float64
     learned = type(getattr(scheme, "rec", None)).__name__ == "LearnedWENO"
     weno5 = type(getattr(scheme, "rec", None)).__name__ == "WENOJS53"
     for tile, cps in candidates(dtype, int(sizes.max()), learned, adjoint, weno5):
+        if learned and tile < 512:
+            continue  # the learned phase's warp scratch needs 512-cell tiles
         solver = BatchedSolver(scheme, sizes, dx, theta=theta, dtype=dtype, tile=tile,
-                               ctas_per_sm=cps, device=device)
+                               ctas_per_sm=cps, device=device, max_steps=k if adjoint else 0)
         with torch.cuda.stream(stream):
-            solver.reset(u0)
-            solver.step(2, graph=True)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            solver.step(k, graph=True)
-            e1.record(stream)
-            e1.synchronize()
+            if adjoint:
+                from pyshocks_gb300.adjoint import CheckpointedSolve
+
+                cs = CheckpointedSolve(solver, k)
+                cs.backward(cs.forward(u0))  # warm-up
+                e0.record(stream)
+                cs.backward(cs.forward(u0))
+                e1.record(stream)
+                e1.synchronize()
+                del cs
+            else:
+                solver.reset(u0)
+                solver.step(2, graph=True)
+                e0.record(stream)
+                solver.step(k, graph=True)
+                e1.record(stream)
+                e1.synchronize()
         if solver.status() == 0:
             table.append((tile, cps, e0.elapsed_time(e1) / k))
         del solver

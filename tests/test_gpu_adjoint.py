@@ -188,3 +188,40 @@ def test_autograd_function_backward():
                                    2.0 / n, nsteps, dts=solver.dt_history().cpu())
     err = (u0.grad.cpu() - ref[0]).abs().max() / ref.abs().max()
     assert float(err) < 1.0e-9
+
+
+def test_config3_size_gradient_16_directions():
+    """The adjoint configuration's check at its instance size (N = 4096): dJ/du0
+    along 16 random directions against central differences (h = 1e-6) of the
+    GPU forward itself, replaying the recorded dt sequence (frozen dt, as
+    adjoint_step), with J = 1/2 |u(T) - u_target|^2 and sqrt(n) checkpoints."""
+    from pyshocks_gb300.adjoint import CheckpointedSolve
+    from pyshocks_gb300.batched import BatchedSolver
+
+    n, nsteps, B = 4096, 400, 2
+    rng = np.random.default_rng(31)
+    u1 = R.exact_cell_average_sine(R.make_uniform_cell_grid(-1, 1, n, 3))[3:-3]
+    u0 = np.tile(u1, B)
+    x = np.linspace(-1.0, 1.0, n + 1)[:-1]
+    pert = np.concatenate([sum(rng.standard_normal() / k**2 * np.sin(k * np.pi * x + rng.uniform(0, 2 * np.pi))
+                               for k in range(1, 9)) for _ in range(B)])
+    scheme = _scheme()
+    solver = BatchedSolver(scheme, [n] * B, 2.0 / n, max_steps=nsteps)
+    cs = CheckpointedSolve(solver, nsteps)
+    target = cs.forward(torch.tensor(u0 + 0.05 * pert)).clone()
+    uT = cs.forward(torch.tensor(u0))
+    grad = cs.backward(uT - target).cpu().numpy()
+    replay = BatchedSolver(scheme, [n] * B, 2.0 / n)
+    replay.set_fixed_dt(solver.dt_history())
+
+    def J(u):
+        replay.reset(torch.tensor(u))
+        replay.step(nsteps)
+        return 0.5 * float(torch.sum((replay.u - target) ** 2))
+
+    h = 1.0e-6
+    for k in range(16):
+        v = rng.standard_normal(u0.size)
+        fd = (J(u0 + h * v) - J(u0 - h * v)) / (2 * h)
+        ad = float(np.dot(grad, v))
+        assert abs(fd - ad) <= 1.0e-5 * max(1.0, abs(ad)), (k, fd, ad)
