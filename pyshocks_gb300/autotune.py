@@ -71,12 +71,12 @@ def _smem_bytes(tile: int, dtype: torch.dtype, learned: bool = False, weno5: boo
 
 
 def _adjoint_smem_bytes(tile: int, dtype: torch.dtype, learned: bool = False) -> int:
-    # the reverse step: 20 windows (halo 20) of the state type, or for float64
+    # the reverse step: 24 windows (halo 20) of the state type, or for float64
     # with the learned reconstruction 22 float windows
     w = tile + 40
     if dtype == torch.float64:
-        return w * (22 * 4 if learned else 20 * 8)
-    return w * 20 * 4
+        return w * (22 * 4 if learned else 24 * 8)
+    return w * 24 * 4
 
 
 def candidates(dtype: torch.dtype, max_cells: int, learned: bool = False,

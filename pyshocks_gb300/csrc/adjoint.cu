@@ -38,7 +38,7 @@ namespace shk {
 constexpr int kAdjTile = 512;
 template <class T> __host__ __device__ constexpr int adj_uhalo() { return 20; }  // 18 needed
 template <class T> __host__ __device__ constexpr int adj_phalo() { return sizeof(T) == 8 ? 10 : 12; }  // 9 needed
-constexpr int kAdjArrays = 20;
+constexpr int kAdjArrays = 24;
 
 template <class T>
 struct AdjSmem {
@@ -46,20 +46,24 @@ struct AdjSmem {
     T *H, *D, *Q, *UL, *UR;
     T *GL, *GR, *GA;
     T *T0, *T1, *T2, *T3, *T4;
+    T *CLu, *CRu, *CL1, *CR1;  // face values of u and k1 from the forward recompute
     int W;  // window length (cells) of every array
 
     __host__ static size_t host_bytes(int W) { return size_t(kAdjArrays) * W * sizeof(T); }
     __device__ void carve(unsigned char* base, int W) {
         T* p = reinterpret_cast<T*>(base);
         T** slots[kAdjArrays] = {&U, &K1, &K2, &PB, &CB, &Z, &ACC, &H, &D, &Q,
-                                 &UL, &UR, &GL, &GR, &GA, &T0, &T1, &T2, &T3, &T4};
+                                 &UL, &UR, &GL, &GR, &GA, &T0, &T1, &T2, &T3, &T4,
+                                 &CLu, &CRu, &CL1, &CR1};
         for (int i = 0; i < kAdjArrays; ++i) *slots[i] = p + size_t(i) * W;
         this->W = W;
     }
-    // forward-stage view (face_fluxes writes the face fluxes into D)
-    __device__ Smem<T> fwd(T* state_out) const {
+    // forward-stage view (face_fluxes writes the face fluxes into D and the
+    // face values into ul, ur: UL, UR unless given)
+    __device__ Smem<T> fwd(T* state_out, T* ul = nullptr, T* ur = nullptr) const {
         Smem<T> s;
-        s.U = U; s.S = state_out; s.H = H; s.D = D; s.Q = Q; s.UL = UL; s.UR = UR;
+        s.U = U; s.S = state_out; s.H = H; s.D = D; s.Q = Q;
+        s.UL = ul ? ul : UL; s.UR = ur ? ur : UR;
         s.W = W;
         return s;
     }
@@ -177,9 +181,12 @@ __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1
 
 // z_i = dt (J_L(v)^T w)_i for i in [lo, hi); v valid on [lo-6, hi+6), w on
 // [lo-3, hi+3). Rusanov flux, WENO-JS5 or learned reconstruction.
+// cul, cur: the face values of v on [lo-3, hi+3) when the forward recompute
+// kept them (WENO-JS5; null: reconstructed here)
 template <class T, int EQ, int REC>
 __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const AdjSmem<T>& a,
-                          const OpParams<T>& p, T dtdx) {
+                          const OpParams<T>& p, T dtdx, const T* cul = nullptr,
+                          const T* cur = nullptr) {
     const int tid = threadIdx.x, nt = blockDim.x;
     if constexpr (REC == SHK_REC_LEARNED) {
         static_assert(sizeof(T) == 4, "the learned VJP runs on float stage states");
@@ -245,18 +252,24 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
         a.Q[c] = (T(13.0 / 3.0) * d) * d;
     }
     __syncthreads();
-    for (int c = lo - 3 + tid; c < hi + 3; c += nt) {
-        T ul, ur;
-        weno53_cell<T>(v[c], a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
-                       a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, ul, ur);
-        a.UL[c] = ul;
-        a.UR[c] = ur;
+    const T* UL = cul;
+    const T* UR = cur;
+    if (!cul) {
+        for (int c = lo - 3 + tid; c < hi + 3; c += nt) {
+            T ul, ur;
+            weno53_cell<T>(v[c], a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
+                           a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, ul, ur);
+            a.UL[c] = ul;
+            a.UR[c] = ur;
+        }
+        __syncthreads();
+        UL = a.UL;
+        UR = a.UR;
     }
-    __syncthreads();
     // face j+1/2: F = 1/2 (f(L) + f(R)) - nu/2 a (L - R), L = ul_{j+1}, R = ur_j
     for (int j = lo - 3 + tid; j < hi + 2; j += nt) {
         const T fb = (w[j + 1] - w[j]) * dtdx;
-        const T L = a.UL[j + 1], R = a.UR[j];
+        const T L = UL[j + 1], R = UR[j];
         const T ha = p.hnu * absmax(wave_speed<EQ>(v[j], p.c), wave_speed<EQ>(v[j + 1], p.c));
         a.GL[j] = fb * fma(T(0.5), flux_prime<EQ>(L, p.c), -ha);
         a.GR[j] = fb * fma(T(0.5), flux_prime<EQ>(R, p.c), ha);
@@ -379,7 +392,7 @@ template <class T, int EQ, int REC>
 __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const OpParams<T>& p,
                              const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0) {
     if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED) {
-        // full double layout: the float arrays fit from CB on (20 in 16 double ones)
+        // full double layout: the float arrays fit from CB on (24 in 20 double ones)
         AdjSmem<float> af;
         af.carve(reinterpret_cast<unsigned char*>(a.CB), a.W);
         adjoint_tile_mixed<EQ>(a, af, gout, te, dtdx, p, bc, g0, n);
@@ -392,13 +405,19 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
         zero_outside(a.PB, g0, n, HU0 - HP0, HU0 + te + HP0);
     }
     constexpr int HU = adj_uhalo<T>();
+    // the forward recompute's face values of u and k1 serve reverse stages 1
+    // and 2 (they cover [HU-16, HU+te+16) and [HU-13, HU+te+13), the stages
+    // read [HU-6, HU+te+6)); the face values of k2 are reconstructed there
+    constexpr bool kCache = REC == SHK_REC_WENOJS53;
     const int tid = threadIdx.x, nt = blockDim.x;
     const T fdt = dtdx * p.fscale;  // face fluxes are stored as F / fscale
     // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12),
     // with the forward step's own formulas (increments about u for float)
     {
         const int lo = HU - 15, hi = HU + te + 15;
-        face_fluxes<T, EQ, REC, SHK_FLUX_RUSANOV>(a.U, lo, hi, a.fwd(a.K1), p);
+        // WENO-JS5: the face values of u stay in CLu/CRu for reverse stage 1
+        face_fluxes<T, EQ, REC, SHK_FLUX_RUSANOV>(a.U, lo, hi, kCache ? a.fwd(a.K1, a.CLu, a.CRu)
+                                                                      : a.fwd(a.K1), p);
         for (int i = lo + tid; i < hi; i += nt) {
             if constexpr (sizeof(T) == 4) {
                 const T d = fdt * (a.D[i - 1] - a.D[i]);
@@ -413,7 +432,9 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     }
     {
         const int lo = HU - 12, hi = HU + te + 12;
-        face_fluxes<T, EQ, REC, SHK_FLUX_RUSANOV>(a.K1, lo, hi, a.fwd(a.K2), p);
+        // and those of k1 in CL1/CR1 for reverse stage 2
+        face_fluxes<T, EQ, REC, SHK_FLUX_RUSANOV>(a.K1, lo, hi, kCache ? a.fwd(a.K2, a.CL1, a.CR1)
+                                                                       : a.fwd(a.K2), p);
         for (int i = lo + tid; i < hi; i += nt) {
             if constexpr (sizeof(T) == 4) {
                 a.K2[i] = a.U[i] + T(0.25) * (a.T0[i] + fdt * (a.D[i - 1] - a.D[i]));
@@ -439,7 +460,8 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     // reverse stage 2: k1b = 1/4 (k2b + dt J(k1)^T k2b) on [HU-3, HU+te+3)
     {
         const int lo = HU - 3, hi = HU + te + 3;
-        vjp_stage<T, EQ, REC>(a.K1, a.CB, a.Z, lo, hi, a, p, dtdx);
+        vjp_stage<T, EQ, REC>(a.K1, a.CB, a.Z, lo, hi, a, p, dtdx, kCache ? a.CL1 : nullptr,
+                              kCache ? a.CR1 : nullptr);
         if (np) bc_transpose(a.Z, g0, n, lo, hi, bc);
         for (int i = lo + tid; i < hi; i += nt) a.CB[i] = T(1.0 / 4.0) * (a.CB[i] + a.Z[i]);
         __syncthreads();
@@ -457,7 +479,8 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
             if (g0 + HU == 0) lo -= 3;
             if (g0 + HU + te == n) hi += 3;
         }
-        vjp_stage<T, EQ, REC>(a.U, a.CB, a.Z, lo, hi, a, p, dtdx);
+        vjp_stage<T, EQ, REC>(a.U, a.CB, a.Z, lo, hi, a, p, dtdx, kCache ? a.CLu : nullptr,
+                              kCache ? a.CRu : nullptr);
         if (np) bc_transpose(a.Z, g0, n, lo, hi, bc);
         for (int i = HU + tid; i < HU + te; i += nt) gout[i - HU] = a.ACC[i] + (a.CB[i] + a.Z[i]);
     }
@@ -806,7 +829,7 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
                                : (dtype == SHK_F64 ? AdjSmem<double>::host_bytes(W)
                                                    : AdjSmem<float>::host_bytes(W));
     {
-        // the reverse step keeps ~20 windows of the tile in shared memory: plans
+        // the reverse step keeps ~24 windows of the tile in shared memory: plans
         // with longer tiles can step forward but not run the adjoint
         int dev0 = 0, optin = 0;
         cudaGetDevice(&dev0);
