@@ -280,6 +280,16 @@ int shk_plan_forward_checkpointed(shk_plan* plan, void* u_a, void* u_b, int32_t 
 int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t nsteps,
                      void* seg, void* p_a, void* p_b, void* stream);
 
+/* shk_plan_adjoint with stage storage (learned reconstruction only): the
+ * segment replay also writes each step's float stage states k1 and k2 into
+ * `stages` (caller-owned, stride x *nfloats floats, *nfloats from
+ * shk_plan_adjoint_stage_floats: 2 x the plan's cells, 0 for schemes without
+ * stage storage), and every reverse step reads them instead of recomputing
+ * its two forward stages. Same result, bit for bit, as shk_plan_adjoint. */
+int shk_plan_adjoint_stage_floats(shk_plan* plan, int64_t* nfloats);
+int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, int32_t nsteps,
+                            void* seg, void* stages, void* p_a, void* p_b, void* stream);
+
 /* FP64 reductions over the batch (grid.py:444-506, conservation checks):
  * out[b] = sum_i u_b[i] (p = 0), sum |u_b[i]| (p = 1) or max |u_b[i]| (p = -1),
  * accumulated in double for either state precision. */

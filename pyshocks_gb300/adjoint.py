@@ -36,9 +36,13 @@ class CheckpointedSolve:
     :arg solver: a :class:`BatchedSolver` created with ``max_steps >= nsteps``.
     :arg nsteps: number of SSPRK33 steps of the forward run.
     :arg stride: checkpoint interval (default ``ceil(sqrt(nsteps))``).
+    :arg store_stages: with the learned reconstruction, keep each replayed
+        step's float stage states (``stride x 2 x cells`` floats) so that the
+        reverse steps skip their two forward stages (same result, bit for bit).
     """
 
-    def __init__(self, solver: BatchedSolver, nsteps: int, stride: int | None = None):
+    def __init__(self, solver: BatchedSolver, nsteps: int, stride: int | None = None,
+                 store_stages: bool = True):
         if solver.max_steps < nsteps:
             raise ValueError("the solver's dt history must hold every step (max_steps >= nsteps)")
         self.solver = solver
@@ -50,6 +54,11 @@ class CheckpointedSolve:
         self.seg = torch.empty((self.stride, solver.total), dtype=dt, device=dev)
         self.p_a = torch.empty(solver.total, dtype=dt, device=dev)
         self.p_b = torch.empty(solver.total, dtype=dt, device=dev)
+        nf = ctypes.c_int64(0)
+        L.check(solver.lib.shk_plan_adjoint_stage_floats(solver._plan, ctypes.byref(nf)),
+                "plan_adjoint_stage_floats")
+        self.stages = (torch.empty((self.stride, nf.value), dtype=torch.float32, device=dev)
+                       if store_stages and nf.value > 0 else None)
 
     def forward(self, u0: torch.Tensor, *, t0=None, tfinal=None) -> torch.Tensor:
         """Run the forward solve from *u0*; returns the final packed state."""
@@ -69,9 +78,10 @@ class CheckpointedSolve:
         s = self.solver
         self.p_a.copy_(p_final.reshape(-1).to(self.p_a))
         L.check(
-            s.lib.shk_plan_adjoint(
+            s.lib.shk_plan_adjoint_staged(
                 s._plan, self.ckpt.data_ptr(), self.stride, self.nsteps, self.seg.data_ptr(),
-                self.p_a.data_ptr(), self.p_b.data_ptr(), L.stream_handle()),
+                L.ptr(self.stages), self.p_a.data_ptr(), self.p_b.data_ptr(),
+                L.stream_handle()),
             "plan_adjoint",
         )
         return (self.p_a if self.nsteps % 2 == 0 else self.p_b).clone()

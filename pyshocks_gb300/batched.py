@@ -262,7 +262,8 @@ class BatchedSolver:
         on neither). *dirichlet*: ghost values ``(B, 2, 3)`` (side, then the
         ghost next to the interior first), or ``(2,)`` per side for all
         ghosts and instances; *neumann*: gradients ``(B, 2)`` or ``(2,)``.
-        Plans with non-periodic boundaries step forward only."""
+        The adjoint of such a plan is the exact transpose with the boundary
+        data as constants."""
         kinds = {"periodic": L.SHK_BC_PERIODIC, "dirichlet": L.SHK_BC_DIRICHLET,
                  "neumann": L.SHK_BC_NEUMANN}
         right = left if right is None else right

@@ -294,6 +294,17 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
     __syncthreads();
 }
 
+// window positions [lo, hi) of a float stage state stored per instance cell
+// (position i is cell g0 + i, periodically)
+__device__ __forceinline__ void load_stage(float* dst, const float* src, int64_t n, int64_t g0,
+                                           int lo, int hi) {
+    const bool once = g0 + lo >= -n && g0 + hi <= 2 * n;
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        const int64_t pos = g0 + i;
+        dst[i] = src[once ? (pos < 0 ? pos + n : (pos >= n ? pos - n : pos)) : imod(pos, n)];
+    }
+}
+
 // Adjoint step of the mixed-precision learned step (step_tile_mixed): the
 // forward stages are recomputed exactly as that step computes them (float
 // operator on float stage states, increments about u), the three reverse
@@ -303,10 +314,13 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
 // increment to the double p once. Of the double arrays only the loaded windows
 // a.U and a.PB are read; af holds the float arrays (af.K1, af.K2 may overlay
 // a.U, which is dead once af.U is written).
+// k1g, k2g (optional): the instance's stored float stage states (replay with
+// stage outputs), which replace the recompute of k1 and k2 bit for bit.
 template <int EQ>
 __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float>& af, double* gout,
                                    int te, double dtdx, const OpParams<double>& p,
-                                   const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0) {
+                                   const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0,
+                                   const float* k1g = nullptr, const float* k2g = nullptr) {
     constexpr int HU = adj_uhalo<double>(), HP = adj_phalo<double>();
     constexpr int REC = SHK_REC_LEARNED;
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -320,27 +334,38 @@ __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float
         apply_bc(af.U, g0, n, 0, te + 2 * HU, bc, 0);
         zero_outside(af.PB, g0, n, HU - HP, HU + te + HP);
     }
-    // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12)
-    {
-        const int lo = HU - 15, hi = HU + te + 15;
-        face_fluxes<float, EQ, REC, SHK_FLUX_RUSANOV>(af.U, lo, hi, af.fwd(af.K1), pf);
-        for (int i = lo + tid; i < hi; i += nt) {
-            const float d = dtf * (af.D[i - 1] - af.D[i]);
-            af.T0[i] = d;
-            af.K1[i] = af.U[i] + d;
-        }
+    // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12), or
+    // the stored stage states there
+    if (k1g) {
+        load_stage(af.K1, k1g, n, g0, HU - 15, HU + te + 15);
+        load_stage(af.K2, k2g, n, g0, HU - 12, HU + te + 12);
         __syncthreads();
-        if (np) apply_bc(af.K1, g0, n, lo, hi, bc, 1);
-    }
-    {
-        const int lo = HU - 12, hi = HU + te + 12;
-        face_fluxes<float, EQ, REC, SHK_FLUX_RUSANOV>(af.K1, lo, hi, af.fwd(af.K2), pf);
-        for (int i = lo + tid; i < hi; i += nt) {
-            const float d = 0.25f * (af.T0[i] + dtf * (af.D[i - 1] - af.D[i]));
-            af.K2[i] = af.U[i] + d;
+        if (np) {
+            apply_bc(af.K1, g0, n, HU - 15, HU + te + 15, bc, 1);
+            apply_bc(af.K2, g0, n, HU - 12, HU + te + 12, bc, 2);
         }
-        __syncthreads();
-        if (np) apply_bc(af.K2, g0, n, lo, hi, bc, 2);
+    } else {
+        {
+            const int lo = HU - 15, hi = HU + te + 15;
+            face_fluxes<float, EQ, REC, SHK_FLUX_RUSANOV>(af.U, lo, hi, af.fwd(af.K1), pf);
+            for (int i = lo + tid; i < hi; i += nt) {
+                const float d = dtf * (af.D[i - 1] - af.D[i]);
+                af.T0[i] = d;
+                af.K1[i] = af.U[i] + d;
+            }
+            __syncthreads();
+            if (np) apply_bc(af.K1, g0, n, lo, hi, bc, 1);
+        }
+        {
+            const int lo = HU - 12, hi = HU + te + 12;
+            face_fluxes<float, EQ, REC, SHK_FLUX_RUSANOV>(af.K1, lo, hi, af.fwd(af.K2), pf);
+            for (int i = lo + tid; i < hi; i += nt) {
+                const float d = 0.25f * (af.T0[i] + dtf * (af.D[i - 1] - af.D[i]));
+                af.K2[i] = af.U[i] + d;
+            }
+            __syncthreads();
+            if (np) apply_bc(af.K2, g0, n, lo, hi, bc, 2);
+        }
     }
     // reverse stage 3: k2b = 2/3 (p + Z3), Z3 = dt J(k2)^T p
     {
@@ -390,14 +415,18 @@ __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float
 // cotangents reach the interior through the Neumann mirrors).
 template <class T, int EQ, int REC>
 __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const OpParams<T>& p,
-                             const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0) {
+                             const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0,
+                             const float* k1g = nullptr, const float* k2g = nullptr) {
     if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED) {
         // full double layout: the float arrays fit from CB on (24 in 20 double ones)
         AdjSmem<float> af;
         af.carve(reinterpret_cast<unsigned char*>(a.CB), a.W);
-        adjoint_tile_mixed<EQ>(a, af, gout, te, dtdx, p, bc, g0, n);
+        adjoint_tile_mixed<EQ>(a, af, gout, te, dtdx, p, bc, g0, n, k1g, k2g);
         return;
     }
+    // stored float stage states (learned reconstruction, float state) replace
+    // the recompute of k1 and k2 bit for bit
+    constexpr bool kStored = sizeof(T) == 4 && REC == SHK_REC_LEARNED;
     const bool np = !bc.periodic();
     if (np) {
         constexpr int HU0 = adj_uhalo<T>(), HP0 = adj_phalo<T>();
@@ -413,6 +442,18 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     const T fdt = dtdx * p.fscale;  // face fluxes are stored as F / fscale
     // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12),
     // with the forward step's own formulas (increments about u for float)
+    if constexpr (kStored) {
+        if (k1g) {
+            load_stage(reinterpret_cast<float*>(a.K1), k1g, n, g0, HU - 15, HU + te + 15);
+            load_stage(reinterpret_cast<float*>(a.K2), k2g, n, g0, HU - 12, HU + te + 12);
+            __syncthreads();
+            if (np) {
+                apply_bc(a.K1, g0, n, HU - 15, HU + te + 15, bc, 1);
+                apply_bc(a.K2, g0, n, HU - 12, HU + te + 12, bc, 2);
+            }
+        }
+    }
+    if (!kStored || !k1g) {
     {
         const int lo = HU - 15, hi = HU + te + 15;
         // WENO-JS5: the face values of u stay in CLu/CRu for reverse stage 1
@@ -445,6 +486,7 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
         }
         __syncthreads();
         if (np) apply_bc(a.K2, g0, n, lo, hi, bc, 2);
+    }
     }
     // reverse stage 3: k2b = 2/3 (p + dt J(k2)^T p) on [HU-6, HU+te+6)
     {
@@ -521,7 +563,9 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
                                                                    const T* __restrict__ pnext,
                                                                    T* __restrict__ pout,
                                                                    const double* __restrict__ dt_row,
-                                                                   OpParams<T> p) {
+                                                                   OpParams<T> p,
+                                                                   const float* __restrict__ k1s,
+                                                                   const float* __restrict__ k2s) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     constexpr bool kMixed = sizeof(T) == 8 && REC == SHK_REC_LEARNED;
@@ -555,8 +599,10 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
         const BcView bc = plan_bc(P, b);
         const int64_t g0 = s0 - adj_uhalo<T>();
-        if constexpr (kMixed) adjoint_tile_mixed<EQ>(a, af, pout + off + s0, te, dtdx, p, bc, g0, n);
-        else adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p, bc, g0, n);
+        const float* k1g = k1s ? k1s + off : nullptr;
+        const float* k2g = k2s ? k2s + off : nullptr;
+        if constexpr (kMixed) adjoint_tile_mixed<EQ>(a, af, pout + off + s0, te, dtdx, p, bc, g0, n, k1g, k2g);
+        else adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p, bc, g0, n, k1g, k2g);
         __syncthreads();
     }
     finish_items(P, 2);
@@ -564,11 +610,13 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
 
 // forward step with a recorded dt (no CFL, no time update): recompute of the
 // states between checkpoints
+// k1s, k2s (optional, float or mixed steps): the stage states of each step
+// for a reverse step that skips their recompute; uout may then be null.
 template <class T, int EQ, int REC>
 __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) replay_step_kernel(PlanDev P, const T* __restrict__ uin,
                                                                T* __restrict__ uout,
                                                                const double* __restrict__ dt_row,
-                                                               OpParams<T> p) {
+                                                               OpParams<T> p, float* k1s, float* k2s) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     constexpr int HL = step_halo<T>();
@@ -588,8 +636,9 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
         const int64_t s0 = int64_t(P.item_tile[item]) * P.tile;
         const int te = static_cast<int>(imin64(P.tile, n - s0));
         const double dt = dt_row[b];
-        if (dt == 0.0) {
-            for (int i = threadIdx.x; i < te; i += blockDim.x) uout[off + s0 + i] = uin[off + s0 + i];
+        if (dt == 0.0) {  // no step: the reverse step is the identity, stage states unused
+            if (uout)
+                for (int i = threadIdx.x; i < te; i += blockDim.x) uout[off + s0 + i] = uin[off + s0 + i];
             __syncthreads();
             continue;
         }
@@ -598,8 +647,10 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
             break;
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
-        step_tile<T, EQ, REC, SHK_FLUX_RUSANOV>(sm, uout + off + s0, te, dtdx, p, plan_bc(P, b),
-                                                s0 - HL, n);
+        step_tile<T, EQ, REC, SHK_FLUX_RUSANOV>(sm, uout ? uout + off + s0 : nullptr, te, dtdx, p,
+                                                plan_bc(P, b), s0 - HL, n,
+                                                k1s ? k1s + off + s0 : nullptr,
+                                                k2s ? k2s + off + s0 : nullptr);
         __syncthreads();
     }
     finish_items(P, 4);
@@ -716,12 +767,12 @@ int by_equation(int eq, F&& f) {
 template <class TS>
 struct AdjLaunch {
     PlanDev D; const void* um; const void* pn; void* po; const double* dt_row; OpParams<TS> p;
-    size_t smem; int grid; cudaStream_t st;
+    size_t smem; int grid; cudaStream_t st; const float* k1s = nullptr; const float* k2s = nullptr;
     template <class T, int EQ, int REC> int operator()() {
         auto k = batched_adjoint_kernel<T, EQ, REC>;
         ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(um), static_cast<const T*>(pn),
-                                         static_cast<T*>(po), dt_row, p);
+                                         static_cast<T*>(po), dt_row, p, k1s, k2s);
         return acuda(cudaGetLastError());
     }
 };
@@ -729,11 +780,12 @@ struct AdjLaunch {
 template <class TS>
 struct ReplayLaunch {
     PlanDev D; const void* uin; void* uout; const double* dt_row; OpParams<TS> p;
-    size_t smem; int grid; cudaStream_t st;
+    size_t smem; int grid; cudaStream_t st; float* k1s = nullptr; float* k2s = nullptr;
     template <class T, int EQ, int REC> int operator()() {
         auto k = replay_step_kernel<T, EQ, REC>;
         ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(uin), static_cast<T*>(uout), dt_row, p);
+        k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(uin), static_cast<T*>(uout), dt_row, p,
+                                         k1s, k2s);
         return acuda(cudaGetLastError());
     }
 };
@@ -810,6 +862,23 @@ int shk_plan_forward_checkpointed(shk_plan* plan, void* u_a, void* u_b, int32_t 
 
 int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t nsteps, void* seg,
                      void* p_a, void* p_b, void* stream) {
+    return shk_plan_adjoint_staged(plan, ckpt, stride, nsteps, seg, nullptr, p_a, p_b, stream);
+}
+
+int shk_plan_adjoint_stage_floats(shk_plan* plan, int64_t* nfloats) {
+    PlanDev D;
+    int dtype = 0, grid = 0;
+    shk_scheme sch;
+    int64_t total = 0;
+    if (!plan || !nfloats) return SHK_EINVAL;
+    int r = plan_view(plan, &D, &dtype, &grid, &sch, &total, nullptr);
+    if (r != SHK_OK) return r;
+    *nfloats = sch.rec == SHK_REC_LEARNED ? 2 * total : 0;
+    return SHK_OK;
+}
+
+int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, int32_t nsteps,
+                            void* seg, void* stages, void* p_a, void* p_b, void* stream) {
     PlanDev D;
     int dtype = 0, grid = 0;
     shk_scheme sch;
@@ -819,6 +888,7 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
     int r = plan_view(plan, &D, &dtype, &grid, &sch, &total, nullptr);
     if (r != SHK_OK) return r;
     if (!adjoint_supported(&sch)) return SHK_EUNSUPPORTED;
+    if (stages && sch.rec != SHK_REC_LEARNED) return SHK_EINVAL;  // float stage states only
     if (!D.dt_hist || D.max_steps < nsteps) return SHK_EINVAL;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const size_t esz = dtype == SHK_F64 ? 8 : 4;
@@ -845,6 +915,13 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
     const int per_sm = std::max(1, static_cast<int>((220 * 1024) / std::max<size_t>(asmem, 1)));
     const int agrid = std::max(1, std::min(D.nitems, per_sm * sms));
     auto seg_at = [&](int j) { return static_cast<char*>(seg) + size_t(j) * bytes; };
+    // stage states of segment step j: k1 then k2, `total` floats each
+    auto k1_at = [&](int j) {
+        return stages ? static_cast<float*>(stages) + size_t(2 * j) * total : nullptr;
+    };
+    auto k2_at = [&](int j) {
+        return stages ? static_cast<float*>(stages) + size_t(2 * j + 1) * total : nullptr;
+    };
     const int nseg = (nsteps + stride - 1) / stride;
     void* cur = p_a;
     void* nxt = p_b;
@@ -853,13 +930,18 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
         const int cnt = std::min(stride, nsteps - base);
         ADJ_CUDA(cudaMemcpyAsync(seg_at(0), static_cast<const char*>(ckpt) + size_t(sgi) * bytes,
                                  bytes, cudaMemcpyDeviceToDevice, st));
-        for (int j = 1; j < cnt; ++j) {
+        // replay: the states u_1 .. u_{cnt-1} of the segment and, with stage
+        // storage, the stage states of every step (the last step's without u_out)
+        for (int j = 1; j < cnt + (stages ? 1 : 0); ++j) {
             const double* row = D.dt_hist + size_t(base + j - 1) * D.B;
+            void* out = j < cnt ? seg_at(j) : nullptr;
             if (dtype == SHK_F64) {
-                ReplayLaunch<double> f{D, seg_at(j - 1), seg_at(j), row, adj_params<double>(&sch), fsmem, grid, st};
+                ReplayLaunch<double> f{D, seg_at(j - 1), out, row, adj_params<double>(&sch), fsmem, grid, st,
+                                       k1_at(j - 1), k2_at(j - 1)};
                 r = by_scheme<double>(sch, f);
             } else {
-                ReplayLaunch<float> f{D, seg_at(j - 1), seg_at(j), row, adj_params<float>(&sch), fsmem, grid, st};
+                ReplayLaunch<float> f{D, seg_at(j - 1), out, row, adj_params<float>(&sch), fsmem, grid, st,
+                                      k1_at(j - 1), k2_at(j - 1)};
                 r = by_scheme<float>(sch, f);
             }
             if (r != SHK_OK) return r;
@@ -867,10 +949,12 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
         for (int j = cnt - 1; j >= 0; --j) {
             const double* row = D.dt_hist + size_t(base + j) * D.B;
             if (dtype == SHK_F64) {
-                AdjLaunch<double> f{D, seg_at(j), cur, nxt, row, adj_params<double>(&sch), asmem, agrid, st};
+                AdjLaunch<double> f{D, seg_at(j), cur, nxt, row, adj_params<double>(&sch), asmem, agrid, st,
+                                    k1_at(j), k2_at(j)};
                 r = by_scheme<double>(sch, f);
             } else {
-                AdjLaunch<float> f{D, seg_at(j), cur, nxt, row, adj_params<float>(&sch), asmem, agrid, st};
+                AdjLaunch<float> f{D, seg_at(j), cur, nxt, row, adj_params<float>(&sch), asmem, agrid, st,
+                                   k1_at(j), k2_at(j)};
                 r = by_scheme<float>(sch, f);
             }
             if (r != SHK_OK) return r;

@@ -458,10 +458,14 @@ __host__ __device__ inline DtState compute_dt(double smax, double cfl, double th
 // the whole operator. Layout (Smem::carve_mixed, or the full double layout):
 // U is the loaded double window, S holds the float window uf and the float
 // stage state, I the increments.
+// k1o, k2o (optional): the tile's float stage states k1 and k2 (interior
+// cells) for a reverse step that then skips their recompute; gout may be
+// null when only those are wanted (the last stage is skipped).
 template <int EQ, int FLUX>
 __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* gout, int te,
                                               double dtdx, const OpParams<double>& p,
-                                              const BcView& bc, int64_t g0, int64_t n) {
+                                              const BcView& bc, int64_t g0, int64_t n,
+                                              float* k1o = nullptr, float* k2o = nullptr) {
     constexpr int HL = step_halo<double>();
     const int tid = threadIdx.x, nt = blockDim.x, W = sm.W;
     const OpParams<float> pf = float_params(p);
@@ -490,6 +494,8 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
         }
         __syncthreads();
         if (!bc.periodic()) apply_bc(fs.S, g0, n, lo, hi, bc, 1);
+        if (k1o)
+            for (int i = HL + tid; i < HL + te; i += nt) k1o[i - HL] = fs.S[i];
     }
     {
         const int lo = HL - 3, hi = HL + te + 3;
@@ -501,8 +507,11 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
         }
         __syncthreads();
         if (!bc.periodic()) apply_bc(fs.S, g0, n, lo, hi, bc, 2);
+        if (k2o)
+            for (int i = HL + tid; i < HL + te; i += nt) k2o[i - HL] = fs.S[i];
     }
     unsigned long long mx = 0;
+    if (!gout) return mx;
     {
         const int lo = HL, hi = HL + te;
         face_fluxes<float, EQ, SHK_REC_LEARNED, FLUX>(fs.S, lo, hi, fs, pf);
@@ -519,12 +528,14 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
 
 // g0: global cell of window position 0 (s - HL); n: cells of the instance;
 // bc: its boundary (periodic: nothing to overwrite)
+// k1o, k2o: as step_tile_mixed (float stage states: float or mixed steps only)
 template <class T, int EQ, int REC, int FLUX>
 __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, T dtdx,
                                             const OpParams<T>& p, const BcView& bc = BcView(),
-                                            int64_t g0 = 0, int64_t n = 0) {
+                                            int64_t g0 = 0, int64_t n = 0, float* k1o = nullptr,
+                                            float* k2o = nullptr) {
     if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED)
-        return step_tile_mixed<EQ, FLUX>(sm, gout, te, dtdx, p, bc, g0, n);
+        return step_tile_mixed<EQ, FLUX>(sm, gout, te, dtdx, p, bc, g0, n, k1o, k2o);
     constexpr int HL = step_halo<T>();
     const int tid = threadIdx.x, nt = blockDim.x;
     const bool np = !bc.periodic();
@@ -545,6 +556,8 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
             }
             __syncthreads();
             if (np) apply_bc(sm.S, g0, n, lo, hi, bc, 1);
+            if (k1o)
+                for (int i = HL + tid; i < HL + te; i += nt) k1o[i - HL] = sm.S[i];
         }
         {
             const int lo = HL - 3, hi = HL + te + 3;
@@ -556,9 +569,12 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
             }
             __syncthreads();
             if (np) apply_bc(sm.S, g0, n, lo, hi, bc, 2);
+            if (k2o)
+                for (int i = HL + tid; i < HL + te; i += nt) k2o[i - HL] = sm.S[i];
         }
         using B = typename Bits<T>::type;
         B mx = 0;
+        if (!gout) return mx;
         const int lo = HL, hi = HL + te;
         face_fluxes<T, EQ, REC, FLUX>(sm.S, lo, hi, sm, p);
         for (int i = lo + tid; i < hi; i += nt) {
