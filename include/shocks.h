@@ -280,13 +280,14 @@ int shk_plan_forward_checkpointed(shk_plan* plan, void* u_a, void* u_b, int32_t 
 int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t nsteps,
                      void* seg, void* p_a, void* p_b, void* stream);
 
-/* shk_plan_adjoint with stage storage (learned reconstruction only): the
- * segment replay also writes each step's float stage states k1 and k2 into
- * `stages` (caller-owned, stride x *nfloats floats, *nfloats from
- * shk_plan_adjoint_stage_floats: 2 x the plan's cells, 0 for schemes without
- * stage storage), and every reverse step reads them instead of recomputing
- * its two forward stages. Same result, bit for bit, as shk_plan_adjoint. */
-int shk_plan_adjoint_stage_floats(shk_plan* plan, int64_t* nfloats);
+/* shk_plan_adjoint with stage storage: the segment replay also writes what
+ * each step's reverse step would recompute, and the reverse steps read it:
+ * the stage states k1, k2 (float, learned reconstruction) or k1, k2 and the
+ * face values of u and k1 (double, WENO-JS5 on periodic instances). `stages`
+ * is caller-owned, stride x *nbytes bytes, *nbytes from
+ * shk_plan_adjoint_stage_bytes (0: the plan recomputes; `stages` must then be
+ * NULL). Same result, bit for bit, as shk_plan_adjoint. */
+int shk_plan_adjoint_stage_bytes(shk_plan* plan, int64_t* nbytes);
 int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, int32_t nsteps,
                             void* seg, void* stages, void* p_a, void* p_b, void* stream);
 

@@ -123,7 +123,7 @@ SIGNATURES: dict[str, tuple] = {
                                               _I32, _D, _D, _P]),
     "shk_plan_forward_checkpointed": (ctypes.c_int, [_P, _P, _P, _I32, _P, _I32, _P]),
     "shk_plan_adjoint": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _P]),
-    "shk_plan_adjoint_stage_floats": (ctypes.c_int, [_P, ctypes.POINTER(_I64)]),
+    "shk_plan_adjoint_stage_bytes": (ctypes.c_int, [_P, ctypes.POINTER(_I64)]),
     "shk_plan_adjoint_staged": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _P, _P]),
     "shk_apply_operator_lf_noalloc_f64": (ctypes.c_int, [_SCH, _P, _P, _I64, _I32, _D, _P]),
     "shk_apply_operator_lf_noalloc_max_cells": (ctypes.c_int64, []),

@@ -36,9 +36,11 @@ class CheckpointedSolve:
     :arg solver: a :class:`BatchedSolver` created with ``max_steps >= nsteps``.
     :arg nsteps: number of SSPRK33 steps of the forward run.
     :arg stride: checkpoint interval (default ``ceil(sqrt(nsteps))``).
-    :arg store_stages: with the learned reconstruction, keep each replayed
-        step's float stage states (``stride x 2 x cells`` floats) so that the
-        reverse steps skip their two forward stages (same result, bit for bit).
+    :arg store_stages: keep what each replayed step's reverse step would
+        recompute (its stage states, and for double WENO-JS5 on periodic
+        instances the face values of u and k1: ``stride x`` 2 float or 6
+        double arrays of the batch) so that the reverse steps skip their
+        forward stages (same result, bit for bit).
     """
 
     def __init__(self, solver: BatchedSolver, nsteps: int, stride: int | None = None,
@@ -54,11 +56,11 @@ class CheckpointedSolve:
         self.seg = torch.empty((self.stride, solver.total), dtype=dt, device=dev)
         self.p_a = torch.empty(solver.total, dtype=dt, device=dev)
         self.p_b = torch.empty(solver.total, dtype=dt, device=dev)
-        nf = ctypes.c_int64(0)
-        L.check(solver.lib.shk_plan_adjoint_stage_floats(solver._plan, ctypes.byref(nf)),
-                "plan_adjoint_stage_floats")
-        self.stages = (torch.empty((self.stride, nf.value), dtype=torch.float32, device=dev)
-                       if store_stages and nf.value > 0 else None)
+        nb = ctypes.c_int64(0)
+        L.check(solver.lib.shk_plan_adjoint_stage_bytes(solver._plan, ctypes.byref(nb)),
+                "plan_adjoint_stage_bytes")
+        self.stages = (torch.empty((self.stride, nb.value), dtype=torch.uint8, device=dev)
+                       if store_stages and nb.value > 0 else None)
 
     def forward(self, u0: torch.Tensor, *, t0=None, tfinal=None) -> torch.Tensor:
         """Run the forward solve from *u0*; returns the final packed state."""

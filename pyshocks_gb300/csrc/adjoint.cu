@@ -294,9 +294,42 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
     __syncthreads();
 }
 
-// window positions [lo, hi) of a float stage state stored per instance cell
+// Stage storage of one replayed step: k1, k2 (learned or float steps, in
+// float), plus the face values of u and k1 (double WENO-JS5 steps, in double),
+// each an array of the plan's `total` cells.
+template <class T, int REC>
+__host__ __device__ constexpr int kStageArrays() {
+    return (sizeof(T) == 8 && REC != SHK_REC_LEARNED) ? 6 : 2;
+}
+template <class T, int REC>
+__device__ __forceinline__ StageOut<stage_t<T, REC>> stage_out(void* base, int64_t total,
+                                                               int64_t at) {
+    using S = stage_t<T, REC>;
+    StageOut<S> so;
+    if (!base) return so;
+    S* b = static_cast<S*>(base) + at;
+    so.k1 = b;
+    so.k2 = b + total;
+    if constexpr (kStageArrays<T, REC>() == 6) {
+        so.ulu = b + 2 * total;
+        so.uru = b + 3 * total;
+        so.ul1 = b + 4 * total;
+        so.ur1 = b + 5 * total;
+    }
+    return so;
+}
+
+template <class S>
+__device__ __forceinline__ StageOut<const S> as_const(const StageOut<S>& so) {
+    StageOut<const S> c;
+    c.k1 = so.k1; c.k2 = so.k2; c.ulu = so.ulu; c.uru = so.uru; c.ul1 = so.ul1; c.ur1 = so.ur1;
+    return c;
+}
+
+// window positions [lo, hi) of a stage array stored per instance cell
 // (position i is cell g0 + i, periodically)
-__device__ __forceinline__ void load_stage(float* dst, const float* src, int64_t n, int64_t g0,
+template <class S>
+__device__ __forceinline__ void load_stage(S* dst, const S* src, int64_t n, int64_t g0,
                                            int lo, int hi) {
     const bool once = g0 + lo >= -n && g0 + hi <= 2 * n;
     for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
@@ -314,13 +347,13 @@ __device__ __forceinline__ void load_stage(float* dst, const float* src, int64_t
 // increment to the double p once. Of the double arrays only the loaded windows
 // a.U and a.PB are read; af holds the float arrays (af.K1, af.K2 may overlay
 // a.U, which is dead once af.U is written).
-// k1g, k2g (optional): the instance's stored float stage states (replay with
-// stage outputs), which replace the recompute of k1 and k2 bit for bit.
+// st (optional): the instance's stored float stage states (replay with stage
+// storage), which replace the recompute of k1 and k2 bit for bit.
 template <int EQ>
 __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float>& af, double* gout,
                                    int te, double dtdx, const OpParams<double>& p,
                                    const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0,
-                                   const float* k1g = nullptr, const float* k2g = nullptr) {
+                                   const StageOut<const float>& st = StageOut<const float>()) {
     constexpr int HU = adj_uhalo<double>(), HP = adj_phalo<double>();
     constexpr int REC = SHK_REC_LEARNED;
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -336,9 +369,9 @@ __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float
     }
     // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12), or
     // the stored stage states there
-    if (k1g) {
-        load_stage(af.K1, k1g, n, g0, HU - 15, HU + te + 15);
-        load_stage(af.K2, k2g, n, g0, HU - 12, HU + te + 12);
+    if (st.k1) {
+        load_stage(af.K1, st.k1, n, g0, HU - 15, HU + te + 15);
+        load_stage(af.K2, st.k2, n, g0, HU - 12, HU + te + 12);
         __syncthreads();
         if (np) {
             apply_bc(af.K1, g0, n, HU - 15, HU + te + 15, bc, 1);
@@ -416,18 +449,22 @@ __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float
 template <class T, int EQ, int REC>
 __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const OpParams<T>& p,
                              const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0,
-                             const float* k1g = nullptr, const float* k2g = nullptr) {
+                             const StageOut<const stage_t<T, REC>>& st =
+                                 StageOut<const stage_t<T, REC>>()) {
     if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED) {
         // full double layout: the float arrays fit from CB on (24 in 20 double ones)
         AdjSmem<float> af;
         af.carve(reinterpret_cast<unsigned char*>(a.CB), a.W);
-        adjoint_tile_mixed<EQ>(a, af, gout, te, dtdx, p, bc, g0, n, k1g, k2g);
+        adjoint_tile_mixed<EQ>(a, af, gout, te, dtdx, p, bc, g0, n, st);
         return;
     }
-    // stored float stage states (learned reconstruction, float state) replace
-    // the recompute of k1 and k2 bit for bit
-    constexpr bool kStored = sizeof(T) == 4 && REC == SHK_REC_LEARNED;
     const bool np = !bc.periodic();
+    // stored stage states (and, for WENO-JS5, face values) replace the forward
+    // recompute bit for bit; the stored faces of a boundary instance lack its
+    // ghost cells, so WENO-JS5 steps with a boundary recompute
+    constexpr bool kStoreable = (sizeof(T) == 4 && REC == SHK_REC_LEARNED) ||
+                                (sizeof(T) == 8 && REC == SHK_REC_WENOJS53);
+    const bool stored = kStoreable && st.k1 && (REC == SHK_REC_LEARNED || !np);
     if (np) {
         constexpr int HU0 = adj_uhalo<T>(), HP0 = adj_phalo<T>();
         apply_bc(a.U, g0, n, 0, te + 2 * HU0, bc, 0);
@@ -442,10 +479,16 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     const T fdt = dtdx * p.fscale;  // face fluxes are stored as F / fscale
     // forward recompute: k1 on [HU-15, HU+te+15), k2 on [HU-12, HU+te+12),
     // with the forward step's own formulas (increments about u for float)
-    if constexpr (kStored) {
-        if (k1g) {
-            load_stage(reinterpret_cast<float*>(a.K1), k1g, n, g0, HU - 15, HU + te + 15);
-            load_stage(reinterpret_cast<float*>(a.K2), k2g, n, g0, HU - 12, HU + te + 12);
+    if constexpr (kStoreable) {
+        if (stored) {
+            load_stage(a.K1, st.k1, n, g0, HU - 15, HU + te + 15);
+            load_stage(a.K2, st.k2, n, g0, HU - 12, HU + te + 12);
+            if constexpr (kCache) {
+                load_stage(a.CLu, st.ulu, n, g0, HU - 6, HU + te + 6);
+                load_stage(a.CRu, st.uru, n, g0, HU - 6, HU + te + 6);
+                load_stage(a.CL1, st.ul1, n, g0, HU - 6, HU + te + 6);
+                load_stage(a.CR1, st.ur1, n, g0, HU - 6, HU + te + 6);
+            }
             __syncthreads();
             if (np) {
                 apply_bc(a.K1, g0, n, HU - 15, HU + te + 15, bc, 1);
@@ -453,7 +496,7 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
             }
         }
     }
-    if (!kStored || !k1g) {
+    if (!stored) {
     {
         const int lo = HU - 15, hi = HU + te + 15;
         // WENO-JS5: the face values of u stay in CLu/CRu for reverse stage 1
@@ -564,8 +607,8 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
                                                                    T* __restrict__ pout,
                                                                    const double* __restrict__ dt_row,
                                                                    OpParams<T> p,
-                                                                   const float* __restrict__ k1s,
-                                                                   const float* __restrict__ k2s) {
+                                                                   const void* stages,
+                                                                   int64_t total) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     constexpr bool kMixed = sizeof(T) == 8 && REC == SHK_REC_LEARNED;
@@ -599,10 +642,10 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
         const BcView bc = plan_bc(P, b);
         const int64_t g0 = s0 - adj_uhalo<T>();
-        const float* k1g = k1s ? k1s + off : nullptr;
-        const float* k2g = k2s ? k2s + off : nullptr;
-        if constexpr (kMixed) adjoint_tile_mixed<EQ>(a, af, pout + off + s0, te, dtdx, p, bc, g0, n, k1g, k2g);
-        else adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p, bc, g0, n, k1g, k2g);
+        const StageOut<const stage_t<T, REC>> st =
+            as_const(stage_out<T, REC>(const_cast<void*>(stages), total, off));
+        if constexpr (kMixed) adjoint_tile_mixed<EQ>(a, af, pout + off + s0, te, dtdx, p, bc, g0, n, st);
+        else adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p, bc, g0, n, st);
         __syncthreads();
     }
     finish_items(P, 2);
@@ -610,13 +653,15 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
 
 // forward step with a recorded dt (no CFL, no time update): recompute of the
 // states between checkpoints
-// k1s, k2s (optional, float or mixed steps): the stage states of each step
-// for a reverse step that skips their recompute; uout may then be null.
+// stages (optional): the step's stage storage, kStageArrays<T, REC> arrays of
+// P's cells in the stage precision (stage_arrays), for a reverse step that
+// skips its forward recompute; uout may then be null.
 template <class T, int EQ, int REC>
 __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) replay_step_kernel(PlanDev P, const T* __restrict__ uin,
                                                                T* __restrict__ uout,
                                                                const double* __restrict__ dt_row,
-                                                               OpParams<T> p, float* k1s, float* k2s) {
+                                                               OpParams<T> p, void* stages,
+                                                               int64_t total) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     constexpr int HL = step_halo<T>();
@@ -649,8 +694,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
         step_tile<T, EQ, REC, SHK_FLUX_RUSANOV>(sm, uout ? uout + off + s0 : nullptr, te, dtdx, p,
                                                 plan_bc(P, b), s0 - HL, n,
-                                                k1s ? k1s + off + s0 : nullptr,
-                                                k2s ? k2s + off + s0 : nullptr);
+                                                stage_out<T, REC>(stages, total, off + s0));
         __syncthreads();
     }
     finish_items(P, 4);
@@ -767,12 +811,12 @@ int by_equation(int eq, F&& f) {
 template <class TS>
 struct AdjLaunch {
     PlanDev D; const void* um; const void* pn; void* po; const double* dt_row; OpParams<TS> p;
-    size_t smem; int grid; cudaStream_t st; const float* k1s = nullptr; const float* k2s = nullptr;
+    size_t smem; int grid; cudaStream_t st; const void* stages = nullptr; int64_t total = 0;
     template <class T, int EQ, int REC> int operator()() {
         auto k = batched_adjoint_kernel<T, EQ, REC>;
         ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(um), static_cast<const T*>(pn),
-                                         static_cast<T*>(po), dt_row, p, k1s, k2s);
+                                         static_cast<T*>(po), dt_row, p, stages, total);
         return acuda(cudaGetLastError());
     }
 };
@@ -780,12 +824,12 @@ struct AdjLaunch {
 template <class TS>
 struct ReplayLaunch {
     PlanDev D; const void* uin; void* uout; const double* dt_row; OpParams<TS> p;
-    size_t smem; int grid; cudaStream_t st; float* k1s = nullptr; float* k2s = nullptr;
+    size_t smem; int grid; cudaStream_t st; void* stages = nullptr; int64_t total = 0;
     template <class T, int EQ, int REC> int operator()() {
         auto k = replay_step_kernel<T, EQ, REC>;
         ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(uin), static_cast<T*>(uout), dt_row, p,
-                                         k1s, k2s);
+                                         stages, total);
         return acuda(cudaGetLastError());
     }
 };
@@ -865,15 +909,24 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
     return shk_plan_adjoint_staged(plan, ckpt, stride, nsteps, seg, nullptr, p_a, p_b, stream);
 }
 
-int shk_plan_adjoint_stage_floats(shk_plan* plan, int64_t* nfloats) {
+// bytes of stage storage per replayed step (0: the plan recomputes)
+static int64_t stage_bytes(const PlanDev& D, int dtype, const shk_scheme& sch, int64_t total) {
+    if (sch.rec == SHK_REC_LEARNED) return 2 * total * int64_t(sizeof(float));
+    const bool periodic = D.bc_left == SHK_BC_PERIODIC && D.bc_right == SHK_BC_PERIODIC;
+    if (dtype == SHK_F64 && sch.rec == SHK_REC_WENOJS53 && periodic)
+        return 6 * total * int64_t(sizeof(double));
+    return 0;
+}
+
+int shk_plan_adjoint_stage_bytes(shk_plan* plan, int64_t* nbytes) {
     PlanDev D;
     int dtype = 0, grid = 0;
     shk_scheme sch;
     int64_t total = 0;
-    if (!plan || !nfloats) return SHK_EINVAL;
+    if (!plan || !nbytes) return SHK_EINVAL;
     int r = plan_view(plan, &D, &dtype, &grid, &sch, &total, nullptr);
     if (r != SHK_OK) return r;
-    *nfloats = sch.rec == SHK_REC_LEARNED ? 2 * total : 0;
+    *nbytes = stage_bytes(D, dtype, sch, total);
     return SHK_OK;
 }
 
@@ -888,7 +941,8 @@ int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, in
     int r = plan_view(plan, &D, &dtype, &grid, &sch, &total, nullptr);
     if (r != SHK_OK) return r;
     if (!adjoint_supported(&sch)) return SHK_EUNSUPPORTED;
-    if (stages && sch.rec != SHK_REC_LEARNED) return SHK_EINVAL;  // float stage states only
+    const int64_t sbytes = stage_bytes(D, dtype, sch, total);
+    if (stages && sbytes == 0) return SHK_EINVAL;  // this plan has no stage storage
     if (!D.dt_hist || D.max_steps < nsteps) return SHK_EINVAL;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const size_t esz = dtype == SHK_F64 ? 8 : 4;
@@ -915,12 +969,9 @@ int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, in
     const int per_sm = std::max(1, static_cast<int>((220 * 1024) / std::max<size_t>(asmem, 1)));
     const int agrid = std::max(1, std::min(D.nitems, per_sm * sms));
     auto seg_at = [&](int j) { return static_cast<char*>(seg) + size_t(j) * bytes; };
-    // stage states of segment step j: k1 then k2, `total` floats each
-    auto k1_at = [&](int j) {
-        return stages ? static_cast<float*>(stages) + size_t(2 * j) * total : nullptr;
-    };
-    auto k2_at = [&](int j) {
-        return stages ? static_cast<float*>(stages) + size_t(2 * j + 1) * total : nullptr;
+    // stage storage of segment step j
+    auto stage_at = [&](int j) -> void* {
+        return stages ? static_cast<char*>(stages) + size_t(j) * size_t(sbytes) : nullptr;
     };
     const int nseg = (nsteps + stride - 1) / stride;
     void* cur = p_a;
@@ -937,11 +988,11 @@ int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, in
             void* out = j < cnt ? seg_at(j) : nullptr;
             if (dtype == SHK_F64) {
                 ReplayLaunch<double> f{D, seg_at(j - 1), out, row, adj_params<double>(&sch), fsmem, grid, st,
-                                       k1_at(j - 1), k2_at(j - 1)};
+                                       stage_at(j - 1), total};
                 r = by_scheme<double>(sch, f);
             } else {
                 ReplayLaunch<float> f{D, seg_at(j - 1), out, row, adj_params<float>(&sch), fsmem, grid, st,
-                                      k1_at(j - 1), k2_at(j - 1)};
+                                      stage_at(j - 1), total};
                 r = by_scheme<float>(sch, f);
             }
             if (r != SHK_OK) return r;
@@ -950,11 +1001,11 @@ int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, in
             const double* row = D.dt_hist + size_t(base + j) * D.B;
             if (dtype == SHK_F64) {
                 AdjLaunch<double> f{D, seg_at(j), cur, nxt, row, adj_params<double>(&sch), asmem, agrid, st,
-                                    k1_at(j), k2_at(j)};
+                                    stage_at(j), total};
                 r = by_scheme<double>(sch, f);
             } else {
                 AdjLaunch<float> f{D, seg_at(j), cur, nxt, row, adj_params<float>(&sch), asmem, agrid, st,
-                                   k1_at(j), k2_at(j)};
+                                   stage_at(j), total};
                 r = by_scheme<float>(sch, f);
             }
             if (r != SHK_OK) return r;

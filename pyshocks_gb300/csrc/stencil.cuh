@@ -8,6 +8,8 @@
 
 #include <cstdint>
 
+#include <type_traits>
+
 #include "device.cuh"
 #include "learned.cuh"
 
@@ -442,6 +444,31 @@ __host__ __device__ inline DtState compute_dt(double smax, double cfl, double th
 }
 
 // ---------------------------------------------------------------------------
+// What a replayed step hands to the reverse sweep (pointers to the tile's
+// interior cells; null: not wanted): the stage states k1, k2 and, for the
+// double WENO-JS5 step, the face values of u and of k1. Their element type is
+// the stage precision: float for the learned or float steps, double otherwise.
+// ---------------------------------------------------------------------------
+template <class S>
+struct StageOut {
+    S* k1 = nullptr;
+    S* k2 = nullptr;
+    S* ulu = nullptr;
+    S* uru = nullptr;
+    S* ul1 = nullptr;
+    S* ur1 = nullptr;
+};
+template <class T, int REC>
+using stage_t = typename std::conditional<sizeof(T) == 8 && REC != SHK_REC_LEARNED, double, float>::type;
+
+// the tile's interior [HL, HL + te) of a window array into out
+template <class S, class V>
+__device__ __forceinline__ void store_interior(S* out, const V* w, int HL, int te) {
+    if (out)
+        for (int i = HL + threadIdx.x; i < HL + te; i += blockDim.x) out[i - HL] = static_cast<S>(w[i]);
+}
+
+// ---------------------------------------------------------------------------
 // fused SSPRK33 step of one tile: window [s - HL, s + te + HL) -> u_out[s, s + te)
 // returns the thread's max |f'(u_new)| bits
 // ---------------------------------------------------------------------------
@@ -458,14 +485,14 @@ __host__ __device__ inline DtState compute_dt(double smax, double cfl, double th
 // the whole operator. Layout (Smem::carve_mixed, or the full double layout):
 // U is the loaded double window, S holds the float window uf and the float
 // stage state, I the increments.
-// k1o, k2o (optional): the tile's float stage states k1 and k2 (interior
-// cells) for a reverse step that then skips their recompute; gout may be
-// null when only those are wanted (the last stage is skipped).
+// so (optional): the float stage states k1, k2 for a reverse step that then
+// skips their recompute; gout may be null when only those are wanted (the
+// last stage is skipped).
 template <int EQ, int FLUX>
 __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* gout, int te,
                                               double dtdx, const OpParams<double>& p,
                                               const BcView& bc, int64_t g0, int64_t n,
-                                              float* k1o = nullptr, float* k2o = nullptr) {
+                                              const StageOut<float>& so = StageOut<float>()) {
     constexpr int HL = step_halo<double>();
     const int tid = threadIdx.x, nt = blockDim.x, W = sm.W;
     const OpParams<float> pf = float_params(p);
@@ -494,8 +521,7 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
         }
         __syncthreads();
         if (!bc.periodic()) apply_bc(fs.S, g0, n, lo, hi, bc, 1);
-        if (k1o)
-            for (int i = HL + tid; i < HL + te; i += nt) k1o[i - HL] = fs.S[i];
+        store_interior(so.k1, fs.S, HL, te);
     }
     {
         const int lo = HL - 3, hi = HL + te + 3;
@@ -507,8 +533,7 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
         }
         __syncthreads();
         if (!bc.periodic()) apply_bc(fs.S, g0, n, lo, hi, bc, 2);
-        if (k2o)
-            for (int i = HL + tid; i < HL + te; i += nt) k2o[i - HL] = fs.S[i];
+        store_interior(so.k2, fs.S, HL, te);
     }
     unsigned long long mx = 0;
     if (!gout) return mx;
@@ -528,14 +553,15 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
 
 // g0: global cell of window position 0 (s - HL); n: cells of the instance;
 // bc: its boundary (periodic: nothing to overwrite)
-// k1o, k2o: as step_tile_mixed (float stage states: float or mixed steps only)
+// so: what the reverse sweep keeps of this step (StageOut); gout may then be
+// null (the last stage is skipped)
 template <class T, int EQ, int REC, int FLUX>
 __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, T dtdx,
                                             const OpParams<T>& p, const BcView& bc = BcView(),
-                                            int64_t g0 = 0, int64_t n = 0, float* k1o = nullptr,
-                                            float* k2o = nullptr) {
+                                            int64_t g0 = 0, int64_t n = 0,
+                                            const StageOut<stage_t<T, REC>>& so = StageOut<stage_t<T, REC>>()) {
     if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED)
-        return step_tile_mixed<EQ, FLUX>(sm, gout, te, dtdx, p, bc, g0, n, k1o, k2o);
+        return step_tile_mixed<EQ, FLUX>(sm, gout, te, dtdx, p, bc, g0, n, so);
     constexpr int HL = step_halo<T>();
     const int tid = threadIdx.x, nt = blockDim.x;
     const bool np = !bc.periodic();
@@ -556,8 +582,7 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
             }
             __syncthreads();
             if (np) apply_bc(sm.S, g0, n, lo, hi, bc, 1);
-            if (k1o)
-                for (int i = HL + tid; i < HL + te; i += nt) k1o[i - HL] = sm.S[i];
+            store_interior(so.k1, sm.S, HL, te);
         }
         {
             const int lo = HL - 3, hi = HL + te + 3;
@@ -569,8 +594,7 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
             }
             __syncthreads();
             if (np) apply_bc(sm.S, g0, n, lo, hi, bc, 2);
-            if (k2o)
-                for (int i = HL + tid; i < HL + te; i += nt) k2o[i - HL] = sm.S[i];
+            store_interior(so.k2, sm.S, HL, te);
         }
         using B = typename Bits<T>::type;
         B mx = 0;
@@ -590,24 +614,31 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
     {
         const int lo = HL - 6, hi = HL + te + 6;
         face_fluxes<T, EQ, REC, FLUX>(sm.U, lo, hi, sm, p);
+        store_interior(so.ulu, sm.UL, HL, te);
+        store_interior(so.uru, sm.UR, HL, te);
         for (int i = lo + tid; i < hi; i += nt) sm.S[i] = fma(dtdx, sm.D[i - 1] - sm.D[i], sm.U[i]);
         __syncthreads();
         if (np) apply_bc(sm.S, g0, n, lo, hi, bc, 1);
+        store_interior(so.k1, sm.S, HL, te);
     }
     // stage 2: k2 = 3/4 u + 1/4 (k1 + dt L(k1)) on [HL-3, HL+te+3) (in place over k1)
     {
         const int lo = HL - 3, hi = HL + te + 3;
         face_fluxes<T, EQ, REC, FLUX>(sm.S, lo, hi, sm, p);
+        store_interior(so.ul1, sm.UL, HL, te);
+        store_interior(so.ur1, sm.UR, HL, te);
         for (int i = lo + tid; i < hi; i += nt) {
             const T k = fma(dtdx, sm.D[i - 1] - sm.D[i], sm.S[i]);
             sm.S[i] = fma(T(1.0 / 4.0), k, T(3.0 / 4.0) * sm.U[i]);
         }
         __syncthreads();
         if (np) apply_bc(sm.S, g0, n, lo, hi, bc, 2);
+        store_interior(so.k2, sm.S, HL, te);
     }
     // stage 3: u+ = 1/3 u + 2/3 (k2 + dt L(k2)) on the tile
     using B = typename Bits<T>::type;
     B mx = 0;
+    if (!gout) return mx;
     {
         const int lo = HL, hi = HL + te;
         face_fluxes<T, EQ, REC, FLUX>(sm.S, lo, hi, sm, p);
