@@ -283,7 +283,7 @@ int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t n
 /* shk_plan_adjoint with stage storage: the segment replay also writes what
  * each step's reverse step would recompute, and the reverse steps read it:
  * the stage states k1, k2 (float, learned reconstruction) or k1, k2 and the
- * face values of u and k1 (double, WENO-JS5 on periodic instances). `stages`
+ * face values of u, k1 and k2 (double, WENO-JS5 on periodic instances). `stages`
  * is caller-owned, stride x *nbytes bytes, *nbytes from
  * shk_plan_adjoint_stage_bytes (0: the plan recomputes; `stages` must then be
  * NULL). Same result, bit for bit, as shk_plan_adjoint. */

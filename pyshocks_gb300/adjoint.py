@@ -38,7 +38,7 @@ class CheckpointedSolve:
     :arg stride: checkpoint interval (default ``ceil(sqrt(nsteps))``).
     :arg store_stages: keep what each replayed step's reverse step would
         recompute (its stage states, and for double WENO-JS5 on periodic
-        instances the face values of u and k1: ``stride x`` 2 float or 6
+        instances the face values of u, k1 and k2: ``stride x`` 2 float or 8
         double arrays of the batch) so that the reverse steps skip their
         forward stages (same result, bit for bit).
     """

@@ -299,7 +299,7 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
 // each an array of the plan's `total` cells.
 template <class T, int REC>
 __host__ __device__ constexpr int kStageArrays() {
-    return (sizeof(T) == 8 && REC != SHK_REC_LEARNED) ? 6 : 2;
+    return (sizeof(T) == 8 && REC != SHK_REC_LEARNED) ? 8 : 2;
 }
 template <class T, int REC>
 __device__ __forceinline__ StageOut<stage_t<T, REC>> stage_out(void* base, int64_t total,
@@ -310,11 +310,13 @@ __device__ __forceinline__ StageOut<stage_t<T, REC>> stage_out(void* base, int64
     S* b = static_cast<S*>(base) + at;
     so.k1 = b;
     so.k2 = b + total;
-    if constexpr (kStageArrays<T, REC>() == 6) {
+    if constexpr (kStageArrays<T, REC>() == 8) {
         so.ulu = b + 2 * total;
         so.uru = b + 3 * total;
         so.ul1 = b + 4 * total;
         so.ur1 = b + 5 * total;
+        so.ul2 = b + 6 * total;
+        so.ur2 = b + 7 * total;
     }
     return so;
 }
@@ -323,6 +325,7 @@ template <class S>
 __device__ __forceinline__ StageOut<const S> as_const(const StageOut<S>& so) {
     StageOut<const S> c;
     c.k1 = so.k1; c.k2 = so.k2; c.ulu = so.ulu; c.uru = so.uru; c.ul1 = so.ul1; c.ur1 = so.ur1;
+    c.ul2 = so.ul2; c.ur2 = so.ur2;
     return c;
 }
 
@@ -471,9 +474,9 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
         zero_outside(a.PB, g0, n, HU0 - HP0, HU0 + te + HP0);
     }
     constexpr int HU = adj_uhalo<T>();
-    // the forward recompute's face values of u and k1 serve reverse stages 1
-    // and 2 (they cover [HU-16, HU+te+16) and [HU-13, HU+te+13), the stages
-    // read [HU-6, HU+te+6)); the face values of k2 are reconstructed there
+    // the forward recompute's face values of u, k1 and k2 serve the reverse
+    // stages (they cover [HU-16, HU+te+16), [HU-13, HU+te+13) and
+    // [HU-9, HU+te+9); the stages read [HU-6, HU+te+6), k2's [HU-9, HU+te+9))
     constexpr bool kCache = REC == SHK_REC_WENOJS53;
     const int tid = threadIdx.x, nt = blockDim.x;
     const T fdt = dtdx * p.fscale;  // face fluxes are stored as F / fscale
@@ -488,6 +491,9 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
                 load_stage(a.CRu, st.uru, n, g0, HU - 6, HU + te + 6);
                 load_stage(a.CL1, st.ul1, n, g0, HU - 6, HU + te + 6);
                 load_stage(a.CR1, st.ur1, n, g0, HU - 6, HU + te + 6);
+                // k2's face values in UL/UR (free: no reconstruction runs here)
+                load_stage(a.UL, st.ul2, n, g0, HU - 9, HU + te + 9);
+                load_stage(a.UR, st.ur2, n, g0, HU - 9, HU + te + 9);
             }
             __syncthreads();
             if (np) {
@@ -530,11 +536,18 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
         __syncthreads();
         if (np) apply_bc(a.K2, g0, n, lo, hi, bc, 2);
     }
+    if constexpr (kCache) {
+        // the face values of k2 on [HU-9, HU+te+9) as the forward's face pass
+        // forms them (as the stored ones; the fluxes it also leaves in D are
+        // not used)
+        face_fluxes<T, EQ, REC, SHK_FLUX_RUSANOV>(a.K2, HU - 8, HU + te + 8, a.fwd(a.K2, a.UL, a.UR), p);
+    }
     }
     // reverse stage 3: k2b = 2/3 (p + dt J(k2)^T p) on [HU-6, HU+te+6)
     {
         const int lo = HU - 6, hi = HU + te + 6;
-        vjp_stage<T, EQ, REC>(a.K2, a.PB, a.Z, lo, hi, a, p, dtdx);
+        vjp_stage<T, EQ, REC>(a.K2, a.PB, a.Z, lo, hi, a, p, dtdx, kCache ? a.UL : nullptr,
+                              kCache ? a.UR : nullptr);
         if (np) bc_transpose(a.Z, g0, n, lo, hi, bc);
         for (int i = lo + tid; i < hi; i += nt) a.CB[i] = T(2.0 / 3.0) * (a.PB[i] + a.Z[i]);
         __syncthreads();
@@ -914,7 +927,7 @@ static int64_t stage_bytes(const PlanDev& D, int dtype, const shk_scheme& sch, i
     if (sch.rec == SHK_REC_LEARNED) return 2 * total * int64_t(sizeof(float));
     const bool periodic = D.bc_left == SHK_BC_PERIODIC && D.bc_right == SHK_BC_PERIODIC;
     if (dtype == SHK_F64 && sch.rec == SHK_REC_WENOJS53 && periodic)
-        return 6 * total * int64_t(sizeof(double));
+        return 8 * total * int64_t(sizeof(double));
     return 0;
 }
 

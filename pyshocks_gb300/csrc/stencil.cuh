@@ -446,7 +446,7 @@ __host__ __device__ inline DtState compute_dt(double smax, double cfl, double th
 // ---------------------------------------------------------------------------
 // What a replayed step hands to the reverse sweep (pointers to the tile's
 // interior cells; null: not wanted): the stage states k1, k2 and, for the
-// double WENO-JS5 step, the face values of u and of k1. Their element type is
+// double WENO-JS5 step, the face values of u, k1 and k2. Their element type is
 // the stage precision: float for the learned or float steps, double otherwise.
 // ---------------------------------------------------------------------------
 template <class S>
@@ -457,6 +457,8 @@ struct StageOut {
     S* uru = nullptr;
     S* ul1 = nullptr;
     S* ur1 = nullptr;
+    S* ul2 = nullptr;  // face values of k2
+    S* ur2 = nullptr;
 };
 template <class T, int REC>
 using stage_t = typename std::conditional<sizeof(T) == 8 && REC != SHK_REC_LEARNED, double, float>::type;
@@ -638,10 +640,13 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, 
     // stage 3: u+ = 1/3 u + 2/3 (k2 + dt L(k2)) on the tile
     using B = typename Bits<T>::type;
     B mx = 0;
-    if (!gout) return mx;
+    if (!gout && !so.ul2) return mx;
     {
         const int lo = HL, hi = HL + te;
         face_fluxes<T, EQ, REC, FLUX>(sm.S, lo, hi, sm, p);
+        store_interior(so.ul2, sm.UL, HL, te);
+        store_interior(so.ur2, sm.UR, HL, te);
+        if (!gout) return mx;
         for (int i = lo + tid; i < hi; i += nt) {
             const T k = fma(dtdx, sm.D[i - 1] - sm.D[i], sm.S[i]);
             const T un = fma(T(2.0 / 3.0), k, T(1.0 / 3.0) * sm.U[i]);
