@@ -151,16 +151,19 @@ __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1
     }
     // interpolation part (weights held fixed): d_k P_k / D folded with the
     // sub-stencil values 6 uhat_k
-    const T rho0 = gR * P0, rho1 = T(6) * gR * P1, rho2 = T(3) * gR * P2;
-    const T lam0 = gL * P2, lam1 = T(6) * gL * P1, lam2 = T(3) * gL * P0;
+    const T g6 = T(6) * P1;
+    const T rho0 = gR * P0, rho1 = gR * g6, rho2 = T(3) * gR * P2;
+    const T lam0 = gL * P2, lam1 = gL * g6, lam2 = T(3) * gL * P0;
     // smoothness part: d ur / d beta_j = -2 P_j (cr_j - W_j (ur - v)) / (e_j D_R), W = (6, 36, 18);
-    // the left side sees beta_j through its mirrored sub-stencil 2 - j
+    // the left side sees beta_j through its mirrored sub-stencil 2 - j. The
+    // factor -2 is folded into the taps below (bb, bh, bd are -1/2 of the
+    // cotangents of beta, h, D).
     const T x0 = fma(gR, fma(T(-6), dR, cr0), gL * fma(T(-18), dL, cl2));
     const T x1 = fma(gR, fma(T(-36), dR, cr1), gL * fma(T(-36), dL, cl1));
     const T x2 = fma(gR, fma(T(-18), dR, cr2), gL * fma(T(-6), dL, cl0));
-    const T bb0 = T(-2) * (P0 * ie0) * x0;
-    const T bb1 = T(-2) * (P1 * ie1) * x1;
-    const T bb2 = T(-2) * (P2 * ie2) * x2;
+    const T bb0 = (P0 * ie0) * x0;
+    const T bb1 = (P1 * ie1) * x1;
+    const T bb2 = (P2 * ie2) * x2;
     // beta_j = h_j^2 + 13/3 D_j^2 with h_j = B_j v / 2, D_j = A_j v / 2
     const T bh0 = bb0 * h0, bh1 = bb1 * h1, bh2 = bb2 * h2;
     const T bd0 = bb0 * (T(13.0 / 3.0) * Dm1);
@@ -169,14 +172,14 @@ __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1
     // taps: A_0 (1,-2,1,0,0) B_0 (1,-4,3,0,0) A_1 (0,1,-2,1,0) B_1 (0,-1,0,1,0)
     //       A_2 (0,0,1,-2,1) B_2 (0,0,3,-4,1); 6 uhat right (2,-7,11,0,0) (0,-1,5,2,0)
     //       (0,0,2,5,-1); left (0,0,11,-7,2) (0,2,5,-1,0) (-1,5,2,0,0)
-    t0 = fma(T(2), rho0, -lam2) + (bh0 + bd0);
+    t0 = fma(T(-2), bh0 + bd0, fma(T(2), rho0, -lam2));
     t1 = fma(T(-7), rho0, -rho1) + fma(T(2), lam1, T(5) * lam2) +
-         (fma(T(-4), bh0, T(-2) * bd0) + (bd1 - bh1));
+         fma(T(8), bh0, fma(T(4), bd0, T(-2) * (bd1 - bh1)));
     t2 = fma(T(11), rho0 + lam0, fma(T(5), rho1 + lam1, T(2) * (rho2 + lam2))) +
-         (fma(T(3), bh0 + bh2, bd0 + bd2) - T(2) * bd1);
+         fma(T(-2), fma(T(3), bh0 + bh2, bd0 + bd2), T(4) * bd1);
     t3 = fma(T(2), rho1, T(5) * rho2) - fma(T(7), lam0, lam1) +
-         ((bh1 + bd1) + fma(T(-4), bh2, T(-2) * bd2));
-    t4 = fma(T(2), lam0, -rho2) + (bh2 + bd2);
+         fma(T(-2), bh1 + bd1, fma(T(8), bh2, T(4) * bd2));
+    t4 = fma(T(-2), bh2 + bd2, fma(T(2), lam0, -rho2));
 }
 
 // z_i = dt (J_L(v)^T w)_i for i in [lo, hi); v valid on [lo-6, hi+6), w on
