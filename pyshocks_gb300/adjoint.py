@@ -40,7 +40,8 @@ class CheckpointedSolve:
         recompute (its stage states, and for double WENO-JS5 on periodic
         instances the face values of u, k1 and k2: ``stride x`` 2 float or 8
         double arrays of the batch) so that the reverse steps skip their
-        forward stages (same result, bit for bit).
+        forward stages (same result, bit for bit). Left out when it would take
+        more than half of the free device memory.
     """
 
     def __init__(self, solver: BatchedSolver, nsteps: int, stride: int | None = None,
@@ -59,8 +60,14 @@ class CheckpointedSolve:
         nb = ctypes.c_int64(0)
         L.check(solver.lib.shk_plan_adjoint_stage_bytes(solver._plan, ctypes.byref(nb)),
                 "plan_adjoint_stage_bytes")
+        want = store_stages and nb.value > 0
+        if want:
+            # stage storage is an optimisation: leave it out when it would take
+            # more than half of the free device memory
+            free, _ = torch.cuda.mem_get_info(dev)
+            want = self.stride * nb.value <= free // 2
         self.stages = (torch.empty((self.stride, nb.value), dtype=torch.uint8, device=dev)
-                       if store_stages and nb.value > 0 else None)
+                       if want else None)
 
     def forward(self, u0: torch.Tensor, *, t0=None, tfinal=None) -> torch.Tensor:
         """Run the forward solve from *u0*; returns the final packed state."""
