@@ -257,6 +257,28 @@ def test_host_stepper_equals_device_plan(gb, dtype, chunks):
     assert hs.status() == 0
 
 
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_host_stepper_learned_equals_device_plan(gb, dtype):
+    """The host-buffer stepper with the learned reconstruction (mixed float64
+    or float32 state) gives the device plan's result bit for bit."""
+    from pyshocks_gb300 import burgers, learned
+    from pyshocks_gb300.batched import BatchedSolver, HostStepper
+
+    sizes = [4096, 1000, 2048, 3000]
+    rng = np.random.default_rng(29)
+    u0 = np.concatenate([R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes])
+    scheme = burgers.Rusanov(rec=learned.LearnedWENO(params=learned.load_default_params()))
+    dx = [2.0 / n for n in sizes]
+    ref = BatchedSolver(scheme, sizes, dx, dtype=dtype)
+    ref.reset(torch.tensor(u0, device="cuda"))
+    ref.step(4)
+    hs = HostStepper(scheme, sizes, dx, dtype=dtype, chunks=3)
+    out = hs.advance(torch.tensor(u0).to(dtype).pin_memory(), nsteps=4)
+    torch.cuda.current_stream().synchronize()
+    assert torch.equal(out, ref.u.cpu())
+    assert hs.status() == 0
+
+
 def test_batched_float32_error_and_conservation(gb):
     """FP32 state: error against the FP64 oracle reported/bounded; the FP64
     conserved-mass sums drift only by rounding."""
