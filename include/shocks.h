@@ -241,6 +241,11 @@ int shk_host_stepper_num_chunks(const shk_host_stepper* hs);
 int shk_host_stepper_advance(shk_host_stepper* hs, const void* h_in, void* h_out, int32_t nsteps,
                              void* stream);
 
+/* shk_plan_set_boundary for every chunk: dirichlet [B][2][3], neumann [B][2]
+ * over the whole batch (device or host memory) */
+int shk_host_stepper_set_boundary(shk_host_stepper* hs, int32_t left, int32_t right,
+                                  const double* dirichlet, const double* neumann, void* stream);
+
 /* OR of the chunks' status words (synchronises `stream`) */
 int shk_host_stepper_status(shk_host_stepper* hs, int32_t* h_status, void* stream);
 

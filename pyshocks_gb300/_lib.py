@@ -118,6 +118,7 @@ SIGNATURES: dict[str, tuple] = {
     "shk_host_stepper_num_chunks": (ctypes.c_int, [_P]),
     "shk_host_stepper_advance": (ctypes.c_int, [_P, _P, _P, _I32, _P]),
     "shk_host_stepper_status": (ctypes.c_int, [_P, ctypes.POINTER(_I32), _P]),
+    "shk_host_stepper_set_boundary": (ctypes.c_int, [_P, _I32, _I32, _P, _P, _P]),
     "shk_ssprk33_vjp_f64": (ctypes.c_int, [_SCH, _P, _P, _P, _I64, _I32, _D, _D, _P]),
     "shk_ssprk33_vjp_bc_f64": (ctypes.c_int, [_SCH, ctypes.POINTER(ShkBoundary), _P, _P, _P, _I64,
                                               _I32, _D, _D, _P]),

@@ -46,6 +46,24 @@ def pack_offsets(sizes: Sequence[int]) -> np.ndarray:
     return off
 
 
+def _boundary_tables(B: int, device, left: str, right: str | None, dirichlet, neumann):
+    """Boundary kinds and the ``(B, 2, 3)`` Dirichlet / ``(B, 2)`` Neumann
+    tables (float64 on *device*) of :meth:`BatchedSolver.set_boundary`."""
+    kinds = {"periodic": L.SHK_BC_PERIODIC, "dirichlet": L.SHK_BC_DIRICHLET,
+             "neumann": L.SHK_BC_NEUMANN}
+    right = left if right is None else right
+
+    def table(v, shape):
+        if v is None:
+            return None
+        t = torch.as_tensor(v, dtype=torch.float64, device=device)
+        if t.dim() == 1 and t.numel() == 2:
+            t = t.reshape((1, 2) + (1,) * (len(shape) - 2)).expand((B,) + shape[1:])
+        return t.reshape(shape).contiguous()
+
+    return kinds[left], kinds[right], table(dirichlet, (B, 2, 3)), table(neumann, (B, 2))
+
+
 class HostStepper:
     """A batch whose state lives in host memory (``shk_host_stepper``).
 
@@ -108,6 +126,16 @@ class HostStepper:
                                                   int(nsteps), L.stream_handle()),
                 "host_stepper_advance")
         return u_out
+
+    def set_boundary(self, left: str = "periodic", right: str | None = None, *,
+                     dirichlet=None, neumann=None) -> None:
+        """As :meth:`BatchedSolver.set_boundary`, for every chunk."""
+        lk, rk, d, nm = _boundary_tables(self.B, torch.device("cuda"), left, right, dirichlet,
+                                         neumann)
+        L.check(self.lib.shk_host_stepper_set_boundary(self._hs, lk, rk, L.ptr(d), L.ptr(nm),
+                                                       L.stream_handle()),
+                "host_stepper_set_boundary")
+        self._bc_keep = (d, nm)
 
     def status(self) -> int:
         st = ctypes.c_int32()
@@ -264,21 +292,7 @@ class BatchedSolver:
         ghosts and instances; *neumann*: gradients ``(B, 2)`` or ``(2,)``.
         The adjoint of such a plan is the exact transpose with the boundary
         data as constants."""
-        kinds = {"periodic": L.SHK_BC_PERIODIC, "dirichlet": L.SHK_BC_DIRICHLET,
-                 "neumann": L.SHK_BC_NEUMANN}
-        right = left if right is None else right
-        lk, rk = kinds[left], kinds[right]
-
-        def table(v, shape):
-            if v is None:
-                return None
-            t = torch.as_tensor(v, dtype=torch.float64, device=self.device)
-            if t.dim() == 1 and t.numel() == 2:
-                t = t.reshape((1, 2) + (1,) * (len(shape) - 2)).expand((self.B,) + shape[1:])
-            return t.reshape(shape).contiguous()
-
-        d = table(dirichlet, (self.B, 2, 3))
-        nm = table(neumann, (self.B, 2))
+        lk, rk, d, nm = _boundary_tables(self.B, self.device, left, right, dirichlet, neumann)
         L.check(self.lib.shk_plan_set_boundary(self._plan, lk, rk, L.ptr(d), L.ptr(nm),
                                                L.stream_handle()), "plan_set_boundary")
         self._bc_keep = (d, nm)

@@ -26,6 +26,7 @@ struct shk_host_stepper {
     size_t elem = 8;
     std::vector<shk_plan*> plans;
     std::vector<int64_t> cell0;  // first packed cell of each chunk, nchunks + 1
+    std::vector<int32_t> inst0;  // first instance of each chunk, nchunks + 1
     std::vector<void*> ua, ub;   // device state buffers of each chunk
     cudaStream_t h2d = nullptr, d2h = nullptr, comp[2] = {nullptr, nullptr};
     std::vector<cudaEvent_t> ev_in, ev_done;
@@ -116,6 +117,7 @@ int shk_host_stepper_create(const shk_scheme* scheme, int32_t batch, const int64
         if (st != SHK_OK) break;
         hs->plans.push_back(p);
         hs->cell0.push_back(h_offsets[b0] - h_offsets[0]);
+        hs->inst0.push_back(b0);
         const size_t bytes = hs->elem * size_t(off.back());
         void *a = nullptr, *b = nullptr;
         if (cudaMalloc(&a, bytes) != cudaSuccess || cudaMalloc(&b, bytes) != cudaSuccess) {
@@ -127,6 +129,7 @@ int shk_host_stepper_create(const shk_scheme* scheme, int32_t batch, const int64
         hs->ub.push_back(b);
     }
     hs->cell0.push_back(h_offsets[batch] - h_offsets[0]);
+    hs->inst0.push_back(batch);
     if (st == SHK_OK) {
         bool ok = cudaStreamCreateWithFlags(&hs->h2d, cudaStreamNonBlocking) == cudaSuccess &&
                   cudaStreamCreateWithFlags(&hs->d2h, cudaStreamNonBlocking) == cudaSuccess &&
@@ -187,6 +190,17 @@ int shk_host_stepper_advance(shk_host_stepper* hs, const void* h_in, void* h_out
     HS_CUDA(cudaEventRecord(hs->ev_end[1], hs->comp[0]));
     HS_CUDA(cudaEventRecord(hs->ev_end[2], hs->comp[1]));
     for (cudaEvent_t e : hs->ev_end) HS_CUDA(cudaStreamWaitEvent(st, e, 0));
+    return SHK_OK;
+}
+
+int shk_host_stepper_set_boundary(shk_host_stepper* hs, int32_t left, int32_t right,
+                                  const double* dirichlet, const double* neumann, void* stream) {
+    if (!hs) return SHK_EINVAL;
+    for (int c = 0; c < hs->nchunks; ++c) {
+        const size_t b0 = static_cast<size_t>(hs->inst0[c]);
+        HS_OK(shk_plan_set_boundary(hs->plans[c], left, right, dirichlet ? dirichlet + 6 * b0 : nullptr,
+                                    neumann ? neumann + 2 * b0 : nullptr, stream));
+    }
     return SHK_OK;
 }
 

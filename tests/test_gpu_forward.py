@@ -257,6 +257,29 @@ def test_host_stepper_equals_device_plan(gb, dtype, chunks):
     assert hs.status() == 0
 
 
+def test_host_stepper_with_boundaries_equals_device_plan(gb):
+    """Dirichlet / Neumann instance data reach every chunk of the host stepper."""
+    from pyshocks_gb300.batched import BatchedSolver, HostStepper
+
+    sizes = [1024, 700, 2048, 96, 3000]
+    rng = np.random.default_rng(37)
+    u0 = np.concatenate([R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes])
+    scheme = _scheme(gb, "rusanov")
+    dx = [2.0 / n for n in sizes]
+    bnd = rng.uniform(-1, 1, (len(sizes), 2, 3))
+    grad = rng.uniform(-1, 1, (len(sizes), 2))
+    for kind, kw in (("dirichlet", {"dirichlet": bnd}), ("neumann", {"neumann": grad})):
+        ref = BatchedSolver(scheme, sizes, dx)
+        ref.set_boundary(kind, **kw)
+        ref.reset(torch.tensor(u0, device="cuda"))
+        ref.step(5)
+        hs = HostStepper(scheme, sizes, dx, chunks=3)
+        hs.set_boundary(kind, **kw)
+        out = hs.advance(torch.tensor(u0).pin_memory(), nsteps=5)
+        torch.cuda.current_stream().synchronize()
+        assert torch.equal(out, ref.u.cpu()), kind
+
+
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_host_stepper_learned_equals_device_plan(gb, dtype):
     """The host-buffer stepper with the learned reconstruction (mixed float64
