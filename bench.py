@@ -497,7 +497,7 @@ def bench_fp32(scheme, sizes, u0, stream, args) -> dict:
 
 
 def _adjoint_rate(scheme, dev, nsteps, dtype, B=256, n=4096, tile="auto") -> dict:
-    """B Burgers instances, N=4096, config-1 initial condition,
+    """B Burgers instances, N=4096, initial condition 0.5 + sin(pi x) (cell averages),
     J = 1/2 |u(T) - u_target|^2, sqrt(n)-checkpointed reverse sweep. One
     gradient = one instance's full dJ/du0."""
     import torch

@@ -62,7 +62,7 @@ typedef struct {
     int32_t equation;  /* SHK_EQ_*                                           */
     int32_t limiter;   /* SHK_REC_MUSCL / MUSCLS: SHK_LIM_* (its theta or van
                         * Albada variant in delta, the slope-ratio cut atol in eps) */
-    double eps;        /* WENO epsilon (WENOJS53 default 1e-12; configs 1e-6) */
+    double eps;        /* WENO epsilon (WENOJS53 default 1e-12; the bench's 1e-6) */
     double delta;      /* ES-WENO delta (bound to dx^2 by burgers bind)       */
     double nu;         /* Rusanov artificial viscosity dx^(alpha-1); 1 if alpha=1 */
     double speed;      /* linear advection velocity (SHK_EQ_ADVECTION)        */

@@ -154,7 +154,7 @@ def generate_pairs(
     device="cuda",
 ):
     """Training pairs from the plain FP64 solver: fine runs at ``n_coarse *
-    ratio`` cells (Rusanov + WENO-JS5, eps 1e-6) from config-1-like and
+    ratio`` cells (Rusanov + WENO-JS5, eps 1e-6) from 0.5 + sin(pi x)-like and
     random-Fourier initial conditions, sampled every ``steps_between`` steps and
     restricted to ``n_coarse`` cells. Returns float32 cell samples
     ``(stencils[n, 5], targets[n, 2], weights[n])``: the stencil
@@ -189,8 +189,8 @@ def generate_pairs(
 
 
 def _initial_conditions(rng, B: int, n: int, device) -> torch.Tensor:
-    """Exact cell averages of a mix of ``m + A sin(k pi x + phi)`` (the config-1
-    family) and random 8-mode Fourier series with 0-3 jumps."""
+    """Exact cell averages of a mix of ``m + A sin(k pi x + phi)`` (the family of
+    0.5 + sin(pi x)) and random 8-mode Fourier series with 0-3 jumps."""
     f = torch.linspace(-1.0, 1.0, n + 1, dtype=torch.float64, device=device)
     fl, fr = f[:-1], f[1:]
     h = 2.0 / n
@@ -292,7 +292,7 @@ class Trainer:
 def train_default(*, n_ics: int = 640, epochs: int = 64, reg: float = 0.1, seed: int = 0,
                   lr: float = 1.0e-2, batch: int = 32768):
     """Train the default network: 5.2e6 cells (1.05e7 face targets; N = 256
-    restricted from N = 4096, Burgers and linear advection, config-1-like and
+    restricted from N = 4096, Burgers and linear advection, 0.5 + sin(pi x)-like and
     random-Fourier initial conditions), Adam with cosine decay to 1e-4.
     Returns ``(params, loss history)``. The committed default was made with
     these arguments and ``NORM_EPS`` (the face loss falls from 6.3e-4 to

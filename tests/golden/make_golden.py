@@ -188,9 +188,9 @@ def main(refdir: pathlib.Path) -> None:
         return fn
 
     # the parity workload: N = 256, t_final = 1, CFL 0.5
-    out["config1_rusanov_n256"] = run("rusanov", 256, sine_ic, tfinal=1.0)
-    out["config1_lf_n256"] = run("lf", 256, sine_ic, tfinal=1.0)
-    out["config1_esweno_n256"] = run("esweno", 256, sine_ic, tfinal=1.0)
+    out["sine_rusanov_n256"] = run("rusanov", 256, sine_ic, tfinal=1.0)
+    out["sine_lf_n256"] = run("lf", 256, sine_ic, tfinal=1.0)
+    out["sine_esweno_n256"] = run("esweno", 256, sine_ic, tfinal=1.0)
     # short fixed-count runs on random data (the batched workload's generator)
     for seed, n in [(11, 64), (12, 96), (13, 128), (14, 50)]:
         out[f"fourier_rusanov_n{n}_s{seed}"] = run("rusanov", n, fourier_ic(seed), maxit=40)
@@ -227,8 +227,8 @@ def main(refdir: pathlib.Path) -> None:
     out["muscls_eo_mc_n128_s54"] = run("eo-muscls_mc", 128, fourier_ic(54), maxit=40)
 
     # Godunov / Engquist-Osher fluxes and the constant / WENO-JS32 reconstructions
-    out["config1_godunov_wenojs53_n256"] = run("godunov-wenojs53", 256, sine_ic, tfinal=1.0)
-    out["config1_eo_wenojs53_n256"] = run("eo-wenojs53", 256, sine_ic, tfinal=1.0)
+    out["sine_godunov_wenojs53_n256"] = run("godunov-wenojs53", 256, sine_ic, tfinal=1.0)
+    out["sine_eo_wenojs53_n256"] = run("eo-wenojs53", 256, sine_ic, tfinal=1.0)
     for sname in ("rusanov", "godunov", "eo"):
         for rname, seed in (("constant", 41), ("wenojs32", 42)):
             out[f"fourier_{sname}_{rname}_n96_s{seed}"] = run(f"{sname}-{rname}", 96,

@@ -190,7 +190,7 @@ def test_autograd_function_backward():
     assert float(err) < 1.0e-9
 
 
-def test_config3_size_gradient_16_directions():
+def test_n4096_gradient_16_directions():
     """The adjoint configuration's check at its instance size (N = 4096): dJ/du0
     along 16 random directions against central differences (h = 1e-6) of the
     GPU forward itself, replaying the recorded dt sequence (frozen dt, as

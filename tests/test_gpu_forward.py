@@ -126,12 +126,12 @@ def test_fused_step_matches_oracle(gb, kind, eq, n):
     assert err < 1.0e-12, err
 
 
-@pytest.mark.parametrize("name,kind", [("config1_rusanov_n256", "rusanov"),
-                                       ("config1_esweno_n256", "esweno"),
-                                       ("config1_lf_n256", "lf"),
-                                       ("config1_godunov_wenojs53_n256", "godunov-wenojs53"),
-                                       ("config1_eo_wenojs53_n256", "eo-wenojs53")])
-def test_config1_step_api_matches_reference(gb, name, kind):
+@pytest.mark.parametrize("name,kind", [("sine_rusanov_n256", "rusanov"),
+                                       ("sine_esweno_n256", "esweno"),
+                                       ("sine_lf_n256", "lf"),
+                                       ("sine_godunov_wenojs53_n256", "godunov-wenojs53"),
+                                       ("sine_eo_wenojs53_n256", "eo-wenojs53")])
+def test_sine_n256_step_api_matches_reference(gb, name, kind):
     """N=256 Burgers to t_final = 1 through the reference-style ``step()`` API:
     within 1e-10 max-abs of the reference's own solution (golden vectors from
     its source) and the same number of steps."""
@@ -153,12 +153,12 @@ def test_config1_step_api_matches_reference(gb, name, kind):
     assert err < 1.0e-10, err
 
 
-def test_config1_batched_plan_matches_reference(gb):
+def test_sine_n256_batched_plan_matches_reference(gb):
     """The same workload through the batched persistent plan (device-side dt,
     final-time clip and +1e-15)."""
     from pyshocks_gb300.batched import BatchedSolver
 
-    g = _golden("config1_rusanov_n256")
+    g = _golden("sine_rusanov_n256")
     scheme = _scheme(gb, "rusanov")
     solver = BatchedSolver(scheme, [256], 2.0 / 256, theta=1.0, max_steps=512)
     solver.reset(torch.tensor(g["u0"][3:-3]), tfinal=1.0)

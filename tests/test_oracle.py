@@ -52,9 +52,9 @@ def test_recon_golden(name, rec):
 
 
 RUNS = [
-    ("config1_rusanov_n256", "rusanov", "burgers", {"tfinal": 1.0}),
-    ("config1_lf_n256", "lf", "burgers", {"tfinal": 1.0}),
-    ("config1_esweno_n256", "esweno", "burgers", {"tfinal": 1.0}),
+    ("sine_rusanov_n256", "rusanov", "burgers", {"tfinal": 1.0}),
+    ("sine_lf_n256", "lf", "burgers", {"tfinal": 1.0}),
+    ("sine_esweno_n256", "esweno", "burgers", {"tfinal": 1.0}),
     ("fourier_rusanov_n64_s11", "rusanov", "burgers", {"maxit": 40}),
     ("fourier_rusanov_n96_s12", "rusanov", "burgers", {"maxit": 40}),
     ("fourier_rusanov_n128_s13", "rusanov", "burgers", {"maxit": 40}),
@@ -62,8 +62,8 @@ RUNS = [
     ("fourier_lf_n64_s21", "lf", "burgers", {"maxit": 40}),
     ("fourier_esweno_n64_s22", "esweno", "burgers", {"maxit": 40}),
     ("lwr_rusanov_n128_s31", "rusanov", "lwr", {"maxit": 60}),
-    ("config1_godunov_wenojs53_n256", "godunov", "burgers", {"tfinal": 1.0}),
-    ("config1_eo_wenojs53_n256", "eo", "burgers", {"tfinal": 1.0}),
+    ("sine_godunov_wenojs53_n256", "godunov", "burgers", {"tfinal": 1.0}),
+    ("sine_eo_wenojs53_n256", "eo", "burgers", {"tfinal": 1.0}),
 ] + [(f"fourier_{f}_{r}_n96_s{s}", f, "burgers", {"maxit": 40})
      for f in ("rusanov", "godunov", "eo") for r, s in (("constant", 41), ("wenojs32", 42))]
 
