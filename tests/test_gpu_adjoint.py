@@ -191,7 +191,7 @@ def test_autograd_function_backward():
 
 
 def test_n4096_gradient_16_directions():
-    """The adjoint configuration's check at its instance size (N = 4096): dJ/du0
+    """The adjoint benchmark's check at its instance size (N = 4096): dJ/du0
     along 16 random directions against central differences (h = 1e-6) of the
     GPU forward itself, replaying the recorded dt sequence (frozen dt, as
     adjoint_step), with J = 1/2 |u(T) - u_target|^2 and sqrt(n) checkpoints."""
