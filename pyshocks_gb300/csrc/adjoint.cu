@@ -94,14 +94,16 @@ __device__ __forceinline__ T damax_dx(T x, T y, T c) {
     return chi * sgn(sx) * speed_prime<EQ, T>();
 }
 
-// Backward of weno53_cell (device.cuh): given the cotangents of ur (urb) and
-// ul (ulb) of cell c, the contributions t_o to the cotangents of v_{c+o},
-// o = -2..2. Inputs as for weno53_cell.
+// Backward of the WENO-JS5 reconstruction of cell c in half differences
+// (device.cuh): given the cotangents of ur (urb) and ul (ulb), the
+// contributions t_o to the cotangents of v_{c+o}, o = -2..2. The face values
+// themselves come from the forward's face pass; the backward recomputes the
+// weights in the half-difference form.
 template <class T>
 __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1, T D0, T Dp1,
                                                 T Qm1, T Q0, T Qp1, T eps, T urb, T ulb, T& t0,
                                                 T& t1, T& t2, T& t3, T& t4) {
-    // forward quantities (as weno53_cell)
+    // forward quantities (weights in product form)
     const T h0 = fma(T(2), Hm1, Dm1);
     const T h1 = H0 + Hm1;
     const T h2 = fma(T(-2), H0, Dp1);
@@ -184,8 +186,8 @@ __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1
 
 // z_i = dt (J_L(v)^T w)_i for i in [lo, hi); v valid on [lo-6, hi+6), w on
 // [lo-3, hi+3). Rusanov flux, WENO-JS5 or learned reconstruction.
-// cul, cur: the face values of v on [lo-3, hi+3) when the forward recompute
-// kept them (WENO-JS5; null: reconstructed here)
+// cul, cur (WENO-JS5): the face values of v on [lo-3, hi+3) as the forward's
+// face pass forms them (stored by the replay, or kept by the recompute)
 template <class T, int EQ, int REC>
 __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const AdjSmem<T>& a,
                           const OpParams<T>& p, T dtdx, const T* cul = nullptr,
@@ -257,18 +259,6 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
     __syncthreads();
     const T* UL = cul;
     const T* UR = cur;
-    if (!cul) {
-        for (int c = lo - 3 + tid; c < hi + 3; c += nt) {
-            T ul, ur;
-            weno53_cell<T>(v[c], a.H[c - 2], a.H[c - 1], a.H[c], a.H[c + 1], a.D[c - 1], a.D[c],
-                           a.D[c + 1], a.Q[c - 1], a.Q[c], a.Q[c + 1], p.eps, ul, ur);
-            a.UL[c] = ul;
-            a.UR[c] = ur;
-        }
-        __syncthreads();
-        UL = a.UL;
-        UR = a.UR;
-    }
     // face j+1/2: F = 1/2 (f(L) + f(R)) - nu/2 a (L - R), L = ul_{j+1}, R = ur_j
     for (int j = lo - 3 + tid; j < hi + 2; j += nt) {
         const T fb = (w[j + 1] - w[j]) * dtdx;

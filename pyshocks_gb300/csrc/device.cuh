@@ -107,69 +107,20 @@ __device__ __forceinline__ double rcp_nr(double x) {
 }
 
 // ---- WENO-JS 5/3 reconstruction of one cell -------------------------------
-// Inputs (window arrays, cell c): v_c, half differences H_k = (v_{k+1}-v_k)/2 for
-// k = c-2..c+1, half second differences D_k = H_k - H_{k-1} and
-// Q_k = 13/12 (2 D_k)^2 for k = c-1..c+1.
+// In half differences (the form of the reverse step's weno53_cell_vjp): cell
+// c, H_k = (v_{k+1}-v_k)/2 for k = c-2..c+1, D_k = H_k - H_{k-1} and
+// Q_k = 13/12 (2 D_k)^2 for k = c-1..c+1;
 // beta_0 = Q_{c-1} + (D_{c-1} + 2 H_{c-1})^2
 // beta_1 = Q_c     + (H_c + H_{c-1})^2
 // beta_2 = Q_{c+1} + (D_{c+1} - 2 H_c)^2
-// which are 13/12 q1^2 + 1/4 q2^2 of src/pyshocks/weno.py:219-228.
-template <class T>
-__device__ __forceinline__ void weno53_cell(T v, T Hm2, T Hm1, T H0, T Hp1, T Dm1, T D0,
-                                            T Dp1, T Qm1, T Q0, T Qp1, T eps, T& ul,
-                                            T& ur) {
-    const T h0 = fma(T(2), Hm1, Dm1);
-    const T h1 = H0 + Hm1;
-    const T h2 = fma(T(-2), H0, Dp1);
-    const T b0 = fma(h0, h0, Qm1);
-    const T b1 = fma(h1, h1, Q0);
-    const T b2 = fma(h2, h2, Qp1);
-    T s0 = eps + b0; s0 = s0 * s0;
-    T s1 = eps + b1; s1 = s1 * s1;
-    T s2 = eps + b2; s2 = s2 * s2;
-    // alpha_k = d_k / s_k (weno.py:254). f64: product form P_k = prod_{j!=k} s_j
-    // (proportional to 1/s_k, no reciprocal); f32: P_k = 1/s_k, which cannot
-    // underflow when eps^4 is below the float range. The float reciprocals are
-    // the one-instruction approximate ones (about 1 ulp): the float state
-    // itself carries 2^-24 relative rounding per stage.
-    T P0, P1, P2;
-    if constexpr (sizeof(T) == 8) {
-        P0 = s1 * s2; P1 = s0 * s2; P2 = s0 * s1;
-    } else {
-        P0 = rcp_approx_f32(s0); P1 = rcp_approx_f32(s1); P2 = rcp_approx_f32(s2);
-    }
-    // 6 (uhat_k - v) of the right side (weno.py:231-239), d_k folded (1, 6, 3):
-    //   uhat_0: -2 d_{c-2} + 5 d_{c-1}       -> -4 H_{c-2} + 10 H_{c-1}
-    //   6 uhat_1:  6 (d_{c-1} + 2 d_c)       -> 12 H_{c-1} + 24 H_c
-    //   3 uhat_2:  3 (4 d_c - d_{c+1})       -> 24 H_c - 6 H_{c+1}
-    const T cr0 = fma(T(10), Hm1, T(-4) * Hm2);
-    const T cr1 = fma(T(24), H0, T(12) * Hm1);
-    const T cr2 = fma(T(-6), Hp1, T(24) * H0);
-    // mirrored left side (reconstruction.py:375)
-    const T cl0 = fma(T(-10), H0, T(4) * Hp1);
-    const T cl1 = fma(T(-24), Hm1, T(-12) * H0);
-    const T cl2 = fma(T(-24), Hm1, T(6) * Hm2);
-    const T nr = fma(P0, cr0, fma(P1, cr1, P2 * cr2));
-    const T nl = fma(P2, cl0, fma(P1, cl1, P0 * cl2));
-    const T m = T(36) * P1;
-    const T dr = fma(T(6), P0, fma(T(18), P2, m));
-    const T dl = fma(T(6), P2, fma(T(18), P0, m));
-    if constexpr (sizeof(T) == 8) {
-        const T r = rcp_nr(dr * dl);
-        ur = fma(nr * dl, r, v);
-        ul = fma(nl * dr, r, v);
-    } else {
-        ur = fma(nr, rcp_approx_f32(dr), v);
-        ul = fma(nl, rcp_approx_f32(dl), v);
-    }
-}
-
-// Forward-path variant of weno53_cell on unscaled differences (fewer FP64
-// instructions): d_k = v_{k+1} - v_k, E_k = d_k - d_{k-1}, G_k = 13/3 E_k^2 + 4 eps,
+// which are 13/12 q1^2 + 1/4 q2^2 of src/pyshocks/weno.py:219-228; the
+// weights alpha_k = d_k / (eps + beta_k)^2 (weno.py:254) in product form.
+// The forward reconstruction on unscaled differences (fewer FP64
+// instructions than half differences): d_k = v_{k+1} - v_k, E_k = d_k - d_{k-1}, G_k = 13/3 E_k^2 + 4 eps,
 // and 4 (beta_j + eps) = G + h'^2 with h'_0 = E_{c-1} + 2 d_{c-1}, h'_1 = d_c + d_{c-1},
 // h'_2 = E_{c+1} - 2 d_c. Every s_j and P_j is thus scaled by a common power
 // of two, which cancels in the normalised weights. The
-// corrections 6 (uhat_k - v) (weights (1, 6, 3) folded as in weno53_cell) use
+// corrections 6 (uhat_k - v), with the ideal weights (1, 6, 3)/10 folded in, use
 // d_{c-2} = 3 d_{c-1} - h'_0 and d_{c+1} = h'_2 + 3 d_c:
 //   cr0 = 2 h'_0 - d_{c-1}      cr1 = 6 d_{c-1} + 12 d_c     cr2 = 3 (d_c - h'_2)
 //   cl0 = 2 h'_2 + d_c          cl1 = 6 E_c - cr1            cl2 = -3 (h'_0 + d_{c-1})
