@@ -149,7 +149,8 @@ typedef struct shk_plan shk_plan;
 
 typedef struct {
     int32_t dtype;        /* SHK_F64 / SHK_F32                                  */
-    int32_t tile;         /* cells per work item (0 = default; at least 512 with
+    int32_t tile;         /* cells per work item (0 = the library's choice for the
+                           * scheme, precision and max_steps; at least 512 with
                            * the learned reconstruction)                         */
     int32_t max_steps;    /* capacity of the dt history (0 = no history)        */
     int32_t ctas_per_sm;  /* persistent grid size per SM (0 = occupancy)         */

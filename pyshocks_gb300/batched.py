@@ -153,7 +153,8 @@ class BatchedSolver:
     :arg theta: Courant factor of the driver closure ``theta * predict_timestep``.
     :arg dtype: ``torch.float64`` or ``torch.float32`` state.
     :arg max_steps: capacity of the per-step dt history (for the adjoint).
-    :arg tile: cells per work item (0: the library default, 1024; ``"auto"``:
+    :arg tile: cells per work item (0: the library default, which depends on
+        the scheme, precision and whether the plan keeps a dt history; ``"auto"``:
         chosen with ``ctas_per_sm`` by :func:`pyshocks_gb300.autotune.tune`).
     :arg ctas_per_sm: resident CTAs per SM of the persistent grid (0: as many
         as the shared memory allows, at most 8).

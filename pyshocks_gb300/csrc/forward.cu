@@ -370,6 +370,18 @@ int cuda_check(cudaError_t e) {
         if (_st != SHK_OK) return _st;                  \
     } while (0)
 
+// the library's tile when the caller gives none: the shapes the autotuner
+// picks on the bench batches (plans that keep a dt history are tuned for
+// their reverse step, whose shared memory grows with the tile)
+int default_tile(const shk_scheme* s, int dtype, int max_steps) {
+    if (s->rec == SHK_REC_LEARNED) return max_steps > 0 ? 1024 : 2048;
+    if (s->rec == SHK_REC_WENOJS53 && s->flux == SHK_FLUX_RUSANOV) {
+        if (dtype == SHK_F32) return max_steps > 0 ? 1024 : 2048;
+        return max_steps > 0 ? 512 : kDefaultTile;
+    }
+    return kDefaultTile;
+}
+
 bool valid_scheme(const shk_scheme* s) {
     if (!s) return false;
     if (s->flux < 0 || s->flux > SHK_FLUX_EO) return false;
@@ -756,7 +768,7 @@ int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_of
     if (scheme->flux == SHK_FLUX_LF) return SHK_EUNSUPPORTED;
     const int dtype = opts ? opts->dtype : SHK_F64;
     if (dtype != SHK_F64 && dtype != SHK_F32) return SHK_EINVAL;
-    int tile = (opts && opts->tile > 0) ? opts->tile : kDefaultTile;
+    int tile = (opts && opts->tile > 0) ? opts->tile : default_tile(scheme, dtype, opts ? opts->max_steps : 0);
     const int align = dtype == SHK_F64 ? 2 : 4;
     if (tile % align || tile < 16 || tile > 8192) return SHK_EINVAL;
     // the learned phase's warp scratch lives in the window's free arrays
