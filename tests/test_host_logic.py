@@ -1,0 +1,58 @@
+"""Host-side logic that needs no GPU: boundary tables, the autotuner's
+candidate shapes and shared-memory estimates, packing and the instance
+partition."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+from pyshocks_gb300 import _lib as L
+from pyshocks_gb300 import autotune
+from pyshocks_gb300.batched import _boundary_tables, pack_offsets, partition_instances
+
+
+def test_boundary_tables_broadcast_and_kinds():
+    lk, rk, d, nm = _boundary_tables(3, torch.device("cpu"), "dirichlet", None, [0.5, -0.25], None)
+    assert (lk, rk) == (L.SHK_BC_DIRICHLET, L.SHK_BC_DIRICHLET)
+    assert d.shape == (3, 2, 3) and d.dtype == torch.float64 and nm is None
+    assert torch.all(d[:, 0, :] == 0.5) and torch.all(d[:, 1, :] == -0.25)
+    full = np.arange(12.0).reshape(2, 2, 3)
+    _, _, d2, _ = _boundary_tables(2, torch.device("cpu"), "dirichlet", "neumann", full,
+                                   [[1.0, 2.0], [3.0, 4.0]])
+    assert torch.equal(d2, torch.tensor(full))
+    lk, rk, d, nm = _boundary_tables(4, torch.device("cpu"), "neumann", None, None, [0.0, 1.0])
+    assert (lk, rk) == (L.SHK_BC_NEUMANN, L.SHK_BC_NEUMANN)
+    assert nm.shape == (4, 2) and torch.all(nm[:, 1] == 1.0)
+    with pytest.raises(KeyError):
+        _boundary_tables(1, torch.device("cpu"), "reflecting", None, None, None)
+
+
+def test_autotune_candidates_fit_shared_memory():
+    smem = autotune.SMEM_PER_SM
+    for dtype in (torch.float64, torch.float32):
+        for learned in (False, True):
+            for adjoint in (False, True):
+                weno5 = not learned
+                cands = autotune.candidates(dtype, 16384, learned, adjoint, weno5)
+                assert cands, (dtype, learned, adjoint)
+                for tile, cps in cands:
+                    per = autotune._smem_bytes(tile, dtype, learned, weno5)
+                    assert per <= smem and (cps == 0 or cps * per <= smem)
+                    if adjoint:
+                        assert autotune._adjoint_smem_bytes(tile, dtype, learned) <= smem
+    # short instances: no tile longer than twice the largest instance (but 512 stays)
+    assert all(t <= 512 for t, _ in autotune.candidates(torch.float64, 100))
+    # the float WENO-JS5 step's 6-array layout admits 4 CTAs of tile 2048
+    assert (2048, 4) in autotune.candidates(torch.float32, 16384, weno5=True)
+
+
+def test_pack_offsets_and_partition():
+    sizes = [5, 1024, 3, 77, 2048, 96]
+    off = pack_offsets(sizes)
+    assert off[0] == 0 and np.all(np.diff(off) == sizes)
+    parts = partition_instances(sizes, 3)
+    assert sorted(np.concatenate(parts).tolist()) == list(range(len(sizes)))
+    loads = [sum(sizes[i] for i in p) for p in parts]
+    assert max(loads) == 2048  # LPT: the largest instance alone bounds the makespan
