@@ -252,3 +252,27 @@ def test_stored_stages_and_faces_give_the_same_gradient(boundary):
         grads.append(cs.backward(p_T))
         assert solver.status() == 0
     assert torch.equal(grads[0], grads[1])
+
+
+def test_plain_results_do_not_depend_on_the_tile():
+    """Plain WENO-JS5 in double: forward steps and reverse sweeps give the same
+    values, bit for bit, at tiles of 64, 512 and 1024 cells (more halo than
+    interior, the reverse sweep's default, the forward's default)."""
+    from pyshocks_gb300.adjoint import CheckpointedSolve
+    from pyshocks_gb300.batched import BatchedSolver
+
+    sizes = [4096, 1500, 600, 96]
+    nsteps = 9
+    rng = np.random.default_rng(47)
+    u0 = np.concatenate([R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes])
+    p_T = torch.tensor(rng.standard_normal(u0.size), device="cuda")
+    outs, grads = [], []
+    for tile in (64, 512, 1024):
+        s = BatchedSolver(_scheme(), sizes, [2.0 / n for n in sizes], tile=tile, max_steps=nsteps)
+        cs = CheckpointedSolve(s, nsteps, stride=4)
+        outs.append(cs.forward(torch.tensor(u0)).clone())
+        grads.append(cs.backward(p_T))
+        assert s.status() == 0
+    for o, g in zip(outs[1:], grads[1:]):
+        assert torch.equal(o, outs[0])
+        assert torch.equal(g, grads[0])

@@ -224,3 +224,32 @@ def test_trained_network_gains_over_plain_wenojs_and_untrained():
     lu = learned.Trainer(learned.init_params(seed=0), reg=0.0)
     assert float(lt.loss_and_grad(s, t, w)) < 0.9 * float(lu.loss_and_grad(s, t, w))
     del rng
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_learned_results_do_not_depend_on_the_tile(dtype):
+    """Forward steps and reverse sweeps with the learned reconstruction give
+    the same values, bit for bit, at the shortest allowed tile (512: the warp
+    scratch just fits), an odd one and the longest default (halo recompute,
+    partial tiles and the scratch placement never change a cell's arithmetic)."""
+    from pyshocks_gb300 import learned
+    from pyshocks_gb300.adjoint import CheckpointedSolve
+    from pyshocks_gb300.batched import BatchedSolver
+
+    sizes = [4096, 1500, 600, 2048]
+    nsteps = 9
+    rng = np.random.default_rng(43)
+    u0 = np.concatenate([R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes])
+    p_T = torch.tensor(rng.standard_normal(u0.size), device="cuda", dtype=dtype)
+    sch = _scheme(learned.load_default_params())
+    outs, grads = [], []
+    for tile in (512, 1000, 2048):
+        s = BatchedSolver(sch, sizes, [2.0 / n for n in sizes], dtype=dtype, tile=tile,
+                          max_steps=nsteps)
+        cs = CheckpointedSolve(s, nsteps, stride=4)
+        outs.append(cs.forward(torch.tensor(u0)).clone())
+        grads.append(cs.backward(p_T))
+        assert s.status() == 0
+    for o, g in zip(outs[1:], grads[1:]):
+        assert torch.equal(o, outs[0])
+        assert torch.equal(g, grads[0])
