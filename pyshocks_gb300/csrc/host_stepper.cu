@@ -7,7 +7,7 @@
 // stream (after the steps' event), so the copies of one chunk overlap the
 // steps of the others and the two copy directions overlap each other. With
 // pinned host buffers the call costs about the steps plus one chunk's copies;
-// with pageable buffers the copies are staged by the driver and overlap less.
+// with pageable buffers the CUDA runtime stages the copies and they overlap less.
 //
 // Every instance is independent (its own dt from its own wave-speed maximum),
 // so the result is bit-identical to one plan over the whole batch.
