@@ -196,6 +196,16 @@ int shk_plan_set_fixed_dt(shk_plan* plan, const double* dt, int32_t nsteps, void
 int shk_plan_set_boundary(shk_plan* plan, int32_t left, int32_t right, const double* dirichlet,
                           const double* neumann, void* stream);
 
+/* time-dependent boundary data (the g(t, x) of scalar.py:397-511 at the stage
+ * times t, t + dt, t + dt/2 of each step): dirichlet [nsteps][3][B][2][3],
+ * neumann [nsteps][3][B][2] (device or host memory, copied on `stream`);
+ * step k >= nsteps takes row nsteps - 1. The caller evaluates the data at its
+ * stage times, so the tables go with prescribed steps (shk_plan_set_fixed_dt).
+ * Drops a captured step graph. */
+int shk_plan_set_boundary_steps(shk_plan* plan, int32_t left, int32_t right,
+                                const double* dirichlet, const double* neumann, int32_t nsteps,
+                                void* stream);
+
 /* capture two steps (u_a -> u_b -> u_a) into a CUDA graph and replay it
  * nsteps/2 times (nsteps must be even). */
 int shk_plan_step_graph(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps,

@@ -105,6 +105,7 @@ SIGNATURES: dict[str, tuple] = {
     "shk_plan_step_graph": (ctypes.c_int, [_P, _P, _P, _I32, _P]),
     "shk_plan_set_fixed_dt": (ctypes.c_int, [_P, _P, _I32, _P]),
     "shk_plan_set_boundary": (ctypes.c_int, [_P, _I32, _I32, _P, _P, _P]),
+    "shk_plan_set_boundary_steps": (ctypes.c_int, [_P, _I32, _I32, _P, _P, _I32, _P]),
     "shk_plan_state": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "shk_plan_copy_time": (ctypes.c_int, [_P, _P, _P]),
     "shk_plan_copy_dt_history": (ctypes.c_int, [_P, _P, _P]),

@@ -298,6 +298,34 @@ class BatchedSolver:
                                                L.stream_handle()), "plan_set_boundary")
         self._bc_keep = (d, nm)
 
+    def set_boundary_steps(self, left: str, right: str | None = None, *, dirichlet=None,
+                           neumann=None) -> None:
+        """Time-dependent boundary data: *dirichlet* ``(nsteps, 3, B, 2, 3)``
+        ghost values or *neumann* ``(nsteps, 3, B, 2)`` gradients at the stage
+        times ``t, t + dt, t + dt/2`` of each step (steps past the table take
+        its last row). The caller evaluates them at its stage times, so they
+        go with prescribed steps (:meth:`set_fixed_dt`)."""
+        kinds = {"periodic": L.SHK_BC_PERIODIC, "dirichlet": L.SHK_BC_DIRICHLET,
+                 "neumann": L.SHK_BC_NEUMANN}
+        right = left if right is None else right
+
+        def table(v, tail):
+            if v is None:
+                return None
+            t = torch.as_tensor(v, dtype=torch.float64, device=self.device).contiguous()
+            if t.dim() != 3 + len(tail) or t.shape[1] != 3 or tuple(t.shape[2:]) != (self.B,) + tail:
+                raise ValueError(f"expected (nsteps, 3, {self.B}, {', '.join(map(str, tail))}), "
+                                 f"got {tuple(t.shape)}")
+            return t
+
+        d = table(dirichlet, (2, 3))
+        nm = table(neumann, (2,))
+        nsteps = (d if d is not None else nm).shape[0] if (d is not None or nm is not None) else 0
+        L.check(self.lib.shk_plan_set_boundary_steps(self._plan, kinds[left], kinds[right], L.ptr(d),
+                                                     L.ptr(nm), int(nsteps), L.stream_handle()),
+                "plan_set_boundary_steps")
+        self._bc_keep = (d, nm)
+
     def set_fixed_dt(self, dt=None, nsteps: int | None = None) -> None:
         """Prescribe the time steps instead of the CFL step.
 

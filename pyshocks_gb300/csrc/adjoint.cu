@@ -614,7 +614,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
                                                                    const double* __restrict__ dt_row,
                                                                    OpParams<T> p,
                                                                    const void* stages,
-                                                                   int64_t total) {
+                                                                   int64_t total, int64_t step) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     constexpr bool kMixed = sizeof(T) == 8 && REC == SHK_REC_LEARNED;
@@ -646,7 +646,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
             break;
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
-        const BcView bc = plan_bc(P, b);
+        const BcView bc = plan_bc(P, b, step);
         const int64_t g0 = s0 - adj_uhalo<T>();
         const StageOut<const stage_t<T, REC>> st =
             as_const(stage_out<T, REC>(const_cast<void*>(stages), total, off));
@@ -667,7 +667,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
                                                                T* __restrict__ uout,
                                                                const double* __restrict__ dt_row,
                                                                OpParams<T> p, void* stages,
-                                                               int64_t total) {
+                                                               int64_t total, int64_t step) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ __align__(8) uint64_t bar;
     constexpr int HL = step_halo<T>();
@@ -699,7 +699,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
         step_tile<T, EQ, REC, SHK_FLUX_RUSANOV>(sm, uout ? uout + off + s0 : nullptr, te, dtdx, p,
-                                                plan_bc(P, b), s0 - HL, n,
+                                                plan_bc(P, b, step), s0 - HL, n,
                                                 stage_out<T, REC>(stages, total, off + s0));
         __syncthreads();
     }
@@ -818,11 +818,12 @@ template <class TS>
 struct AdjLaunch {
     PlanDev D; const void* um; const void* pn; void* po; const double* dt_row; OpParams<TS> p;
     size_t smem; int grid; cudaStream_t st; const void* stages = nullptr; int64_t total = 0;
+    int64_t step = 0;  // index of the forward step (its boundary data)
     template <class T, int EQ, int REC> int operator()() {
         auto k = batched_adjoint_kernel<T, EQ, REC>;
         ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(um), static_cast<const T*>(pn),
-                                         static_cast<T*>(po), dt_row, p, stages, total);
+                                         static_cast<T*>(po), dt_row, p, stages, total, step);
         return acuda(cudaGetLastError());
     }
 };
@@ -831,11 +832,12 @@ template <class TS>
 struct ReplayLaunch {
     PlanDev D; const void* uin; void* uout; const double* dt_row; OpParams<TS> p;
     size_t smem; int grid; cudaStream_t st; void* stages = nullptr; int64_t total = 0;
+    int64_t step = 0;  // index of the replayed step (its boundary data)
     template <class T, int EQ, int REC> int operator()() {
         auto k = replay_step_kernel<T, EQ, REC>;
         ADJ_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k<<<grid, kThreads, smem, st>>>(D, static_cast<const T*>(uin), static_cast<T*>(uout), dt_row, p,
-                                         stages, total);
+                                         stages, total, step);
         return acuda(cudaGetLastError());
     }
 };
@@ -994,11 +996,11 @@ int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, in
             void* out = j < cnt ? seg_at(j) : nullptr;
             if (dtype == SHK_F64) {
                 ReplayLaunch<double> f{D, seg_at(j - 1), out, row, adj_params<double>(&sch), fsmem, grid, st,
-                                       stage_at(j - 1), total};
+                                       stage_at(j - 1), total, base + j - 1};
                 r = by_scheme<double>(sch, f);
             } else {
                 ReplayLaunch<float> f{D, seg_at(j - 1), out, row, adj_params<float>(&sch), fsmem, grid, st,
-                                      stage_at(j - 1), total};
+                                      stage_at(j - 1), total, base + j - 1};
                 r = by_scheme<float>(sch, f);
             }
             if (r != SHK_OK) return r;
@@ -1007,11 +1009,11 @@ int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, in
             const double* row = D.dt_hist + size_t(base + j) * D.B;
             if (dtype == SHK_F64) {
                 AdjLaunch<double> f{D, seg_at(j), cur, nxt, row, adj_params<double>(&sch), asmem, agrid, st,
-                                    stage_at(j), total};
+                                    stage_at(j), total, base + j};
                 r = by_scheme<double>(sch, f);
             } else {
                 AdjLaunch<float> f{D, seg_at(j), cur, nxt, row, adj_params<float>(&sch), asmem, agrid, st,
-                                   stage_at(j), total};
+                                   stage_at(j), total, base + j};
                 r = by_scheme<float>(sch, f);
             }
             if (r != SHK_OK) return r;

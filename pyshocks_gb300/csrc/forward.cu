@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
             const T dtdx = item_dtdx;
             OpParams<T> pb = p;
             pb.dx = item_dx;
-            mx = step_tile<T, EQ, REC, FLUX>(sm, uout + off + s0, te, dtdx, pb, plan_bc(P, b),
+            mx = step_tile<T, EQ, REC, FLUX>(sm, uout + off + s0, te, dtdx, pb, plan_bc(P, b, k),
                                              s0 - HL, n);
         }
         const B bm = block_max<B>(mx, reinterpret_cast<B*>(red));
@@ -587,7 +587,9 @@ struct shk_plan {
     int64_t fixed_cap = 0, fixed_steps = 0;
     int bc_left = SHK_BC_PERIODIC, bc_right = SHK_BC_PERIODIC;
     double* bc_dir = nullptr;  // [B][2][3]
-    double* bc_neu = nullptr;  // [B][2]
+    double* bc_neu = nullptr;  // [B][2], or per-step [bc_steps][3][B][2]
+    int64_t bc_steps = 0;      // 0: time-independent boundary data
+    size_t bc_dir_cap = 0, bc_neu_cap = 0;  // doubles allocated
     int32_t* item_order = nullptr;  // [nitems] longest first
     unsigned int* sched = nullptr;  // [8] scheduling counters
     // host mirror of the number of steps launched since reset
@@ -605,7 +607,7 @@ struct shk_plan {
         P.partial = partial; P.B = B;
         P.dt_fixed = fixed_steps > 0 ? dt_fixed : nullptr; P.fixed_steps = fixed_steps;
         P.bc_left = bc_left; P.bc_right = bc_right; P.bc_dir = bc_dir; P.bc_neu = bc_neu; P.nitems = nitems; P.tile = tile; P.max_steps = max_steps;
-        P.item_order = item_order; P.sched = sched;
+        P.item_order = item_order; P.sched = sched; P.bc_steps = bc_steps;
         return P;
     }
 };
@@ -958,9 +960,15 @@ int shk_plan_set_fixed_dt(shk_plan* plan, const double* dt, int32_t nsteps, void
     return SHK_OK;
 }
 
-int shk_plan_set_boundary(shk_plan* plan, int32_t left, int32_t right, const double* dirichlet,
-                          const double* neumann, void* stream) {
-    if (!plan) return SHK_EINVAL;
+}  // extern "C"
+
+namespace {
+// boundary kinds and data for every instance: `rows` sets of [B][2][3]
+// Dirichlet values / [B][2] Neumann gradients (1: time-independent; else
+// steps x 3 stages)
+int set_plan_boundary(shk_plan* plan, int32_t left, int32_t right, const double* dirichlet,
+                      const double* neumann, int64_t rows, int64_t steps, void* stream) {
+    if (!plan || rows < 1) return SHK_EINVAL;
     shk_boundary b = periodic_boundary();
     b.left = left;
     b.right = right;
@@ -970,23 +978,49 @@ int shk_plan_set_boundary(shk_plan* plan, int32_t left, int32_t right, const dou
     if ((need_dir && !dirichlet) || (need_neu && !neumann)) return SHK_EINVAL;
     cudaStream_t st = as_stream(stream);
     const size_t B = static_cast<size_t>(plan->B);
-    if (need_dir && !plan->bc_dir &&
-        cudaMalloc(reinterpret_cast<void**>(&plan->bc_dir), sizeof(double) * 6 * B) != cudaSuccess)
-        return SHK_ENOMEM;
-    if (need_neu && !plan->bc_neu &&
-        cudaMalloc(reinterpret_cast<void**>(&plan->bc_neu), sizeof(double) * 2 * B) != cudaSuccess)
-        return SHK_ENOMEM;
+    auto ensure = [&](double** buf, size_t* cap, size_t n) {
+        if (*cap >= n) return true;
+        if (*buf) {
+            if (cudaStreamSynchronize(st) != cudaSuccess) return false;  // a step may still read it
+            cudaFree(*buf);
+        }
+        *buf = nullptr;
+        *cap = 0;
+        if (cudaMalloc(reinterpret_cast<void**>(buf), sizeof(double) * n) != cudaSuccess) return false;
+        *cap = n;
+        return true;
+    };
+    const size_t ndir = 6 * B * size_t(rows), nneu = 2 * B * size_t(rows);
+    if (need_dir && !ensure(&plan->bc_dir, &plan->bc_dir_cap, ndir)) return SHK_ENOMEM;
+    if (need_neu && !ensure(&plan->bc_neu, &plan->bc_neu_cap, nneu)) return SHK_ENOMEM;
     if (need_dir)
-        SHK_CUDA(cudaMemcpyAsync(plan->bc_dir, dirichlet, sizeof(double) * 6 * B, cudaMemcpyDefault, st));
+        SHK_CUDA(cudaMemcpyAsync(plan->bc_dir, dirichlet, sizeof(double) * ndir, cudaMemcpyDefault, st));
     if (need_neu)
-        SHK_CUDA(cudaMemcpyAsync(plan->bc_neu, neumann, sizeof(double) * 2 * B, cudaMemcpyDefault, st));
+        SHK_CUDA(cudaMemcpyAsync(plan->bc_neu, neumann, sizeof(double) * nneu, cudaMemcpyDefault, st));
     plan->bc_left = left;
     plan->bc_right = right;
+    plan->bc_steps = steps;
     if (plan->graph) {  // kernels take the plan's device view by value
         cudaGraphExecDestroy(plan->graph);
         plan->graph = nullptr;
     }
     return SHK_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int shk_plan_set_boundary(shk_plan* plan, int32_t left, int32_t right, const double* dirichlet,
+                          const double* neumann, void* stream) {
+    return set_plan_boundary(plan, left, right, dirichlet, neumann, 1, 0, stream);
+}
+
+int shk_plan_set_boundary_steps(shk_plan* plan, int32_t left, int32_t right,
+                                const double* dirichlet, const double* neumann, int32_t nsteps,
+                                void* stream) {
+    if (nsteps < 1) return SHK_EINVAL;
+    return set_plan_boundary(plan, left, right, dirichlet, neumann, 3 * int64_t(nsteps), nsteps,
+                             stream);
 }
 
 int shk_plan_step_graph(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps, void* stream) {

@@ -677,8 +677,9 @@ struct PlanDev {
     const double* dt_fixed;  // [fixed_steps][B] prescribed steps, or null (CFL steps)
     int64_t fixed_steps;
     int bc_left, bc_right;   // SHK_BC_* of every instance
-    const double* bc_dir;    // [B][2][3] Dirichlet ghost values
-    const double* bc_neu;    // [B][2] Neumann gradients
+    const double* bc_dir;    // [B][2][3] Dirichlet ghost values, or [bc_steps][3][B][2][3]
+    const double* bc_neu;    // [B][2] Neumann gradients, or [bc_steps][3][B][2]
+    int64_t bc_steps;        // 0: time-independent data; else per-step, per-stage tables
     const int32_t* item_order;  // [nitems] items longest first (dynamic scheduling)
     unsigned int* sched;        // [8] item counters of the scheduled kernels
     int32_t B, nitems, tile, max_steps;
@@ -711,14 +712,25 @@ __device__ __forceinline__ void finish_items(const PlanDev& P, int slot) {
     }
 }
 
-// the boundary of instance b (time-independent data: one stage for all three)
-__device__ __forceinline__ BcView plan_bc(const PlanDev& P, int b) {
+// the boundary of instance b at step k: time-independent data (one set for
+// all three stages), or the step's row of a per-step table (steps past the
+// table take its last row)
+__device__ __forceinline__ BcView plan_bc(const PlanDev& P, int b, int64_t k) {
     BcView v;
     v.left = P.bc_left;
     v.right = P.bc_right;
     if (!v.periodic()) {
-        v.dir = P.bc_dir ? P.bc_dir + size_t(b) * 6 : nullptr;
-        v.neu = P.bc_neu ? P.bc_neu + size_t(b) * 2 : nullptr;
+        if (P.bc_steps > 0) {
+            const int64_t kk = k < P.bc_steps ? k : P.bc_steps - 1;
+            const size_t row = size_t(kk) * 3 * P.B + b;
+            v.dir = P.bc_dir ? P.bc_dir + row * 6 : nullptr;
+            v.dir_ss = 6 * P.B;
+            v.neu = P.bc_neu ? P.bc_neu + row * 2 : nullptr;
+            v.neu_ss = 2 * P.B;
+        } else {
+            v.dir = P.bc_dir ? P.bc_dir + size_t(b) * 6 : nullptr;
+            v.neu = P.bc_neu ? P.bc_neu + size_t(b) * 2 : nullptr;
+        }
         v.dx = 1.0 / P.inv_dx[b];
     }
     return v;
