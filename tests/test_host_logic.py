@@ -56,3 +56,41 @@ def test_pack_offsets_and_partition():
     assert sorted(np.concatenate(parts).tolist()) == list(range(len(sizes)))
     loads = [sum(sizes[i] for i in p) for p in parts]
     assert max(loads) == 2048  # LPT: the largest instance alone bounds the makespan
+
+
+def test_bench_workload_is_the_batched_configuration():
+    """The bench's synthetic batch: 4096 instances with N from {1024, ..., 16384}
+    (25,865,216 cells for the committed seed), and initial states that are the
+    exact cell averages of m + sum_k A_k sin(k pi x + phi_k) plus 0-3 steps,
+    checked against an independent per-cell quadrature (Gauss-Legendre for the
+    smooth part, the covered fraction of the cell for each step)."""
+    import importlib.util
+    import pathlib
+
+    spec = importlib.util.spec_from_file_location(
+        "bench_for_test", pathlib.Path(__file__).resolve().parents[1] / "bench.py")
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+
+    sizes, params = bench.workload_params(bench.SEED)
+    assert sizes.size == 4096 and set(np.unique(sizes)) <= set(bench.SIZES)
+    assert int(sizes.sum()) == 25_865_216
+    assert all(-0.5 <= p[0] <= 0.5 and 0 <= len(p[3]) <= 3 for p in params)
+
+    pick = [0, 1, 2]
+    sub_sizes = sizes[pick]
+    u = bench.initial_state(sub_sizes, [params[i] for i in pick], "cpu").numpy()
+    xi, wi = np.polynomial.legendre.leggauss(8)
+    at = 0
+    for b, n in zip(pick, sub_sizes):
+        m, amp, phi, hj, xj = params[b]
+        h = 2.0 / n
+        f = -1.0 + h * np.arange(n + 1)
+        xm = 0.5 * (f[1:] + f[:-1])
+        xq = xm[:, None] + 0.5 * h * xi[None, :]
+        smooth = m + sum(a * np.sin((k + 1) * np.pi * xq + p) for k, (a, p) in enumerate(zip(amp, phi)))
+        ref = (smooth * wi[None, :]).sum(1) * 0.5
+        for hh, x0 in zip(hj, xj):
+            ref += hh * np.clip((f[1:] - x0) / h, 0.0, 1.0)
+        assert np.max(np.abs(u[at:at + n] - ref)) < 1.0e-11, b
+        at += n
