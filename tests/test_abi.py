@@ -123,3 +123,20 @@ def test_product_path_never_imports_the_oracle():
         text = p.read_text()
         assert "oracle" not in re.findall(r"(?:import|from)\s+(\w+)", text), p
         assert "numpy_ref" not in text and "torch_ref" not in text, p
+
+
+def test_integration_notes_cover_every_entry_point():
+    """Every function that include/shocks.h declares has a row (or a grouped
+    mention such as ``shk_plan_create/reset``) in INTEGRATION.md."""
+    import re
+
+    header = (ROOT / "include" / "shocks.h").read_text()
+    notes = (ROOT / "INTEGRATION.md").read_text()
+    names = set(re.findall(r"\b(shk_[a-z0-9_]+)\s*\(", header))
+    mentioned = set(re.findall(r"\b(shk_[a-z0-9_]+)", notes))
+    for group in re.findall(r"`(shk_[a-z0-9_]+(?:/[a-z0-9_]+)+)`", notes):
+        head, *rest = group.split("/")
+        for tail in rest:  # shk_plan_create/reset -> shk_plan_reset (any common prefix)
+            parts = head.split("_")
+            mentioned.update("_".join(parts[:i] + [tail]) for i in range(2, len(parts)))
+    assert sorted(names - mentioned) == []
