@@ -182,6 +182,15 @@ def predict_timestep_from_maxit(tfinal: float, maxit: int) -> tuple[int, float]:
     return maxit, tfinal / maxit + 1.0e-15
 
 
+def predict_timestep_from_resolutions(a: float, b: float, resolutions, *, umax: float = 1.0,
+                                      p: int = 1) -> float:
+    """``src/pyshocks/timestepping.py:264-280``: a step stable for every
+    resolution of a study, ``(dx_min)^p / umax`` with ``dx_min = (b - a) /
+    max(resolutions)``."""
+    dx = (b - a) / max(resolutions)
+    return dx**p / umax
+
+
 def predict_maxit_from_timestep(tfinal: float, dt: float) -> tuple[int, float]:
     """``src/pyshocks/timestepping.py:251-261``."""
     maxit = int(tfinal / dt)

@@ -83,10 +83,11 @@ def test_burgers_riemann_convergence_gpu(name, sizes):
     rec = reconstruction.ConstantReconstruction()
     scheme = (burgers.Rusanov(rec=rec, alpha=0.98) if name == "rusanov"
               else burgers.EngquistOsher(rec=rec))
+    from pyshocks_gb300 import timestepping as ts
+
     tfinal = 1.0
-    dt = (2.0 / max(sizes)) / 10.0
-    maxit = int(tfinal / dt)
-    dt = tfinal / maxit + 1.0e-15
+    maxit, dt = ts.predict_maxit_from_timestep(
+        tfinal, ts.predict_timestep_from_resolutions(-1.0, 1.0, sizes, umax=10.0))
 
     def riemann(t):
         return lambda x: np.where(x < 0.5 * t, 1.0, 0.0)

@@ -94,3 +94,16 @@ def test_bench_workload_is_the_batched_configuration():
             ref += hh * np.clip((f[1:] - x0) / h, 0.0, 1.0)
         assert np.max(np.abs(u[at:at + n] - ref)) < 1.0e-11, b
         at += n
+
+
+def test_timestep_helpers_follow_the_reference():
+    """``predict_timestep_from_resolutions`` / ``predict_maxit_from_timestep`` /
+    ``predict_timestep_from_maxit`` (``src/pyshocks/timestepping.py:242-280``)."""
+    from pyshocks_gb300 import timestepping as ts
+
+    dt = ts.predict_timestep_from_resolutions(-1.0, 1.0, [64, 128, 96], umax=10.0)
+    assert dt == (2.0 / 128) / 10.0
+    assert ts.predict_timestep_from_resolutions(0.0, 1.0, [10], p=2) == 0.1**2
+    maxit, dt2 = ts.predict_maxit_from_timestep(1.0, dt)
+    assert maxit == int(1.0 / dt) and dt2 == 1.0 / maxit + 1.0e-15
+    assert ts.predict_timestep_from_maxit(2.0, 8) == (8, 0.25 + 1.0e-15)
