@@ -345,10 +345,19 @@ def scheme_ids() -> tuple[str, ...]:
     return tuple(_SCHEMES)
 
 
+# the reference's entropy-stable summation-by-parts schemes (SS-MUSCL,
+# SS-WENO 2-4-2, flux-split Rusanov on SBP operators): not on this path
+_NOT_ON_THIS_PATH = ("ssmuscl", "ssweno242", "splitrusanov")
+
+
 def make_scheme_from_name(name: str, **kwargs: Any) -> SchemeBase:
     """``src/pyshocks/burgers/__init__.py:82-98``."""
     cls = _SCHEMES.get(name)
     if cls is None:
+        if name in _NOT_ON_THIS_PATH:
+            raise NotImplementedError(
+                f"Scheme {name!r} (summation-by-parts, entropy-stable) has no GPU "
+                f"implementation. Try one of {', '.join(scheme_ids())}.")
         raise ValueError(f"Scheme {name!r} not found. Try one of {', '.join(scheme_ids())}.")
     return cls(**{f.name: kwargs[f.name] for f in fields(cls) if f.name in kwargs})
 

@@ -107,3 +107,21 @@ def test_timestep_helpers_follow_the_reference():
     maxit, dt2 = ts.predict_maxit_from_timestep(1.0, dt)
     assert maxit == int(1.0 / dt) and dt2 == 1.0 / maxit + 1.0e-15
     assert ts.predict_timestep_from_maxit(2.0, 8) == (8, 0.25 + 1.0e-15)
+
+
+def test_scheme_names_follow_the_reference():
+    """The reference's Burgers scheme names (``src/pyshocks/burgers/__init__.py:62-98``):
+    the finite-volume ones build, the summation-by-parts ones say they are not
+    on this path, unknown names raise ValueError."""
+    from pyshocks_gb300 import burgers, reconstruction
+
+    weno = reconstruction.WENOJS53()
+    for name in ("default", "godunov", "rusanov", "lf", "eo"):
+        assert burgers.make_scheme_from_name(name, rec=weno).rec is weno
+    assert burgers.make_scheme_from_name("esweno32", rec=reconstruction.ESWENO32()) is not None
+    assert type(burgers.make_scheme_from_name("default", rec=weno)).__name__ == "LaxFriedrichs"
+    for name in ("ssmuscl", "ssweno242", "splitrusanov"):
+        with pytest.raises(NotImplementedError):
+            burgers.make_scheme_from_name(name)
+    with pytest.raises(ValueError):
+        burgers.make_scheme_from_name("nope")
