@@ -167,6 +167,11 @@ def make_reconstruction_from_name(name: str, **kwargs: Any) -> Reconstruction:
     """``src/pyshocks/reconstruction.py:547-566``: unknown keyword arguments are
     ignored, as in the reference."""
     cls = _RECONSTRUCTION.get(name)
+    if cls is None and name == "ssweno242":
+        # the reference's entropy-stable SBP reconstruction: not on this path
+        raise NotImplementedError(
+            f"Reconstruction {name!r} (summation-by-parts) has no GPU implementation. "
+            f"Try one of {', '.join(reconstruction_ids())}.")
     if cls is None:
         raise ValueError(
             f"Reconstruction {name!r} not found. Try one of {', '.join(reconstruction_ids())}."

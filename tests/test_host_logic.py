@@ -125,3 +125,8 @@ def test_scheme_names_follow_the_reference():
             burgers.make_scheme_from_name(name)
     with pytest.raises(ValueError):
         burgers.make_scheme_from_name("nope")
+    # reconstructions (src/pyshocks/reconstruction.py:528-566)
+    for name in ("default", "constant", "muscl", "muscls", "wenojs32", "wenojs53", "esweno32"):
+        assert reconstruction.make_reconstruction_from_name(name) is not None
+    with pytest.raises(NotImplementedError):
+        reconstruction.make_reconstruction_from_name("ssweno242")
