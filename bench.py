@@ -182,18 +182,22 @@ def _measured_peaks() -> dict:
     return {}
 
 
-def run_cpu_sample(sizes, params, *, n_inst: int, nsteps: int, threads: int = 0):
-    """Time the C restatement of the reference path on the first *n_inst*
-    instances for *nsteps* steps (best of 3); returns (cell-steps/s, threads)."""
-    import torch
-
-    from oracle import c_ref
-
+def _cpu_inputs(sizes, params, n_inst: int):
+    """Packed initial state, offsets and cell sizes of the first *n_inst*
+    instances, on the host."""
     sub_sizes = sizes[:n_inst]
     u0 = initial_state(sub_sizes, params[:n_inst], "cpu").numpy()
     off = np.zeros(n_inst + 1, dtype=np.int64)
     off[1:] = np.cumsum(sub_sizes)
-    dx = 2.0 / sub_sizes.astype(np.float64)
+    return u0, off, 2.0 / sub_sizes.astype(np.float64)
+
+
+def run_cpu_sample(sizes, params, *, n_inst: int, nsteps: int, threads: int = 0):
+    """Time the C restatement of the reference path on the first *n_inst*
+    instances for *nsteps* steps (best of 3); returns (cell-steps/s, threads)."""
+    from oracle import c_ref
+
+    u0, off, dx = _cpu_inputs(sizes, params, n_inst)
     c_ref.run_batch(u0, off, dx, theta=THETA, eps=EPS, nsteps=1, nthreads=threads)  # warm-up
     best = None
     used = 1
@@ -203,25 +207,29 @@ def run_cpu_sample(sizes, params, *, n_inst: int, nsteps: int, threads: int = 0)
                                      nthreads=threads)
         el = time.perf_counter() - t0
         best = el if best is None else min(best, el)
-    del torch
     return float(off[-1]) * nsteps / best, used
 
 
 def bench_reference(args, rank: int) -> None:
     if rank != 0:
         return
+    from oracle import c_ref
+
     sizes, params = workload_params(SEED)
     n_inst = args.cpu_instances
+    u0, off, dx = _cpu_inputs(sizes, params, n_inst)
     vals = []
     used = 1
     for i in range(args.warmup + args.steps):
-        rate, used = run_cpu_sample(sizes, params, n_inst=n_inst, nsteps=1)
+        t0 = time.perf_counter()
+        _, _, used = c_ref.run_batch(u0, off, dx, theta=THETA, eps=EPS, nsteps=1, nthreads=0)
+        rate = float(off[-1]) / (time.perf_counter() - t0)
         if i >= args.warmup:
             vals.append(rate)
     value = float(np.median(vals))
-    cells = int(np.sum(sizes[:n_inst]))
+    cells = int(off[-1])
     sample = (f"first {n_inst} of the {BATCH} seeded instances ({cells} cells), one SSPRK33 "
-              f"step per timed step, best of 3")
+              f"step per timed step from the initial state, median of the timed steps")
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -406,8 +414,8 @@ def bench_gpu(args, rank: int, world: int) -> None:
     if rank == 0 and not args.no_cpu and not args.profile:
         rate, used = run_cpu_sample(sizes, params, n_inst=args.cpu_instances, nsteps=1)
         cpu = {"value": rate, "unit": "cell-steps/s", "cores": used, "kind": "port",
-               "sample": f"first {args.cpu_instances} instances of the batch, one step, "
-                         f"C restatement (oracle/shocks_ref.c), best of 3"}
+               "sample": f"first {args.cpu_instances} of the {BATCH} instances of the batch, "
+                         f"one step, C restatement (oracle/shocks_ref.c), best of 3"}
 
     if rank == 0:
         line = {
@@ -684,7 +692,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--cpu-instances", type=int, default=256)
+    ap.add_argument("--cpu-instances", type=int, default=BATCH,
+                    help="instances of the batch in the CPU samples (default: all)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the float32 and adjoint measurements")
