@@ -324,8 +324,10 @@ int shk_plan_reduce(shk_plan* plan, const void* u, int32_t p, double* out, void*
  * buffers).
  *  - n is limited to shk_apply_operator_lf_noalloc_max_cells() interior cells
  *    (2,097,152); larger n returns SHK_ETOOLARGE before any launch.
- *  - The first call on each device looks up the scratch address on that device
+ *  - The first call in each CUDA context looks up the scratch address there
  *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *    The address is kept per context (by its cuCtxGetId), so a context created
+ *    after cudaDeviceReset gets its own lookup instead of a stale address.
  *  - The scratch (32 KiB per GPU, held from library load to process exit) is
  *    shared by all calls and keeps the last call's contents; every slot a call
  *    reads is written by that call first. Calls that overlap on the GPU race on

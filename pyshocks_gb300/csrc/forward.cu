@@ -12,6 +12,7 @@
 // Periodic boundaries are applied by circular indexing of the n interior
 // cells: with stencil reach 3 and 3 ghost cells the reference's interior
 // outputs equal the circular ones (its zero padding reaches ghost outputs only).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -1093,26 +1094,63 @@ static __device__ __align__(256) double g_noalloc_scratch[kNoAllocMaxTiles + 1];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mutex;
-double* g_noalloc_addr[kMaxDevices] = {};
+struct NoAllocAddr {
+    unsigned long long ctx_id = 0;  // cuCtxGetId of the context the address belongs to
+    double* addr = nullptr;
+};
+NoAllocAddr g_noalloc_addr[kMaxDevices];
 
-// Device address of g_noalloc_scratch on the current device. In host code the
-// symbol itself is only a host-side stand-in, so the address must come from
-// cudaGetSymbolAddress, once per device, with that device current.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique ID of the calling thread's current CUDA context (0 if none). The
+// driver functions come through the runtime's entry-point query, so the
+// library does not link libcuda itself.
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) !=
+                cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) !=
+                cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess)
+            return 0;
+        get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        get_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+// Device address of g_noalloc_scratch in the current device's context. In host
+// code the symbol itself is only a host-side stand-in, so the address must come
+// from cudaGetSymbolAddress with that device current. It is looked up once per
+// context: a context created after cudaDeviceReset loads the module again, so
+// the address of an earlier context is not reused.
 int noalloc_scratch(double** out) {
     int dev = 0;
     SHK_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) return SHK_EUNSUPPORTED;
+    const unsigned long long id = current_context_id();  // 0 before the runtime made one current
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_addr[dev]) {
+    NoAllocAddr& slot = g_noalloc_addr[dev];
+    if (!slot.addr || id == 0 || slot.ctx_id != id) {
         void* p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
             std::fprintf(stderr, "libshocks: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
             return SHK_ECUDA;
         }
-        g_noalloc_addr[dev] = static_cast<double*>(p);
+        slot.addr = static_cast<double*>(p);
+        slot.ctx_id = current_context_id();  // the context the lookup ran in
     }
-    *out = g_noalloc_addr[dev];
+    *out = slot.addr;
     return SHK_OK;
 }
 
@@ -1179,6 +1217,7 @@ extern "C" int shk_apply_operator_lf_noalloc_f64(const shk_scheme* scheme, const
     const int W = kNoAllocTile + 2 * op_halo<double>();
     const size_t smem = Smem<double>::host_bytes(W);
     OpParams<double> p = make_params<double>(scheme);
+    p.dx = dx;
     ApplyOpLaunch f{u, out, n, nghosts, kNoAllocTile, dx, scratch + kNoAllocMaxTiles, p, smem, nt, st,
                     periodic_boundary()};
     return dispatch_scheme<double>(scheme, f);
