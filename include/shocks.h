@@ -308,8 +308,9 @@ int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, in
                             void* seg, void* stages, void* p_a, void* p_b, void* stream);
 
 /* FP64 reductions over the batch (grid.py:444-506, conservation checks):
- * out[b] = sum_i u_b[i] (p = 0), sum |u_b[i]| (p = 1) or max |u_b[i]| (p = -1),
- * accumulated in double for either state precision. */
+ * out[b] = sum_i u_b[i] (p = 0), sum |u_b[i]| (p = 1), sum u_b[i]^2 (p = 2) or
+ * max |u_b[i]| (p = -1), accumulated in double for either state precision, in
+ * a fixed order (deterministic for a given plan). */
 int shk_plan_reduce(shk_plan* plan, const void* u, int32_t p, double* out, void* stream);
 
 /* ---- no-allocation variant --------------------------------------------- */

@@ -3,6 +3,12 @@
 Translation units compile in parallel; each gets exactly one ``-gencode``
 (``arch=compute_103a,code=sm_103a``). IEEE division and square root stay on
 (no fast-math): the FP64 path must reproduce the reference to round-off.
+
+Two variants come from the same sources: ``libshocks.so`` (the library) and
+``libshocks_check.so``, the bounds-check build (``-DSHOCKS_BOUNDS_CHECK``:
+every window, stage-storage and state index checked, violations logged in a
+device word; ``include/shocks_check.h``), which the tests use as the memory
+checker of the kernels.
 """
 
 from __future__ import annotations
@@ -33,8 +39,14 @@ def sources() -> list[pathlib.Path]:
     return sorted(CSRC.glob("*.cu"))
 
 
-def _compile(nvcc: str, src: pathlib.Path, extra: list[str]) -> pathlib.Path:
-    obj = BUILD / (src.stem + ".o")
+VARIANTS = {
+    "lib": (LIB, BUILD, []),
+    "check": (HERE / "libshocks_check.so", HERE / "_build_check", ["-DSHOCKS_BOUNDS_CHECK"]),
+}
+
+
+def _compile(nvcc: str, src: pathlib.Path, outdir: pathlib.Path, extra: list[str]) -> pathlib.Path:
+    obj = outdir / (src.stem + ".o")
     cmd = [
         nvcc, "-gencode", GENCODE, "-O3", "-lineinfo", "-std=c++17",
         "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-c",
@@ -46,29 +58,42 @@ def _compile(nvcc: str, src: pathlib.Path, extra: list[str]) -> pathlib.Path:
     return obj
 
 
-def build(force: bool = False, extra: list[str] | None = None, verbose: bool = False) -> pathlib.Path:
-    """Compile every ``csrc/*.cu`` and link ``libshocks.so``; returns its path."""
-    srcs = sources()
-    deps = srcs + sorted(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "shocks.h"]
-    if LIB.exists() and not force:
-        newest = max(p.stat().st_mtime for p in deps)
-        if LIB.stat().st_mtime >= newest:
-            return LIB
+def _stale(lib: pathlib.Path) -> bool:
+    deps = sources() + sorted(CSRC.glob("*.cuh")) + sorted((HERE.parent / "include").glob("*.h"))
+    return not lib.exists() or lib.stat().st_mtime < max(p.stat().st_mtime for p in deps)
+
+
+def build(force: bool = False, extra: list[str] | None = None, verbose: bool = False,
+          variants: tuple[str, ...] = ("lib",)) -> pathlib.Path:
+    """Compile every ``csrc/*.cu`` and link the requested variants
+    (``"lib"``: ``libshocks.so``, ``"check"``: ``libshocks_check.so``), all
+    translation units in one parallel pool; returns the first variant's path."""
+    todo = [v for v in variants if force or _stale(VARIANTS[v][0])]
+    if not todo:
+        return VARIANTS[variants[0]][0]
     nvcc = nvcc_path()
-    BUILD.mkdir(exist_ok=True)
-    extra = list(extra or [])
-    with ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 1))) as ex:
-        objs = list(ex.map(lambda s: _compile(nvcc, s, extra), srcs))
-    tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc, "-gencode", GENCODE, "-shared", "-o", str(tmp), *map(str, objs)]
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB)
-    if verbose:
-        print(f"built {LIB}", file=sys.stderr)
-    return LIB
+    srcs = sources()
+    jobs = []
+    for v in todo:
+        outdir = VARIANTS[v][1]
+        outdir.mkdir(exist_ok=True)
+        jobs += [(v, src, outdir, VARIANTS[v][2] + list(extra or [])) for src in srcs]
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
+        objs = list(ex.map(lambda j: (j[0], _compile(nvcc, j[1], j[2], j[3])), jobs))
+    for v in todo:
+        lib = VARIANTS[v][0]
+        tmp = lib.with_suffix(".so.tmp")
+        cmd = [nvcc, "-gencode", GENCODE, "-shared", "-o", str(tmp),
+               *[str(o) for vv, o in objs if vv == v]]
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
+        os.replace(tmp, lib)
+        if verbose:
+            print(f"built {lib}", file=sys.stderr)
+    return VARIANTS[variants[0]][0]
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True)
+    build(force="--force" in sys.argv, verbose=True,
+          variants=("lib", "check") if "--check" in sys.argv else ("lib",))

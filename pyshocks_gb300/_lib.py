@@ -139,6 +139,13 @@ SIGNATURES: dict[str, tuple] = {
     "shk_measure_fp_peak": (ctypes.c_int, [_I32, _I32, ctypes.POINTER(_D)]),
 }
 
+# prototypes of the bounds-check build's two extra entry points (include/shocks_check.h)
+CHECK_SIGNATURES: dict[str, tuple] = {
+    "shk_check_bounds": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P]),
+    "shk_check_force_timeout": (ctypes.c_int, [ctypes.c_uint32, _I64]),
+}
+CHECK_LIB_PATH = HERE / "libshocks_check.so"
+
 _lock = threading.Lock()
 _lib = None
 
@@ -174,6 +181,18 @@ def load_library(path: pathlib.Path | None = None) -> ctypes.CDLL:
         )
     cdll = ctypes.CDLL(str(path))
     for name, (res, args) in SIGNATURES.items():
+        fn = getattr(cdll, name)
+        fn.restype = res
+        fn.argtypes = args
+    return cdll
+
+
+def load_check_library() -> ctypes.CDLL:
+    """Load the bounds-check build ``libshocks_check.so`` (the library's ABI plus
+    ``shk_check_bounds`` and ``shk_check_force_timeout``); a test instrument,
+    never loaded by the package itself."""
+    cdll = load_library(CHECK_LIB_PATH)
+    for name, (res, args) in CHECK_SIGNATURES.items():
         fn = getattr(cdll, name)
         fn.restype = res
         fn.argtypes = args

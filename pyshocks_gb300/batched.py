@@ -262,11 +262,18 @@ class BatchedSolver:
         return int(st.value)
 
     def check_status(self) -> None:
+        """Raise on the plan's device status bits: a non-finite time step
+        (``ValueError``, as ``step()``), an expired bounded wait, or (in the
+        bounds-check build) an index outside its array (``RuntimeError``). A
+        launch that reported either of the latter leaves its output undefined;
+        reset the plan before stepping it again."""
         st = self.status()
         if st & L.ERR_NONFINITE:
             raise ValueError("Time step is not finite (an instance was frozen)")
         if st & L.ERR_TIMEOUT:
             raise RuntimeError("bounded device wait expired in the step kernel")
+        if st & L.ERR_BOUNDS:
+            raise RuntimeError("a kernel index left its array (bounds-check build)")
 
     # }}}
 
@@ -371,13 +378,28 @@ class BatchedSolver:
         return self.u
 
     def reduce(self, p: int = 0, u: torch.Tensor | None = None) -> torch.Tensor:
-        """Per-instance FP64 ``sum u`` (p=0), ``sum |u|`` (p=1) or ``max |u|``
-        (p=-1), deterministic order."""
+        """Per-instance FP64 ``sum u`` (p=0), ``sum |u|`` (p=1), ``sum u^2``
+        (p=2) or ``max |u|`` (p=-1), deterministic order."""
         u = self.u if u is None else u
         out = torch.empty(self.B, dtype=torch.float64, device=self.device)
         L.check(self.lib.shk_plan_reduce(self._plan, u.data_ptr(), int(p), out.data_ptr(),
                                          L.stream_handle()), "plan_reduce")
         return out
+
+    def norm(self, p=1, u: torch.Tensor | None = None, *, weighted: bool = False) -> torch.Tensor:
+        """Per-instance interior norms of ``src/pyshocks/grid.py:444-506`` (p = 1,
+        2 or inf; ``weighted`` multiplies the sums by dx), from FP64 sums."""
+        if p == 1:
+            r = self.reduce(1, u)
+        elif p == 2:
+            r = self.reduce(2, u)
+        elif p in {np.inf, "inf"}:
+            return self.reduce(-1, u)
+        else:
+            raise ValueError(f"Unrecognized norm order 'p': {p!r}.")
+        if weighted:
+            r = r * torch.as_tensor(self.dx, device=r.device)
+        return r if p == 1 else torch.sqrt(r)
 
 
 def _per_instance(v, B, device, default) -> torch.Tensor:

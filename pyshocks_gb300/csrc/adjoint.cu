@@ -42,25 +42,25 @@ constexpr int kAdjArrays = 24;
 
 template <class T>
 struct AdjSmem {
-    T *U, *K1, *K2, *PB, *CB, *Z, *ACC;
-    T *H, *D, *Q, *UL, *UR;
-    T *GL, *GR, *GA;
-    T *T0, *T1, *T2, *T3, *T4;
-    T *CLu, *CRu, *CL1, *CR1;  // face values of u and k1 from the forward recompute
+    Win<T> U, K1, K2, PB, CB, Z, ACC;
+    Win<T> H, D, Q, UL, UR;
+    Win<T> GL, GR, GA;
+    Win<T> T0, T1, T2, T3, T4;
+    Win<T> CLu, CRu, CL1, CR1;  // face values of u and k1 from the forward recompute
     int W;  // window length (cells) of every array
 
     __host__ static size_t host_bytes(int W) { return size_t(kAdjArrays) * W * sizeof(T); }
     __device__ void carve(unsigned char* base, int W) {
         T* p = reinterpret_cast<T*>(base);
-        T** slots[kAdjArrays] = {&U, &K1, &K2, &PB, &CB, &Z, &ACC, &H, &D, &Q,
-                                 &UL, &UR, &GL, &GR, &GA, &T0, &T1, &T2, &T3, &T4,
-                                 &CLu, &CRu, &CL1, &CR1};
-        for (int i = 0; i < kAdjArrays; ++i) *slots[i] = p + size_t(i) * W;
+        Win<T>* slots[kAdjArrays] = {&U, &K1, &K2, &PB, &CB, &Z, &ACC, &H, &D, &Q,
+                                     &UL, &UR, &GL, &GR, &GA, &T0, &T1, &T2, &T3, &T4,
+                                     &CLu, &CRu, &CL1, &CR1};
+        for (int i = 0; i < kAdjArrays; ++i) *slots[i] = make_win(p + size_t(i) * W, W);
         this->W = W;
     }
     // forward-stage view (face_fluxes writes the face fluxes into D and the
     // face values into ul, ur: UL, UR unless given)
-    __device__ Smem<T> fwd(T* state_out, T* ul = nullptr, T* ur = nullptr) const {
+    __device__ Smem<T> fwd(Win<T> state_out, Win<T> ul = Win<T>(), Win<T> ur = Win<T>()) const {
         Smem<T> s;
         s.U = U; s.S = state_out; s.H = H; s.D = D; s.Q = Q;
         s.UL = ul ? ul : UL; s.UR = ur ? ur : UR;
@@ -188,10 +188,9 @@ __device__ __forceinline__ void weno53_cell_vjp(T Hm2, T Hm1, T H0, T Hp1, T Dm1
 // [lo-3, hi+3). Rusanov flux, WENO-JS5 or learned reconstruction.
 // cul, cur (WENO-JS5): the face values of v on [lo-3, hi+3) as the forward's
 // face pass forms them (stored by the replay, or kept by the recompute)
-template <class T, int EQ, int REC>
-__device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const AdjSmem<T>& a,
-                          const OpParams<T>& p, T dtdx, const T* cul = nullptr,
-                          const T* cur = nullptr) {
+template <class T, int EQ, int REC, class PV, class PW, class PZ, class PC = Win<const T>>
+__device__ void vjp_stage(PV v, PW w, PZ z, int lo, int hi, const AdjSmem<T>& a,
+                          const OpParams<T>& p, T dtdx, PC cul = PC(), PC cur = PC()) {
     const int tid = threadIdx.x, nt = blockDim.x;
     if constexpr (REC == SHK_REC_LEARNED) {
         static_assert(sizeof(T) == 4, "the learned VJP runs on float stage states");
@@ -207,7 +206,8 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
         MlpBackFrags bk;
         mlp_load_back_frags(p.lp.mlp, bk);
         // warp scratch: GL, GR, GA (3W floats, unused by this branch)
-        float* scr = learned_scratch(a.GL) + (tid >> 5) * kWarpScratchVjp;
+        float* scr = win_span(learned_scratch(a.GL, 3 * a.W), (tid >> 5) * kWarpScratchVjp,
+                              kWarpScratchVjp);
         const int lane = tid & 31, g = lane >> 2, tq = lane & 3;
         const int myrow = 16 * (tq >> 1) + 8 * (tq & 1) + g;
         const int c0 = lo - 2, ncell = hi + 2 - c0;
@@ -257,8 +257,8 @@ __device__ void vjp_stage(const T* v, const T* w, T* z, int lo, int hi, const Ad
         a.Q[c] = (T(13.0 / 3.0) * d) * d;
     }
     __syncthreads();
-    const T* UL = cul;
-    const T* UR = cur;
+    const PC UL = cul;
+    const PC UR = cur;
     // face j+1/2: F = 1/2 (f(L) + f(R)) - nu/2 a (L - R), L = ul_{j+1}, R = ur_j
     for (int j = lo - 3 + tid; j < hi + 2; j += nt) {
         const T fb = (w[j + 1] - w[j]) * dtdx;
@@ -300,7 +300,7 @@ __device__ __forceinline__ StageOut<stage_t<T, REC>> stage_out(void* base, int64
     using S = stage_t<T, REC>;
     StageOut<S> so;
     if (!base) return so;
-    S* b = static_cast<S*>(base) + at;
+    const Win<S> b = make_win(static_cast<S*>(base), kStageArrays<T, REC>() * total) + at;
     so.k1 = b;
     so.k2 = b + total;
     if constexpr (kStageArrays<T, REC>() == 8) {
@@ -324,8 +324,8 @@ __device__ __forceinline__ StageOut<const S> as_const(const StageOut<S>& so) {
 
 // window positions [lo, hi) of a stage array stored per instance cell
 // (position i is cell g0 + i, periodically)
-template <class S>
-__device__ __forceinline__ void load_stage(S* dst, const S* src, int64_t n, int64_t g0,
+template <class PD, class PS>
+__device__ __forceinline__ void load_stage(PD dst, PS src, int64_t n, int64_t g0,
                                            int lo, int hi) {
     const bool once = g0 + lo >= -n && g0 + hi <= 2 * n;
     for (int i = lo + threadIdx.x; i < hi; i += blockDim.x) {
@@ -346,7 +346,7 @@ __device__ __forceinline__ void load_stage(S* dst, const S* src, int64_t n, int6
 // st (optional): the instance's stored float stage states (replay with stage
 // storage), which replace the recompute of k1 and k2 bit for bit.
 template <int EQ>
-__device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float>& af, double* gout,
+__device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float>& af, Win<double> gout,
                                    int te, double dtdx, const OpParams<double>& p,
                                    const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0,
                                    const StageOut<const float>& st = StageOut<const float>()) {
@@ -443,14 +443,14 @@ __device__ void adjoint_tile_mixed(const AdjSmem<double>& a, const AdjSmem<float
 // reverse stage of a boundary tile also covers the ghost cells (their
 // cotangents reach the interior through the Neumann mirrors).
 template <class T, int EQ, int REC>
-__device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const OpParams<T>& p,
+__device__ void adjoint_tile(const AdjSmem<T>& a, Win<T> gout, int te, T dtdx, const OpParams<T>& p,
                              const BcView& bc = BcView(), int64_t g0 = 0, int64_t n = 0,
                              const StageOut<const stage_t<T, REC>>& st =
                                  StageOut<const stage_t<T, REC>>()) {
     if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED) {
         // full double layout: the float arrays fit from CB on (24 in 20 double ones)
         AdjSmem<float> af;
-        af.carve(reinterpret_cast<unsigned char*>(a.CB), a.W);
+        af.carve(reinterpret_cast<unsigned char*>(win_raw(a.CB)), a.W);
         adjoint_tile_mixed<EQ>(a, af, gout, te, dtdx, p, bc, g0, n, st);
         return;
     }
@@ -539,8 +539,8 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     // reverse stage 3: k2b = 2/3 (p + dt J(k2)^T p) on [HU-6, HU+te+6)
     {
         const int lo = HU - 6, hi = HU + te + 6;
-        vjp_stage<T, EQ, REC>(a.K2, a.PB, a.Z, lo, hi, a, p, dtdx, kCache ? a.UL : nullptr,
-                              kCache ? a.UR : nullptr);
+        vjp_stage<T, EQ, REC>(a.K2, a.PB, a.Z, lo, hi, a, p, dtdx, kCache ? a.UL : Win<T>(),
+                              kCache ? a.UR : Win<T>());
         if (np) bc_transpose(a.Z, g0, n, lo, hi, bc);
         for (int i = lo + tid; i < hi; i += nt) a.CB[i] = T(2.0 / 3.0) * (a.PB[i] + a.Z[i]);
         __syncthreads();
@@ -551,8 +551,8 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
     // reverse stage 2: k1b = 1/4 (k2b + dt J(k1)^T k2b) on [HU-3, HU+te+3)
     {
         const int lo = HU - 3, hi = HU + te + 3;
-        vjp_stage<T, EQ, REC>(a.K1, a.CB, a.Z, lo, hi, a, p, dtdx, kCache ? a.CL1 : nullptr,
-                              kCache ? a.CR1 : nullptr);
+        vjp_stage<T, EQ, REC>(a.K1, a.CB, a.Z, lo, hi, a, p, dtdx, kCache ? a.CL1 : Win<T>(),
+                              kCache ? a.CR1 : Win<T>());
         if (np) bc_transpose(a.Z, g0, n, lo, hi, bc);
         for (int i = lo + tid; i < hi; i += nt) a.CB[i] = T(1.0 / 4.0) * (a.CB[i] + a.Z[i]);
         __syncthreads();
@@ -570,8 +570,8 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
             if (g0 + HU == 0) lo -= 3;
             if (g0 + HU + te == n) hi += 3;
         }
-        vjp_stage<T, EQ, REC>(a.U, a.CB, a.Z, lo, hi, a, p, dtdx, kCache ? a.CLu : nullptr,
-                              kCache ? a.CRu : nullptr);
+        vjp_stage<T, EQ, REC>(a.U, a.CB, a.Z, lo, hi, a, p, dtdx, kCache ? a.CLu : Win<T>(),
+                              kCache ? a.CRu : Win<T>());
         if (np) bc_transpose(a.Z, g0, n, lo, hi, bc);
         for (int i = HU + tid; i < HU + te; i += nt) gout[i - HU] = a.ACC[i] + (a.CB[i] + a.Z[i]);
     }
@@ -583,18 +583,18 @@ __device__ void adjoint_tile(const AdjSmem<T>& a, T* gout, int te, T dtdx, const
 constexpr int kMixedAdjSlots = 22;
 __device__ inline void carve_mixed(unsigned char* base, int W, AdjSmem<double>& a, AdjSmem<float>& af) {
     float* f = reinterpret_cast<float*>(base);
-    a.U = reinterpret_cast<double*>(f);
-    a.PB = reinterpret_cast<double*>(f + 2 * W);
-    a.K1 = a.K2 = a.CB = a.Z = a.ACC = a.H = a.D = a.Q = a.UL = a.UR = nullptr;
-    a.GL = a.GR = a.GA = a.T0 = a.T1 = a.T2 = a.T3 = a.T4 = nullptr;
+    a.U = win_cast<double>(make_win(f, 2 * W));
+    a.PB = win_cast<double>(make_win(f + 2 * W, 2 * W));
+    a.K1 = a.K2 = a.CB = a.Z = a.ACC = a.H = a.D = a.Q = a.UL = a.UR = Win<double>();
+    a.GL = a.GR = a.GA = a.T0 = a.T1 = a.T2 = a.T3 = a.T4 = Win<double>();
     a.W = W;
-    af.K1 = f;
-    af.K2 = f + W;
-    af.U = f + 4 * W;
-    af.PB = f + 5 * W;
-    float** rest[] = {&af.CB, &af.Z, &af.ACC, &af.H, &af.D, &af.Q, &af.UL, &af.UR,
-                      &af.GL, &af.GR, &af.GA, &af.T0, &af.T1, &af.T2, &af.T3, &af.T4};
-    for (int i = 0; i < 16; ++i) *rest[i] = f + (6 + i) * W;
+    af.K1 = make_win(f, W);
+    af.K2 = make_win(f + W, W);
+    af.U = make_win(f + 4 * W, W);
+    af.PB = make_win(f + 5 * W, W);
+    Win<float>* rest[] = {&af.CB, &af.Z, &af.ACC, &af.H, &af.D, &af.Q, &af.UL, &af.UR,
+                          &af.GL, &af.GR, &af.GA, &af.T0, &af.T1, &af.T2, &af.T3, &af.T4};
+    for (int i = 0; i < 16; ++i) *rest[i] = make_win(f + (6 + i) * W, W);
     af.W = W;
 }
 
@@ -628,6 +628,8 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
     }
     __syncthreads();
     uint32_t phase = 0;
+    const Win<const T> gpnext = make_win(pnext, total);
+    const Win<T> gpout = make_win(pout, total);
     __shared__ int s_item;
     for (int item = next_item(P, 2, &s_item); item >= 0; item = next_item(P, 2, &s_item)) {
         const int b = P.item_inst[item];
@@ -637,7 +639,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
         const int te = static_cast<int>(imin64(P.tile, n - s0));
         const double dt = dt_row[b];
         if (dt == 0.0) {  // no step was taken: identity
-            for (int i = threadIdx.x; i < te; i += blockDim.x) pout[off + s0 + i] = pnext[off + s0 + i];
+            for (int i = threadIdx.x; i < te; i += blockDim.x) gpout[off + s0 + i] = gpnext[off + s0 + i];
             __syncthreads();
             continue;
         }
@@ -650,8 +652,8 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
         const int64_t g0 = s0 - adj_uhalo<T>();
         const StageOut<const stage_t<T, REC>> st =
             as_const(stage_out<T, REC>(const_cast<void*>(stages), total, off));
-        if constexpr (kMixed) adjoint_tile_mixed<EQ>(a, af, pout + off + s0, te, dtdx, p, bc, g0, n, st);
-        else adjoint_tile<T, EQ, REC>(a, pout + off + s0, te, dtdx, p, bc, g0, n, st);
+        if constexpr (kMixed) adjoint_tile_mixed<EQ>(a, af, gpout + (off + s0), te, dtdx, p, bc, g0, n, st);
+        else adjoint_tile<T, EQ, REC>(a, gpout + (off + s0), te, dtdx, p, bc, g0, n, st);
         __syncthreads();
     }
     finish_items(P, 2);
@@ -679,6 +681,8 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
     }
     __syncthreads();
     uint32_t phase = 0;
+    const Win<const T> guin = make_win(uin, total);
+    const Win<T> guout = make_win(uout, total);
     __shared__ int s_item;
     for (int item = next_item(P, 4, &s_item); item >= 0; item = next_item(P, 4, &s_item)) {
         const int b = P.item_inst[item];
@@ -689,7 +693,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
         const double dt = dt_row[b];
         if (dt == 0.0) {  // no step: the reverse step is the identity, stage states unused
             if (uout)
-                for (int i = threadIdx.x; i < te; i += blockDim.x) uout[off + s0 + i] = uin[off + s0 + i];
+                for (int i = threadIdx.x; i < te; i += blockDim.x) guout[off + s0 + i] = guin[off + s0 + i];
             __syncthreads();
             continue;
         }
@@ -698,7 +702,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
             break;
         }
         const T dtdx = static_cast<T>(dt * P.inv_dx[b]);
-        step_tile<T, EQ, REC, SHK_FLUX_RUSANOV>(sm, uout ? uout + off + s0 : nullptr, te, dtdx, p,
+        step_tile<T, EQ, REC, SHK_FLUX_RUSANOV>(sm, uout ? guout + (off + s0) : Win<T>(), te, dtdx, p,
                                                 plan_bc(P, b, step), s0 - HL, n,
                                                 stage_out<T, REC>(stages, total, off + s0));
         __syncthreads();
@@ -736,12 +740,13 @@ __global__ void __launch_bounds__(kThreads) single_vjp_kernel(const T* __restric
     bc.neu = &bcp.neumann[0][0];
     bc.neu_ss = 2;
     bc.dx = dx;
-    adjoint_tile<T, EQ, SHK_REC_WENOJS53>(a, pout + g + s0, te, dtdx, p, bc, s0 - adj_uhalo<T>(), n);
+    const Win<T> gpout = make_win(pout, n + 2 * g);
+    adjoint_tile<T, EQ, SHK_REC_WENOJS53>(a, gpout + (g + s0), te, dtdx, p, bc, s0 - adj_uhalo<T>(), n);
     // ghost cotangents are zero (interior-only adjoint)
     if (blockIdx.x == 0)
         for (int i = threadIdx.x; i < g; i += blockDim.x) {
-            pout[i] = T(0);
-            pout[g + n + i] = T(0);
+            gpout[i] = T(0);
+            gpout[g + n + i] = T(0);
         }
 }
 
@@ -1024,3 +1029,10 @@ int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, in
 }
 
 }  // extern "C"
+
+#ifdef SHOCKS_BOUNDS_CHECK
+// this translation unit's bounds log (read by shk_check_bounds in forward.cu)
+extern "C" int shk_check_tu_adjoint(shk::BoundsLog* out, int32_t reset) {
+    return acuda(shk::bounds_log_read(out, reset != 0));
+}
+#endif

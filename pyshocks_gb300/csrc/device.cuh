@@ -29,6 +29,9 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+#include <utility>
+
 #include "../../include/shocks.h"
 
 namespace shk {
@@ -42,6 +45,145 @@ enum : int32_t {
 // bounded-wait iteration limit for mbarrier polls (each try_wait may suspend
 // the thread for a short, hardware-defined time)
 constexpr long long kWaitLimit = 1LL << 20;
+
+// ---- window pointers ---------------------------------------------------------
+// The shared-memory window arrays, the stage storage and the state arrays of
+// the stencil kernels are addressed through Win<T>. In the library build a
+// Win<T> is a plain T*, and the helpers below compile to pointer arithmetic.
+// In the bounds-check build (-DSHOCKS_BOUNDS_CHECK, libshocks_check.so) a
+// Win<T> carries the bounds of the array it points into: an index outside
+// them records the first violation of the translation unit (block, thread,
+// offset from the array start, array extent) in a device log and redirects
+// the access to a sink word, so a faulty index is reported instead of
+// touching memory it does not own. No trap, no assert.
+#ifdef SHOCKS_BOUNDS_CHECK
+struct BoundsLog {
+    int32_t flag;
+    int32_t block;
+    int32_t thread;
+    int32_t pad;
+    int64_t offset;  // element offset of the bad access from the array start
+    int64_t extent;  // elements of the array
+};
+static __device__ BoundsLog g_bounds_log;
+static __device__ __align__(16) unsigned char g_bounds_sink[64];
+
+static __device__ __noinline__ void bounds_fail(long long offset, long long extent) {
+    if (atomicOr(&g_bounds_log.flag, 1) == 0) {
+        g_bounds_log.block = static_cast<int32_t>(blockIdx.x);
+        g_bounds_log.thread = static_cast<int32_t>(threadIdx.x);
+        g_bounds_log.offset = offset;
+        g_bounds_log.extent = extent;
+    }
+}
+
+template <class T>
+struct Win {
+    T* p = nullptr;
+    T* lo = nullptr;
+    T* hi = nullptr;
+    __host__ __device__ Win() {}
+    __host__ __device__ Win(decltype(nullptr)) {}
+    __host__ __device__ Win(T* p_, T* lo_, T* hi_) : p(p_), lo(lo_), hi(hi_) {}
+    template <class U, class = typename std::enable_if<std::is_convertible<U*, T*>::value>::type>
+    __host__ __device__ Win(const Win<U>& o) : p(o.p), lo(o.lo), hi(o.hi) {}
+    __device__ T& operator[](long long i) const {
+        T* q = p + i;
+        if (q < lo || q >= hi) {
+            bounds_fail(static_cast<long long>(q - lo), static_cast<long long>(hi - lo));
+            return *reinterpret_cast<T*>(g_bounds_sink);
+        }
+        return *q;
+    }
+    __host__ __device__ Win operator+(long long k) const { return Win(p + k, lo, hi); }
+    __host__ __device__ Win operator-(long long k) const { return Win(p - k, lo, hi); }
+    __host__ __device__ explicit operator bool() const { return p != nullptr; }
+};
+// a window over n elements from p
+template <class T>
+__host__ __device__ __forceinline__ Win<T> make_win(T* p, long long n) { return Win<T>(p, p, p + n); }
+// the same bytes seen as another element type
+template <class U, class T>
+__host__ __device__ __forceinline__ Win<U> win_cast(const Win<T>& w) {
+    return Win<U>(reinterpret_cast<U*>(w.p), reinterpret_cast<U*>(w.lo), reinterpret_cast<U*>(w.hi));
+}
+// raw pointer to the cnt elements from w[i] once they are checked to lie in
+// the array (the array start on a violation: in bounds, for instructions that
+// need a real address such as ldmatrix or a bulk copy)
+template <class T>
+__device__ __forceinline__ T* win_span(const Win<T>& w, long long i, long long cnt) {
+    T* q = w.p + i;
+    if (q < w.lo || q + cnt > w.hi) {
+        bounds_fail(static_cast<long long>(q - w.lo), static_cast<long long>(w.hi - w.lo));
+        return w.lo;
+    }
+    return q;
+}
+// whether the cnt elements from w[i] lie in the array (logged if not)
+template <class T>
+__device__ __forceinline__ bool win_fits(const Win<T>& w, long long i, long long cnt) {
+    const T* q = w.p + i;
+    if (q < w.lo || q + cnt > w.hi) {
+        bounds_fail(static_cast<long long>(q - w.lo), static_cast<long long>(w.hi - w.lo));
+        return false;
+    }
+    return true;
+}
+template <class T>
+__host__ __device__ __forceinline__ T* win_raw(const Win<T>& w) { return w.p; }
+// index i of a length-n array (a gathered read): false and logged if outside
+__device__ __forceinline__ bool chk_index(long long i, long long n) {
+    if (i < 0 || i >= n) {
+        bounds_fail(i, n);
+        return false;
+    }
+    return true;
+}
+// host: copy (and optionally clear) this translation unit's log
+static inline cudaError_t bounds_log_read(BoundsLog* out, bool reset) {
+    cudaError_t e = cudaMemcpyFromSymbol(out, g_bounds_log, sizeof(BoundsLog));
+    if (e == cudaSuccess && reset) {
+        BoundsLog z = {};
+        e = cudaMemcpyToSymbol(g_bounds_log, &z, sizeof(BoundsLog));
+    }
+    return e;
+}
+#else
+template <class T>
+using Win = T*;
+template <class T>
+__host__ __device__ __forceinline__ T* make_win(T* p, long long) { return p; }
+template <class U, class T>
+__host__ __device__ __forceinline__ U* win_cast(T* w) { return reinterpret_cast<U*>(w); }
+template <class T>
+__device__ __forceinline__ T* win_span(T* w, long long i, long long) { return w + i; }
+template <class T>
+__device__ __forceinline__ bool win_fits(T*, long long, long long) { return true; }
+template <class T>
+__host__ __device__ __forceinline__ T* win_raw(T* w) { return w; }
+__device__ __forceinline__ bool chk_index(long long, long long) { return true; }
+#endif
+// element type of a pointer or window
+template <class P>
+using elem_t = typename std::remove_cv<typename std::remove_reference<decltype(std::declval<P>()[0])>::type>::type;
+
+// ---- test hooks of the bounds-check build ----------------------------------
+// libshocks_check.so can make the window loader's bounded wait run out: the
+// loader then declares `extra` bytes more than its copies deliver (every copy
+// lands, none stays in flight, the barrier never completes) and polls at most
+// `limit` times per wait. The library build has neither.
+#ifdef SHOCKS_BOUNDS_CHECK
+static __device__ uint32_t g_test_extra_tx;
+static __device__ long long g_test_wait_limit;
+__device__ __forceinline__ uint32_t test_extra_tx() { return g_test_extra_tx; }
+__device__ __forceinline__ long long wait_limit() {
+    const long long l = g_test_wait_limit;
+    return l > 0 ? l : kWaitLimit;
+}
+#else
+__device__ __forceinline__ constexpr uint32_t test_extra_tx() { return 0u; }
+__device__ __forceinline__ constexpr long long wait_limit() { return kWaitLimit; }
+#endif
 
 // ---- bit tricks for max-reductions on |x| (integer pipe, exact) ---------
 __device__ __forceinline__ unsigned long long abs_bits(double x) {
@@ -394,7 +536,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 // bounded wait: returns false if the limit expired
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-    for (long long it = 0; it < kWaitLimit; ++it) {
+    const long long limit = wait_limit();
+    for (long long it = 0; it < limit; ++it) {
         if (mbar_try_wait(bar, parity)) return true;
     }
     return false;

@@ -26,6 +26,9 @@
 #include <vector>
 
 #include "stencil.cuh"
+#ifdef SHOCKS_BOUNDS_CHECK
+#include "shocks_check.h"
+#endif
 
 namespace shk {
 
@@ -74,6 +77,9 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
     const int64_t k = *reinterpret_cast<volatile int64_t*>(P.step);
     const int cur = static_cast<int>(k & 1), nxt = cur ^ 1;
     bool ok = true;
+    const int64_t total = P.offsets[P.B];
+    const Win<const T> guin = make_win(uin, total);
+    const Win<T> guout = make_win(uout, total);
 
     __shared__ int s_item;
     for (int item = next_item(P, 0, &s_item); item >= 0 && ok; item = next_item(P, 0, &s_item)) {
@@ -97,8 +103,8 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
         if (!(ds.active && ds.finite)) {
             // instance finished or frozen: copy the tile through
             for (int i = threadIdx.x; i < te; i += blockDim.x) {
-                const T v = uin[off + s0 + i];
-                uout[off + s0 + i] = v;
+                const T v = guin[off + s0 + i];
+                guout[off + s0 + i] = v;
                 const B bb = abs_bits(wave_speed<EQ>(v, p.c));
                 mx = bb > mx ? bb : mx;
             }
@@ -111,7 +117,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
             const T dtdx = item_dtdx;
             OpParams<T> pb = p;
             pb.dx = item_dx;
-            mx = step_tile<T, EQ, REC, FLUX>(sm, uout + off + s0, te, dtdx, pb, plan_bc(P, b, k),
+            mx = step_tile<T, EQ, REC, FLUX>(sm, guout + (off + s0), te, dtdx, pb, plan_bc(P, b, k),
                                              s0 - HL, n);
         }
         const B bm = block_max<B>(mx, reinterpret_cast<B*>(red));
@@ -185,6 +191,7 @@ __global__ void __launch_bounds__(kThreads) batched_partial_kernel(PlanDev P, co
             const double v = static_cast<double>(u[off + s0 + i]);
             if (mode == 0) acc += v;
             else if (mode == 1) acc += fabs(v);
+            else if (mode == 2) acc = fma(v, v, acc);
             else acc = fmax(acc, fabs(v));
         }
         // fixed-shape tree: deterministic for a given launch shape
@@ -278,16 +285,17 @@ __global__ void __launch_bounds__(kThreads) apply_operator_kernel(const T* __res
     const bool periodic = bc.periodic();
     if (!periodic) apply_bc(sm.U, s0 - HL, n, 0, te + 2 * HL, bc, 0);
     face_fluxes<T, EQ, REC, FLUX>(sm.U, HL, HL + te, sm, p);
+    const Win<T> gout = make_win(out, n + 2 * g);
     for (int i = threadIdx.x; i < te; i += blockDim.x) {
         const int w = HL + i;
         // -(f[1:] - f[:-1]) / dx  (schemes.py:346)
         const T r = -((sm.D[w] - sm.D[w - 1]) * p.fscale) / dx;
         const int64_t gi = s0 + i;
-        out[g + gi] = r;
+        gout[g + gi] = r;
         // ghost cells of the output: periodic image of the interior output
         if (periodic) {
-            if (gi < g) out[g + n + gi] = r;
-            if (gi >= n - g) out[gi - (n - g)] = r;
+            if (gi < g) gout[g + n + gi] = r;
+            if (gi >= n - g) gout[gi - (n - g)] = r;
         }
     }
 }
@@ -335,15 +343,16 @@ __global__ void __launch_bounds__(kThreads) single_step_kernel(const T* __restri
         return;
     }
     const BcView bc = call_bc(bcp, dx);
-    step_tile<T, EQ, REC, FLUX>(sm, uout + g + s0, te, dtdx, p, bc, s0 - HL, n);
+    const Win<T> gout = make_win(uout, n + 2 * g);
+    step_tile<T, EQ, REC, FLUX>(sm, gout + (g + s0), te, dtdx, p, bc, s0 - HL, n);
     __syncthreads();
     if (!bc.periodic()) return;  // ghosts: bc_ghost_kernel after the step
     // periodic ghost image of the new state
     for (int i = threadIdx.x; i < te; i += blockDim.x) {
         const int64_t gi = s0 + i;
-        const T v = uout[g + gi];
-        if (gi < g) uout[g + n + gi] = v;
-        if (gi >= n - g) uout[gi - (n - g)] = v;
+        const T v = gout[g + gi];
+        if (gi < g) gout[g + n + gi] = v;
+        if (gi >= n - g) gout[gi - (n - g)] = v;
     }
 }
 
@@ -894,6 +903,13 @@ int shk_plan_status(shk_plan* plan, int32_t* h_status, void* stream) {
     SHK_CUDA(cudaMemcpyAsync(h_status, plan->status, sizeof(int32_t), cudaMemcpyDeviceToHost,
                              as_stream(stream)));
     SHK_CUDA(cudaStreamSynchronize(as_stream(stream)));
+#ifdef SHOCKS_BOUNDS_CHECK
+    // the bounds-check build also reports a recorded out-of-bounds index
+    int32_t flag = 0;
+    const int r = shk_check_bounds(0, &flag, nullptr, nullptr, nullptr, nullptr);
+    if (r != SHK_OK) return r;
+    if (flag) *h_status |= ERR_BOUNDS;
+#endif
     return SHK_OK;
 }
 
@@ -1054,7 +1070,7 @@ int shk_plan_step_graph(shk_plan* plan, void* u_a, void* u_b, int32_t nsteps, vo
 }
 
 int shk_plan_reduce(shk_plan* plan, const void* u, int32_t p, double* out, void* stream) {
-    if (!plan || !u || !out || (p != 0 && p != 1 && p != -1)) return SHK_EINVAL;
+    if (!plan || !u || !out || (p != 0 && p != 1 && p != 2 && p != -1)) return SHK_EINVAL;
     cudaStream_t st = as_stream(stream);
     const PlanDev D = plan->dev();
     if (plan->dtype == SHK_F64)
@@ -1226,3 +1242,33 @@ extern "C" int shk_apply_operator_lf_noalloc_f64(const shk_scheme* scheme, const
 extern "C" int64_t shk_apply_operator_lf_noalloc_max_cells(void) {
     return static_cast<int64_t>(kNoAllocMaxTiles) * kNoAllocTile;
 }
+
+// ===========================================================================
+// bounds-check build (libshocks_check.so): logs and test hooks
+// ===========================================================================
+#ifdef SHOCKS_BOUNDS_CHECK
+extern "C" int shk_check_tu_adjoint(shk::BoundsLog* out, int32_t reset);
+
+extern "C" int shk_check_bounds(int32_t reset, int32_t* flag, int32_t* block, int32_t* thread,
+                                int64_t* offset, int64_t* extent) {
+    SHK_CUDA(cudaDeviceSynchronize());
+    shk::BoundsLog logs[2] = {};
+    SHK_CUDA(shk::bounds_log_read(&logs[0], reset != 0));
+    const int r = shk_check_tu_adjoint(&logs[1], reset);
+    if (r != SHK_OK) return r;
+    const shk::BoundsLog* hit = logs[0].flag ? &logs[0] : (logs[1].flag ? &logs[1] : nullptr);
+    if (flag) *flag = hit ? 1 : 0;
+    if (block) *block = hit ? hit->block : -1;
+    if (thread) *thread = hit ? hit->thread : -1;
+    if (offset) *offset = hit ? hit->offset : 0;
+    if (extent) *extent = hit ? hit->extent : 0;
+    return SHK_OK;
+}
+
+extern "C" int shk_check_force_timeout(uint32_t extra_bytes, int64_t wait_limit) {
+    const long long lim = static_cast<long long>(wait_limit);
+    SHK_CUDA(cudaMemcpyToSymbol(shk::g_test_extra_tx, &extra_bytes, sizeof(extra_bytes)));
+    SHK_CUDA(cudaMemcpyToSymbol(shk::g_test_wait_limit, &lim, sizeof(lim)));
+    return SHK_OK;
+}
+#endif

@@ -40,15 +40,15 @@ __host__ __device__ inline int64_t imod(int64_t a, int64_t n) {
 // ---------------------------------------------------------------------------
 template <class T>
 struct Smem {
-    T* U;   // u at the start of the step (window)
-    T* S;   // stage state k1 / k2
-    T* H;   // half differences
-    T* D;   // half second differences; reused for face fluxes F
-    T* Q;   // 13/12 (2D)^2; reused for ES-WENO omega_0
-    T* UL;  // ul (value at the left face of the cell)
-    T* UR;  // ur (value at the right face of the cell)
-    T* I;   // float states: stage increments (see step_tile); null for double
-    int W;  // window length (cells) of every array
+    Win<T> U;   // u at the start of the step (window)
+    Win<T> S;   // stage state k1 / k2
+    Win<T> H;   // half differences
+    Win<T> D;   // half second differences; reused for face fluxes F
+    Win<T> Q;   // 13/12 (2D)^2; reused for ES-WENO omega_0
+    Win<T> UL;  // ul (value at the left face of the cell)
+    Win<T> UR;  // ur (value at the right face of the cell)
+    Win<T> I;   // float states: stage increments (see step_tile); null for double
+    int W;      // window length (cells) of every array
 
     // float states carry one more array (the stage increments)
     static constexpr int kArrays = sizeof(T) == 4 ? 8 : 7;
@@ -64,8 +64,9 @@ struct Smem {
     // values directly, so H and Q are not needed (6 arrays)
     __device__ void carve_compact(unsigned char* base, int W) {
         T* p = reinterpret_cast<T*>(base);
-        U = p; S = p + W; D = p + 2 * W; UL = p + 3 * W; UR = p + 4 * W; I = p + 5 * W;
-        H = Q = nullptr;
+        U = make_win(p, W); S = make_win(p + W, W); D = make_win(p + 2 * W, W);
+        UL = make_win(p + 3 * W, W); UR = make_win(p + 4 * W, W); I = make_win(p + 5 * W, W);
+        H = Q = Win<T>();
         this->W = W;
     }
     // compact layout of that mixed step: U (double window), then as float
@@ -73,22 +74,23 @@ struct Smem {
     // contiguous (the learned phase's warp scratch, before D takes the face
     // fluxes); Q aliases D (the learned reconstruction does not use it)
     __device__ void carve_mixed(unsigned char* base, int W) {
-        U = reinterpret_cast<T*>(base);
+        U = make_win(reinterpret_cast<T*>(base), W);
         float* f = reinterpret_cast<float*>(base + size_t(W) * sizeof(double));
-        S = reinterpret_cast<T*>(f);
-        I = reinterpret_cast<T*>(f + 2 * W);
-        H = reinterpret_cast<T*>(f + 3 * W);
-        D = reinterpret_cast<T*>(f + 4 * W);
-        UL = reinterpret_cast<T*>(f + 5 * W);
-        UR = reinterpret_cast<T*>(f + 6 * W);
+        S = win_cast<T>(make_win(f, 2 * W));
+        I = win_cast<T>(make_win(f + 2 * W, W));
+        H = win_cast<T>(make_win(f + 3 * W, W));
+        D = win_cast<T>(make_win(f + 4 * W, W));
+        UL = win_cast<T>(make_win(f + 5 * W, W));
+        UR = win_cast<T>(make_win(f + 6 * W, W));
         Q = D;
         this->W = W;
     }
     __device__ void carve(unsigned char* base, int W) {
         T* p = reinterpret_cast<T*>(base);
-        U = p; S = p + W; H = p + 2 * W; D = p + 3 * W; Q = p + 4 * W;
-        UL = p + 5 * W; UR = p + 6 * W;
-        I = kArrays > 7 ? p + 7 * W : nullptr;
+        U = make_win(p, W); S = make_win(p + W, W); H = make_win(p + 2 * W, W);
+        D = make_win(p + 3 * W, W); Q = make_win(p + 4 * W, W);
+        UL = make_win(p + 5 * W, W); UR = make_win(p + 6 * W, W);
+        I = kArrays > 7 ? make_win(p + 7 * W, W) : Win<T>();
         this->W = W;
     }
 };
@@ -133,9 +135,10 @@ struct BcView {
 
 // S: window array; g0: global cell of window position 0; [wlo, whi): the
 // positions holding values of this stage. Call after a barrier; ends with one.
-template <class V>
-__device__ void apply_bc(V* S, int64_t g0, int64_t n, int wlo, int whi, const BcView& bc,
+template <class PS>
+__device__ void apply_bc(PS S, int64_t g0, int64_t n, int wlo, int whi, const BcView& bc,
                          int stage) {
+    using V = elem_t<PS>;
     const int t = threadIdx.x;
     if (t < 6) {
         const int side = t / 3, k = t - 3 * side;
@@ -160,8 +163,9 @@ __device__ void apply_bc(V* S, int64_t g0, int64_t n, int wlo, int whi, const Bc
 // Neumann ghost (mirror - (2k+1) dx g) moves to its mirrored interior cell.
 // One thread walks the six ghosts in order (mirrors of the two sides can
 // coincide on tiny instances). Call after a barrier; ends with one.
-template <class V>
-__device__ void bc_transpose(V* z, int64_t g0, int64_t n, int wlo, int whi, const BcView& bc) {
+template <class PZ>
+__device__ void bc_transpose(PZ z, int64_t g0, int64_t n, int wlo, int whi, const BcView& bc) {
+    using V = elem_t<PZ>;
     if (threadIdx.x == 0) {
         for (int t = 0; t < 6; ++t) {
             const int side = t / 3, k = t - 3 * side;
@@ -180,8 +184,9 @@ __device__ void bc_transpose(V* z, int64_t g0, int64_t n, int wlo, int whi, cons
 
 // zero a window array at positions outside the instance [0, n) (the circular
 // loader wrapped them in): cotangents of a non-periodic instance
-template <class V>
-__device__ void zero_outside(V* z, int64_t g0, int64_t n, int wlo, int whi) {
+template <class PZ>
+__device__ void zero_outside(PZ z, int64_t g0, int64_t n, int wlo, int whi) {
+    using V = elem_t<PZ>;
     for (int w = wlo + threadIdx.x; w < whi; w += blockDim.x) {
         const int64_t gi = g0 + w;
         if (gi < 0 || gi >= n) z[w] = V(0);
@@ -207,11 +212,15 @@ __host__ __device__ inline OpParams<float> float_params(const OpParams<T>& p) {
     return f;
 }
 
-// 16-byte aligned start of a shared-memory scratch region
-template <class P>
-__device__ __forceinline__ float* learned_scratch(P* region) {
-    const uintptr_t a = reinterpret_cast<uintptr_t>(region);
-    return reinterpret_cast<float*>((a + 15) & ~uintptr_t(15));
+// the scratch of the learned phase: the nfloats floats of shared memory from
+// `region` that the layout leaves free in that phase, from a 16-byte aligned
+// start
+template <class PR>
+__device__ __forceinline__ Win<float> learned_scratch(PR region, int nfloats) {
+    float* r = reinterpret_cast<float*>(win_raw(region));
+    const uintptr_t a = reinterpret_cast<uintptr_t>(r);
+    float* s = reinterpret_cast<float*>((a + 15) & ~uintptr_t(15));
+    return make_win(s, nfloats - static_cast<int>(s - r));
 }
 
 // learned reconstruction of cells [clo, chi): one cell per lane, 32 cells per
@@ -220,14 +229,14 @@ __device__ __forceinline__ float* learned_scratch(P* region) {
 // window (v_{c+o} - v_c, o = -2..2) and rounded to float; the face values are
 // v_c + correction in the state precision.
 // scratch: kWarpScratch floats per warp of shared memory (16-byte aligned).
-template <class T>
-__device__ __forceinline__ void learned_phase(const T* v, int clo, int chi, T* UL, T* UR,
-                                              const LearnedParams& lp, float* scratch) {
+template <class T, class PV, class PO>
+__device__ __forceinline__ void learned_phase(PV v, int clo, int chi, PO UL, PO UR,
+                                              const LearnedParams& lp, const Win<float>& scratch) {
     MlpFrags f;
     mlp_load_frags(lp.mlp, f);
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    float* scr = scratch + warp * kWarpScratch;
+    float* scr = win_span(scratch, warp * kWarpScratch, kWarpScratch);
     const int ncell = chi - clo;
     const int myrow = 16 * (t >> 1) + 8 * (t & 1) + g;  // within the 32-cell block
     for (int q = warp; q * 32 < ncell; q += nw) {
@@ -251,8 +260,8 @@ __device__ __forceinline__ void learned_phase(const T* v, int clo, int chi, T* U
 // from the stage input v (valid on [lo-3, hi+3)). Leaves F / p.fscale in sm.D
 // (fscale = 1/4 for the FP64 Burgers-Rusanov flux with nu = 1, else 1).
 // ---------------------------------------------------------------------------
-template <class T, int EQ, int REC, int FLUX>
-__device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Smem<T>& sm,
+template <class T, int EQ, int REC, int FLUX, class PV>
+__device__ __forceinline__ void face_fluxes(PV v, int lo, int hi, const Smem<T>& sm,
                                             const OpParams<T>& p) {
     const int tid = threadIdx.x, nt = blockDim.x;
     if constexpr (REC == SHK_REC_WENOJS53 && sizeof(T) == 8) {
@@ -292,9 +301,10 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
         }
         __syncthreads();
     } else if constexpr (REC == SHK_REC_LEARNED) {
-        // warp scratch: H onward (free in this phase; every learned layout
-        // leaves at least 1027 floats there, see learned_scratch)
-        learned_phase<T>(v, lo - 1, hi + 1, sm.UL, sm.UR, p.lp, learned_scratch(sm.H));
+        // warp scratch: H onward (free in this phase: H and D, 2W floats, in
+        // every learned layout; with tiles of at least kLearnedMinTile that is
+        // more than the 8 x kWarpScratch + 3 floats needed)
+        learned_phase<T>(v, lo - 1, hi + 1, sm.UL, sm.UR, p.lp, learned_scratch(sm.H, 2 * sm.W));
         __syncthreads();
     } else if constexpr (REC == SHK_REC_CONSTANT) {
         // reconstruction.py:153-163: ul = ur = u
@@ -368,7 +378,7 @@ __device__ __forceinline__ void face_fluxes(const T* v, int lo, int hi, const Sm
 // Returns false if the bulk copy did not complete within the wait limit.
 // ---------------------------------------------------------------------------
 template <class T>
-__device__ bool load_window(T* dst, const T* base, int64_t n, int64_t g0, int W,
+__device__ bool load_window(Win<T> dst, const T* base, int64_t n, int64_t g0, int W,
                             uint64_t* bar, uint32_t& phase) {
     const size_t sz = sizeof(T);
     // a window no longer than its instance wraps at most once: one compare
@@ -385,7 +395,7 @@ __device__ bool load_window(T* dst, const T* base, int64_t n, int64_t g0, int W,
     bool bulk = false;
     if (threadIdx.x == 0) {
         bulk = (reinterpret_cast<uintptr_t>(base) % 16 == 0) &&
-               (reinterpret_cast<uintptr_t>(dst) % 16 == 0);
+               (reinterpret_cast<uintptr_t>(win_raw(dst)) % 16 == 0);
         int64_t pos = g0;
         const int64_t end = g0 + W;
         int npieces = 0;
@@ -399,18 +409,24 @@ __device__ bool load_window(T* dst, const T* base, int64_t n, int64_t g0, int W,
     }
     bulk = __syncthreads_or(bulk);
     if (!bulk) {
-        for (int w = threadIdx.x; w < W; w += blockDim.x) dst[w] = base[wrap(g0 + w)];
+        for (int w = threadIdx.x; w < W; w += blockDim.x) {
+            const int64_t src = wrap(g0 + w);
+            if (chk_index(src, n)) dst[w] = base[src];
+        }
         __syncthreads();
         return true;
     }
     if (threadIdx.x == 0) {
-        mbar_expect_tx(bar, static_cast<uint32_t>(W * sz));
+        mbar_expect_tx(bar, static_cast<uint32_t>(W * sz) + test_extra_tx());
         int64_t pos = g0;
         const int64_t end = g0 + W;
         while (pos < end) {
             const int64_t src = wrap(pos);
             const int64_t len = min(end - pos, n - src);
-            bulk_g2s(dst + (pos - g0), base + src, static_cast<uint32_t>(len * sz), bar);
+            // (bounds-check build: a piece outside the window or the instance is
+            // not copied; the wait for it then expires)
+            if (chk_index(src, n) && chk_index(src + len - 1, n) && win_fits(dst, pos - g0, len))
+                bulk_g2s(win_raw(dst) + (pos - g0), base + src, static_cast<uint32_t>(len * sz), bar);
             pos += len;
         }
     }
@@ -451,21 +467,22 @@ __host__ __device__ inline DtState compute_dt(double smax, double cfl, double th
 // ---------------------------------------------------------------------------
 template <class S>
 struct StageOut {
-    S* k1 = nullptr;
-    S* k2 = nullptr;
-    S* ulu = nullptr;
-    S* uru = nullptr;
-    S* ul1 = nullptr;
-    S* ur1 = nullptr;
-    S* ul2 = nullptr;  // face values of k2
-    S* ur2 = nullptr;
+    Win<S> k1 = nullptr;
+    Win<S> k2 = nullptr;
+    Win<S> ulu = nullptr;
+    Win<S> uru = nullptr;
+    Win<S> ul1 = nullptr;
+    Win<S> ur1 = nullptr;
+    Win<S> ul2 = nullptr;  // face values of k2
+    Win<S> ur2 = nullptr;
 };
 template <class T, int REC>
 using stage_t = typename std::conditional<sizeof(T) == 8 && REC != SHK_REC_LEARNED, double, float>::type;
 
 // the tile's interior [HL, HL + te) of a window array into out
-template <class S, class V>
-__device__ __forceinline__ void store_interior(S* out, const V* w, int HL, int te) {
+template <class PO, class PW>
+__device__ __forceinline__ void store_interior(PO out, PW w, int HL, int te) {
+    using S = elem_t<PO>;
     if (out)
         for (int i = HL + threadIdx.x; i < HL + te; i += blockDim.x) out[i - HL] = static_cast<S>(w[i]);
 }
@@ -491,7 +508,7 @@ __device__ __forceinline__ void store_interior(S* out, const V* w, int HL, int t
 // skips their recompute; gout may be null when only those are wanted (the
 // last stage is skipped).
 template <int EQ, int FLUX>
-__device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* gout, int te,
+__device__ unsigned long long step_tile_mixed(const Smem<double>& sm, Win<double> gout, int te,
                                               double dtdx, const OpParams<double>& p,
                                               const BcView& bc, int64_t g0, int64_t n,
                                               const StageOut<float>& so = StageOut<float>()) {
@@ -499,16 +516,16 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
     const int tid = threadIdx.x, nt = blockDim.x, W = sm.W;
     const OpParams<float> pf = float_params(p);
     Smem<float> fs;
-    fs.U = reinterpret_cast<float*>(sm.S);
+    fs.U = win_cast<float>(sm.S);
     fs.S = fs.U + W;
-    fs.H = reinterpret_cast<float*>(sm.H);
-    fs.D = reinterpret_cast<float*>(sm.D);
-    fs.Q = reinterpret_cast<float*>(sm.Q);
-    fs.UL = reinterpret_cast<float*>(sm.UL);
-    fs.UR = reinterpret_cast<float*>(sm.UR);
-    fs.I = reinterpret_cast<float*>(sm.I);
+    fs.H = win_cast<float>(sm.H);
+    fs.D = win_cast<float>(sm.D);
+    fs.Q = win_cast<float>(sm.Q);
+    fs.UL = win_cast<float>(sm.UL);
+    fs.UR = win_cast<float>(sm.UR);
+    fs.I = win_cast<float>(sm.I);
     fs.W = W;
-    float* inc = fs.I;
+    const Win<float> inc = fs.I;
     const float dtf = static_cast<float>(dtdx);
     for (int i = tid; i < te + 2 * HL; i += nt) fs.U[i] = static_cast<float>(sm.U[i]);
     __syncthreads();
@@ -558,7 +575,7 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, double* go
 // so: what the reverse sweep keeps of this step (StageOut); gout may then be
 // null (the last stage is skipped)
 template <class T, int EQ, int REC, int FLUX>
-__device__ typename Bits<T>::type step_tile(const Smem<T>& sm, T* gout, int te, T dtdx,
+__device__ typename Bits<T>::type step_tile(const Smem<T>& sm, Win<T> gout, int te, T dtdx,
                                             const OpParams<T>& p, const BcView& bc = BcView(),
                                             int64_t g0 = 0, int64_t n = 0,
                                             const StageOut<stage_t<T, REC>>& so = StageOut<stage_t<T, REC>>()) {

@@ -231,7 +231,16 @@ def adjoint_step(
         _, fn = torch.func.vjp(lambda v: advance(stepper, dt, t, v), u)
         return fn(p)[0]
 
-    chk = load(stepper.checkpoint, maxit)
+    def _load(m):
+        # file checkpoints return host arrays: the state goes back to p's device
+        chk = dict(load(stepper.checkpoint, m))
+        if not isinstance(chk["u"], torch.Tensor):
+            chk["u"] = torch.as_tensor(chk["u"], device=p0.device)
+        chk["t"] = _as_float(torch.as_tensor(chk["t"]))
+        chk["m"] = int(chk["m"])
+        return chk
+
+    chk = _load(maxit)
     assert chk["m"] == maxit
     t = tfinal = chk["t"]
     p = p0
@@ -244,7 +253,7 @@ def adjoint_step(
         p = apply_boundary(chk["t"], chk["u"], p)
     yield AdjointStepCompleted(t=t, tfinal=tfinal, dt=0.0, iteration=maxit, u=chk["u"], p=p)
     for m in range(maxit - 1, -1, -1):
-        chk = load(stepper.checkpoint, m)
+        chk = _load(m)
         dt = t - chk["t"]
         assert chk["m"] == m
         p = _vjp(dt, chk["t"], chk["u"], p)

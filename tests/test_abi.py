@@ -12,12 +12,10 @@ import pytest
 ROOT = pathlib.Path(__file__).resolve().parents[1]
 
 
-def _declared_functions() -> list[str]:
-    names = []
-    for h in sorted((ROOT / "include").glob("*.h")):
-        text = h.read_text()
-        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-        names += re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(shk_\w+)\s*\(", text, flags=re.M)
+def _declared_functions(header: str = "shocks.h") -> list[str]:
+    text = (ROOT / "include" / header).read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?\w+\s*\*?\s*(shk_\w+)\s*\(", text, flags=re.M)
     return sorted(set(names))
 
 
@@ -27,6 +25,14 @@ def cdll():
 
     _build.build()
     return _lib.load_library()
+
+
+@pytest.fixture(scope="module")
+def checked_cdll():
+    from pyshocks_gb300 import _build, _lib
+
+    _build.build(variants=("check",))
+    return _lib.load_check_library()
 
 
 def test_header_declares_functions():
@@ -46,6 +52,22 @@ def test_ctypes_prototypes_cover_header(cdll):
 
     assert set(_declared_functions()) == set(_lib.SIGNATURES), (
         set(_declared_functions()) ^ set(_lib.SIGNATURES))
+    assert set(_declared_functions("shocks_check.h")) == set(_lib.CHECK_SIGNATURES)
+
+
+def test_headers_cover_every_header_file():
+    """Every header under include/ is one of the two checked here."""
+    assert sorted(p.name for p in (ROOT / "include").glob("*.h")) == ["shocks.h", "shocks_check.h"]
+
+
+def test_check_library_exports_the_library_abi_and_its_hooks(checked_cdll, cdll):
+    """libshocks_check.so (the bounds-check build) is a drop-in for
+    libshocks.so with two more entry points; libshocks.so has neither."""
+    names = _declared_functions() + _declared_functions("shocks_check.h")
+    missing = [n for n in names if not hasattr(checked_cdll, n)]
+    assert not missing, missing
+    for n in _declared_functions("shocks_check.h"):
+        assert not hasattr(cdll, n), n
 
 
 def test_strerror_without_gpu(cdll):
@@ -123,20 +145,3 @@ def test_product_path_never_imports_the_oracle():
         text = p.read_text()
         assert "oracle" not in re.findall(r"(?:import|from)\s+(\w+)", text), p
         assert "numpy_ref" not in text and "torch_ref" not in text, p
-
-
-def test_integration_notes_cover_every_entry_point():
-    """Every function that include/shocks.h declares has a row (or a grouped
-    mention such as ``shk_plan_create/reset``) in INTEGRATION.md."""
-    import re
-
-    header = (ROOT / "include" / "shocks.h").read_text()
-    notes = (ROOT / "INTEGRATION.md").read_text()
-    names = set(re.findall(r"\b(shk_[a-z0-9_]+)\s*\(", header))
-    mentioned = set(re.findall(r"\b(shk_[a-z0-9_]+)", notes))
-    for group in re.findall(r"`(shk_[a-z0-9_]+(?:/[a-z0-9_]+)+)`", notes):
-        head, *rest = group.split("/")
-        for tail in rest:  # shk_plan_create/reset -> shk_plan_reset (any common prefix)
-            parts = head.split("_")
-            mentioned.update("_".join(parts[:i] + [tail]) for i in range(2, len(parts)))
-    assert sorted(names - mentioned) == []

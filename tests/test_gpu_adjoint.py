@@ -276,3 +276,35 @@ def test_plain_results_do_not_depend_on_the_tile():
     for o, g in zip(outs[1:], grads[1:]):
         assert torch.equal(o, outs[0])
         assert torch.equal(g, grads[0])
+
+
+def test_step_and_adjoint_step_through_npz_checkpoints(tmp_path):
+    """``step`` saving every state to ``.npz`` files (keys m, t, u; the
+    reference's ``NumpyCheckpoint``, ``src/pyshocks/checkpointing.py:209-254``)
+    and ``adjoint_step`` reading them back give the in-memory run's states and
+    gradient bit for bit."""
+    import pyshocks_gb300 as gb
+    from pyshocks_gb300.checkpointing import InMemoryCheckpoint, NumpyCheckpoint, load
+
+    n, maxit = 96, 12
+    g = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+    u0 = torch.tensor(R.exact_cell_average_sine(g), device="cuda")
+    grid = gb.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
+    bc = gb.scalar.PeriodicBoundary()
+    out = {}
+    for name, chk in (("mem", InMemoryCheckpoint("Iteration")),
+                      ("npz", NumpyCheckpoint("Iteration", dirname=tmp_path))):
+        stepper = gb.timestepping.make_time_stepper(_scheme(), grid, bc, theta=1.0,
+                                                    checkpoint=chk)
+        for ev in gb.timestepping.step(stepper, u0, maxit=maxit):
+            pass
+        uT = ev.u
+        for ev in gb.timestepping.adjoint_step(stepper, uT.clone(), maxit=maxit):
+            pass
+        out[name] = (uT, ev.p, chk)
+    assert torch.equal(out["mem"][0], out["npz"][0])
+    assert torch.equal(out["mem"][1], out["npz"][1])
+    assert sorted(p.name for p in tmp_path.iterdir())[-1] == f"Iteration_{maxit:09d}.npz"
+    last = load(out["npz"][2], maxit)
+    assert int(last["m"]) == maxit
+    np.testing.assert_array_equal(last["u"], out["mem"][0].cpu().numpy())

@@ -525,3 +525,50 @@ def test_full_size_shift_equivariance_and_conservation(gb, dtype):
         assert torch.equal(torch.roll(a[b], shift), s.instance(b)), b
     tol = 1.0e-13 if dtype == torch.float64 else 1.0e-6
     assert np.max(np.abs(m1 - m0) / np.array(sizes)) < tol
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_norms_match_oracle(gb, dtype):
+    """``norm``/``rnorm`` of ``src/pyshocks/grid.py:444-531`` (p = 1, 2, inf,
+    weighted or not) on device tensors, and the batched plan's FP64 reductions
+    (``shk_plan_reduce`` p = 0, 1, 2, inf through ``BatchedSolver.norm``)
+    against the oracle's NumPy norms: 1e-13 relative for float64 states, 1e-6
+    for float32 ones (the state's own rounding; the sums are FP64)."""
+    from pyshocks_gb300.batched import BatchedSolver
+
+    tol = 1.0e-13 if dtype == torch.float64 else 1.0e-6
+    sizes = [1024, 333, 7, 4096]
+    rng = np.random.default_rng(17)
+    u0s, v0s = [], []
+    for n in sizes:
+        og = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+        u0s.append(R.random_fourier_ic(rng, og.f))
+        v0s.append(R.random_fourier_ic(rng, og.f))
+    for n, u0, v0 in zip(sizes, u0s, v0s):
+        og = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+        grid = gb.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
+        uq = torch.tensor(u0, device="cuda").to(dtype)
+        vq = torch.tensor(v0, device="cuda").to(dtype)
+        ur = uq.double().cpu().numpy()
+        vr = vq.double().cpu().numpy()
+        for p in (1, 2, np.inf):
+            for w in (False, True):
+                ref = R.norm(og, ur, p=p, weighted=w)
+                got = float(gb.norm(grid, uq, p=p, weighted=w))
+                assert abs(got - ref) <= tol * abs(ref), (n, p, w)
+                rr = R.rnorm(og, ur, vr, p=p, weighted=w)
+                rg = float(gb.rnorm(grid, uq, vq, p=p, weighted=w))
+                assert abs(rg - rr) <= 10 * tol * abs(rr), (n, p, w)
+    scheme = _scheme(gb, "rusanov")
+    solver = BatchedSolver(scheme, sizes, [2.0 / n for n in sizes], dtype=dtype)
+    solver.reset(torch.tensor(np.concatenate([u[3:-3] for u in u0s])))
+    for b, n in enumerate(sizes):
+        og = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+        ur = solver.instance(b).double().cpu().numpy()
+        g = np.concatenate([np.zeros(3), ur, np.zeros(3)])
+        for p in (1, 2, np.inf):
+            for w in (False, True):
+                ref = R.norm(og, g, p=p, weighted=w)
+                got = float(solver.norm(p, weighted=w)[b])
+                assert abs(got - ref) <= tol * abs(ref), (n, p, w)
+        assert abs(float(solver.reduce(0)[b]) - float(np.sum(ur))) <= tol * float(np.sum(np.abs(ur)))

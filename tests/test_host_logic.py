@@ -130,3 +130,27 @@ def test_scheme_names_follow_the_reference():
         assert reconstruction.make_reconstruction_from_name(name) is not None
     with pytest.raises(NotImplementedError):
         reconstruction.make_reconstruction_from_name("ssweno242")
+
+
+@pytest.mark.parametrize(("bits", "exc", "match"), [
+    (0, None, None),
+    (L.ERR_NONFINITE, ValueError, "not finite"),
+    (L.ERR_TIMEOUT, RuntimeError, "bounded device wait"),
+    (L.ERR_BOUNDS, RuntimeError, "left its array"),
+    (L.ERR_NONFINITE | L.ERR_TIMEOUT, ValueError, "not finite"),
+])
+def test_status_bits_raise_on_the_host(bits, exc, match):
+    """BatchedSolver.check_status decodes the plan's status word: the device
+    sets ERR_NONFINITE (the reference's non-finite dt ValueError,
+    timestepping.py:144-145), ERR_TIMEOUT (an expired bounded wait) or
+    ERR_BOUNDS (the bounds-check build); the word is read through status(),
+    replaced here by a stub returning the bits."""
+    from pyshocks_gb300.batched import BatchedSolver
+
+    s = object.__new__(BatchedSolver)
+    s.status = lambda: bits
+    if exc is None:
+        s.check_status()
+    else:
+        with pytest.raises(exc, match=match):
+            s.check_status()
