@@ -582,6 +582,7 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
     rates = {}
     shapes = {}
     for name, sch, dt in (("plain_f64", plain, torch.float64),
+                          ("plain_f32", plain, torch.float32),
                           ("learned_f64", lscheme, torch.float64),
                           ("learned_f32", lscheme, torch.float32)):
         s = BatchedSolver(sch, [n] * B, 2.0 / n, dtype=dt, tile=args.tile)
@@ -593,7 +594,8 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
     prm = workload_params(SEED + 5, batch=Bl)[1]
 
     def run(sch, nn, dt):
-        s = BatchedSolver(sch, [nn] * Bl, 2.0 / nn, dtype=dt)
+        """The B=64 accuracy set on nn cells to t=T: (state, steps taken)."""
+        s = BatchedSolver(sch, [nn] * Bl, 2.0 / nn, dtype=dt, max_steps=2 * nn)
         with torch.cuda.stream(stream):
             s.reset(initial_state(np.full(Bl, nn), prm, dev), tfinal=T)
             while float(s.time().min()) < T:
@@ -601,25 +603,41 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
             stream.synchronize()
         if s.status():
             raise RuntimeError("accuracy run failed")
-        return s.u.double().reshape(Bl, nn)
+        # mean number of steps an instance takes to reach T (per-instance CFL dt)
+        steps = float((s.dt_history() > 0).sum(0).double().mean())
+        return s.u.double().reshape(Bl, nn), steps
 
-    ref = run(plain, n * r, torch.float64).reshape(Bl, n, r).mean(-1)
+    fine, _ = run(plain, n * r, torch.float64)
+    # cumulative integral of the fine piecewise-constant solution at its faces
+    nf = n * r
+    cum = torch.cat([torch.zeros(Bl, 1, dtype=torch.float64, device=dev),
+                     torch.cumsum(fine, -1) * (2.0 / nf)], -1)
 
     def l1(u):
-        return float((u - ref).abs().sum(-1).mean() * 2.0 / n)
+        """L1 distance to the fine solution averaged onto u's cells (exact
+        cell averages of the piecewise-constant fine solution, any N)."""
+        nn = u.shape[-1]
+        xf = torch.arange(nn + 1, dtype=torch.float64, device=dev) * (nf / nn)
+        i0 = torch.clamp(xf.floor().long(), max=nf - 1)
+        w = xf - i0
+        F = cum[:, i0] + w * (cum[:, i0 + 1] - cum[:, i0])
+        avg = (F[:, 1:] - F[:, :-1]) / (2.0 / nn)
+        return float((u - avg).abs().sum(-1).mean() * 2.0 / nn)
 
-    err = {"plain_f64": l1(run(plain, n, torch.float64)),
-           "plain_f32": l1(run(plain, n, torch.float32)),
-           "learned_f64": l1(run(lscheme, n, torch.float64)),
-           "learned_f32": l1(run(lscheme, n, torch.float32)),
-           "untrained_f64": l1(run(uscheme, n, torch.float64))}
+    runs = {"plain_f64": run(plain, n, torch.float64), "plain_f32": run(plain, n, torch.float32),
+            "learned_f64": run(lscheme, n, torch.float64),
+            "learned_f32": run(lscheme, n, torch.float32),
+            "untrained_f64": run(uscheme, n, torch.float64)}
+    err = {k_: l1(v[0]) for k_, v in runs.items()}
+    iso = bench_iso_l1(plain, lscheme, run, l1, err, runs, rates, stream, dev, args, B, n, T)
     adj = {"learned_f64": _adjoint_rate(lscheme, dev, args.adjoint_steps, torch.float64, tile=args.tile),
            "learned_f32": _adjoint_rate(lscheme, dev, args.adjoint_steps, torch.float32, tile=args.tile)}
     return {
         "forward": {"unit": "cell-steps/s", "config": {"batch": B, "n": n, "steps": k},
                     "launch_shapes": shapes, **rates,
                     "speedup_learned_f64": rates["learned_f64"] / rates["plain_f64"],
-                    "speedup_learned_f32": rates["learned_f32"] / rates["plain_f64"]},
+                    "speedup_learned_f32": rates["learned_f32"] / rates["plain_f64"],
+                    "learned_f64_vs_plain_f32": rates["learned_f64"] / rates["plain_f32"]},
         "adjoint": {"unit": "gradients/s", "plain_f64": adjoint_plain["value"],
                     "launch_shapes": {"plain_f64": adjoint_plain["config"]["launch_shape"],
                                       "learned_f64": adj["learned_f64"]["config"]["launch_shape"],
@@ -628,12 +646,74 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
                     "learned_f32": adj["learned_f32"]["value"],
                     "speedup_learned_f64": adj["learned_f64"]["value"] / adjoint_plain["value"],
                     "speedup_learned_f32": adj["learned_f32"]["value"] / adjoint_plain["value"]},
-        "l1_vs_fine_plain": {"config": {"batch": Bl, "n": n, "t_final": T, "fine": n * r}, **err},
+        "l1_vs_fine_plain": {"config": {"batch": Bl, "n": n, "t_final": T, "fine": n * r},
+                             **err, "steps": {k_: v[1] for k_, v in runs.items()}},
+        "iso_l1": iso,
         "note": ("learned_f64 keeps the state and its accumulation in float64 and runs the "
                  "operator in float32 (bfloat16 tensor-core network); learned_f32 also "
                  "stores the state in float32. untrained_f64: the network at initialisation "
                  "(softmax at the ideal weights) with the same trust band"),
     }
+
+
+def bench_iso_l1(plain, lscheme, run, l1, err, runs, rates, stream, dev, args, B, n, T) -> dict:
+    """Learned vs plain at equal L1 error. The plain scheme (float64 and
+    float32 state) is run on finer grids of the same accuracy set until its L1
+    against the fine solution reaches the learned scheme's L1 at N=n (a
+    resolution ladder, then a log-log interpolation between the bracketing
+    resolutions, rounded up to a multiple of 64 and verified by a run there).
+    Time to solution is for the configuration's batch (B instances to t=T):
+    B x N x (mean steps an instance takes to reach T on that grid) / the
+    cell-steps/s measured at B x N. The ratios are plain time / learned time."""
+    import math
+
+    import torch
+
+    from pyshocks_gb300.batched import BatchedSolver
+
+    target = err["learned_f64"]
+    k = args.steps + (args.steps % 2)
+
+    def rate_at(sch, nn, dt):
+        s = BatchedSolver(sch, [nn] * B, 2.0 / nn, dtype=dt, tile=args.tile)
+        u0 = initial_state(np.full(B, nn), workload_params(SEED + 4, batch=B)[1], dev)
+        r = B * nn / (_timed_steps(s, u0, k, stream) * 1e-3)
+        del s
+        return r
+
+    out = {"target_l1": target, "learned_n": n,
+           "config": {"batch": B, "t_final": T, "accuracy_batch": 64}}
+    lsteps = runs["learned_f64"][1]
+    t_learned = B * n * lsteps / rates["learned_f64"]
+    out["learned_f64"] = {"n": n, "l1": target, "steps": lsteps, "rate": rates["learned_f64"],
+                          "time_to_solution_s": t_learned}
+    for name, dt in (("plain_f64", torch.float64), ("plain_f32", torch.float32)):
+        pts = [(n, err[name])]
+        nn = n
+        while pts[-1][1] > target and nn < 2 * n:
+            nn += n // 8
+            pts.append((nn, l1(run(plain, nn, dt)[0])))
+        if pts[-1][1] > target:
+            raise RuntimeError(f"{name}: no grid up to {nn} cells reaches L1 {target:.3e}")
+        if len(pts) == 1:
+            nstar = n
+        else:
+            (n1, e1), (n2, e2) = pts[-2], pts[-1]
+            p = math.log(e1 / e2) / math.log(n2 / n1) if e1 > e2 else 1.0
+            nstar = n1 * (e1 / target) ** (1.0 / p)
+            nstar = int(math.ceil(nstar / 64.0)) * 64
+        u, steps = run(plain, nstar, dt)
+        e = l1(u)
+        while e > target:
+            nstar += 64
+            u, steps = run(plain, nstar, dt)
+            e = l1(u)
+        r = rate_at(plain, nstar, dt)
+        t = B * nstar * steps / r
+        out[name] = {"n": nstar, "l1": e, "steps": steps, "rate": r, "time_to_solution_s": t,
+                     "ladder": [[a, b] for a, b in pts]}
+        out[f"ratio_learned_f64_vs_{name}"] = t / t_learned
+    return out
 
 
 def bench_inverse(dev, args) -> dict:
@@ -715,10 +795,11 @@ def main() -> None:
     ap.add_argument("--adjoint-steps", type=int, default=4000)
     ap.add_argument("--accuracy-steps", type=int, default=2000,
                     help="steps of the float32-vs-float64 comparison of the batch (full: 2000)")
-    ap.add_argument("--inverse-steps", type=int, default=300,
-                    help="SSPRK33 steps per solve of the inverse-problem leg (full: 3000)")
-    ap.add_argument("--inverse-iters", type=int, default=3,
-                    help="timed gradient-descent iterations of the inverse-problem leg (full: 50)")
+    ap.add_argument("--inverse-steps", type=int, default=3000,
+                    help="SSPRK33 steps per solve of the inverse-problem leg (the configuration's 3000)")
+    ap.add_argument("--inverse-iters", type=int, default=2,
+                    help="timed gradient-descent iterations of the inverse-problem leg (of the "
+                         "configuration's 50)")
     ap.add_argument("--inverse-only", action="store_true",
                     help="run only the inverse-problem leg (one JSON line)")
     ap.add_argument("--scheme", choices=["plain", "plain32", "learned", "learned32"], default="plain",

@@ -242,4 +242,6 @@ def main(refdir: pathlib.Path) -> None:
 
 
 if __name__ == "__main__":
-    main(pathlib.Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of a pyshocks source checkout>")
+    main(pathlib.Path(sys.argv[1]))

@@ -253,3 +253,87 @@ def test_learned_results_do_not_depend_on_the_tile(dtype):
     for o, g in zip(outs[1:], grads[1:]):
         assert torch.equal(o, outs[0])
         assert torch.equal(g, grads[0])
+
+
+def _trained_case(n, kind):
+    if kind == "sine":
+        return R.exact_cell_average_sine(R.make_uniform_cell_grid(-1.0, 1.0, n, 3))[3:-3][None]
+    import bench
+
+    _, prm = bench.workload_params(bench.SEED + 4, batch=4)
+    return bench.initial_state(np.full(4, n), prm, "cpu").reshape(4, n).numpy()
+
+
+@pytest.mark.parametrize(("n", "nsteps", "kind"), [(256, 150, "sine"), (4096, 100, "fourier")])
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_trained_network_steps_match_oracle(n, nsteps, kind, dtype):
+    """The shipped network (``load_default_params``, the one the benchmark
+    uses) stepped for 100-150 steps through shocks: the config-1 sine at N=256
+    past shock formation, and four bench-family states (Fourier modes and
+    jumps) at N=4096, against the oracle's learned scheme with the same
+    bfloat16 roundings and the same dt sequence.
+
+    Tolerances, and why: the kernels form the stencil differences, the
+    normalisation and the softmax in float32 (the oracle in float64) and use
+    tanh.approx.bf16x2 (the oracle rounds an exact tanh), so a few of the
+    bfloat16 roundings differ. Flipping 1 % of the oracle's bfloat16 roundings
+    moves these trajectories by at most 1.2e-5 of the initial range (L1 4e-7,
+    a thousandth of the method's L1 error against the fine solution,
+    1.9e-4 at N=4096). The bar is 2e-3 of the range in max-abs and 2e-5 in
+    L1 (a tenth of the method error). The fraction of faces in the WENO-JS
+    fallback at the final state is reported (and must be below 5 %)."""
+    from pyshocks_gb300 import learned
+    from pyshocks_gb300.batched import BatchedSolver
+
+    params = learned.load_default_params()
+    assert learned.DEFAULT_PARAMS.exists()
+    u0 = _trained_case(n, kind)
+    B = u0.shape[0]
+    solver = BatchedSolver(_scheme(params), [n] * B, 2.0 / n, dtype=dtype, max_steps=nsteps)
+    solver.reset(torch.tensor(u0.reshape(-1)))
+    solver.step(nsteps)
+    assert solver.status() == 0
+    got = solver.u.double().cpu().reshape(B, n)
+    dts = solver.dt_history().cpu()
+    wts = {"params": params.double().cpu(), "tau": 1.0e-2, "band": 0.1, "bf16": True}
+    u0t = torch.tensor(u0, dtype=dtype).double()
+    ref, _ = T.forward(u0t, 2.0 / n, nsteps, dts=dts, rec="learned", weights=wts)
+    rng = torch.tensor(np.ptp(u0, axis=-1))
+    d = (got - ref).abs()
+    maxrel = float((d.amax(-1) / rng).max())
+    l1 = float((d.mean(-1) * 2.0).max())
+    (_, _), (fr, fl) = LR.cell_face_values(wts["params"], LR.stencils_periodic(ref), eps=1.0e-6,
+                                           tau=1.0e-2, band=0.1, bf16=True, return_fallback=True)
+    fallback = float(torch.cat([fr, fl]).double().mean())
+    print(f"trained network n={n} steps={nsteps} {dtype}: max-abs/range {maxrel:.3e}, "
+          f"L1 {l1:.3e}, fallback faces {fallback:.4f}")
+    assert maxrel < 2.0e-3, maxrel
+    assert l1 < 2.0e-5, l1
+    assert fallback < 0.05
+
+
+@pytest.mark.parametrize(("n", "nsteps"), [(256, 40), (4096, 12)])
+def test_trained_network_adjoint_matches_autograd(n, nsteps):
+    """The hand-written adjoint (MLP backward on the tensor cores) of the
+    shipped network against torch autograd through the oracle's learned scheme
+    with the same bfloat16 roundings and frozen dt, J = 1/2 |u(T) - u_target|^2,
+    float32 state. Tolerance 5e-3 relative, as for the untrained network (float
+    operator, tanh.approx, fp16 backward products)."""
+    from pyshocks_gb300 import learned
+    from pyshocks_gb300.adjoint import CheckpointedSolve
+    from pyshocks_gb300.batched import BatchedSolver
+
+    params = learned.load_default_params()
+    u0 = _trained_case(n, "sine")[0]
+    tgt = u0 + 0.05 * np.sin(3 * np.pi * np.linspace(-1, 1, n, endpoint=False))
+    solver = BatchedSolver(_scheme(params), [n], 2.0 / n, dtype=torch.float32, max_steps=nsteps)
+    cs = CheckpointedSolve(solver, nsteps)
+    uT = cs.forward(torch.tensor(u0))
+    g = cs.backward(uT - torch.tensor(tgt, device="cuda", dtype=torch.float32)).double().cpu()
+    wts = {"params": params.double().cpu(), "tau": 1.0e-2, "band": 0.1, "bf16": True}
+    u0t = torch.tensor(u0, dtype=torch.float32).double()[None]
+    ref, _, _ = T.adjoint_gradient(u0t, torch.tensor(tgt)[None], 2.0 / n, nsteps,
+                                   dts=solver.dt_history().cpu(), rec="learned", weights=wts)
+    err = float((g - ref[0]).abs().max() / ref.abs().max())
+    print(f"trained network adjoint n={n} steps={nsteps}: max rel err {err:.3e}")
+    assert err < 5.0e-3, err
