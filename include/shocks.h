@@ -313,6 +313,46 @@ int shk_plan_adjoint_staged(shk_plan* plan, const void* ckpt, int32_t stride, in
  * a fixed order (deterministic for a given plan). */
 int shk_plan_reduce(shk_plan* plan, const void* u, int32_t p, double* out, void* stream);
 
+/* ---- the reference's ghosted step, forward and exact transpose ---------- */
+
+/* Single instance on the reference's ghosted array of n + 2 nghosts cells, with
+ * the reference's own arithmetic on the whole array: every operator evaluation
+ * fills the ghosts by the boundary at its stage time (scalar.py:397-540), the
+ * reconstruction sees zeros beyond the array ends (the zero-padded "same"
+ * convolutions of convolve.py:113-114), the fluxes at the two array ends are
+ * zero (scalar.py:249), and the ghost cells have outputs. Schemes: Rusanov
+ * (any alpha, via nu) or global Lax-Friedrichs (scalar.py:258-278: the wave
+ * speed is the maximum of |f'| over the whole filled array) with the
+ * constant or WENO-JS5 reconstruction; Burgers, advection or LWR. nghosts >=
+ * the reconstruction's stencil width (1 constant, 3 WENO-JS5), and <= 3 with a
+ * Dirichlet / Neumann boundary. `workspace` is caller device memory of at
+ * least shk_ghosted_workspace_bytes(n, nghosts) bytes (256-byte aligned
+ * inside); nothing is allocated. */
+int64_t shk_ghosted_workspace_bytes(int64_t n, int32_t nghosts);
+
+/* apply_operator (schemes.py:339-346) on every cell, ghosts included. */
+int shk_apply_operator_ghosted_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
+                                   double* out, int64_t n, int32_t nghosts, double dx, void* workspace,
+                                   int64_t workspace_bytes, void* stream);
+
+/* advance() of SSPRK33 (timestepping.py:312-320) on the raw ghosted array:
+ * u_out = 1/3 u + 2/3 (k2 + dt L(k2)) on every cell, the ghosts included (the
+ * raw ghost values pass through), with the boundary at t, t + dt, t + dt/2. */
+int shk_ssprk33_step_ghosted_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
+                                 double* u_out, int64_t n, int32_t nghosts, double dx, double dt,
+                                 void* workspace, int64_t workspace_bytes, void* stream);
+
+/* p_out = J^T p_next with J the Jacobian of that step with respect to the whole
+ * ghosted u (dt frozen): the `jac.T @ p` of adjoint_step (timestepping.py:174,
+ * 205-206), matrix-free. Ghost entries of p_next reach the interior through
+ * the operator's ghost rows; ghost entries of p_out are the pass-through
+ * (= p_next's, the raw ghost inputs of L being overwritten by the boundary).
+ * max() and |.| follow JAX's tie conventions (an even split). */
+int shk_ssprk33_vjp_ghosted_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
+                                const double* p_next, double* p_out, int64_t n, int32_t nghosts,
+                                double dx, double dt, void* workspace, int64_t workspace_bytes,
+                                void* stream);
+
 /* ---- no-allocation variant --------------------------------------------- */
 
 /* Lax-Friedrichs apply_operator for callers that cannot allocate device

@@ -255,3 +255,107 @@ def exact_cell_average_sine_periodic(n: int, a: float = -1.0, b: float = 1.0, me
     h = (b - a) / n
     f = torch.linspace(a, b, n + 1, dtype=torch.float64)
     return mean + (torch.cos(math.pi * f[:-1]) - torch.cos(math.pi * f[1:])) / (math.pi * h)
+
+
+# {{{ one ghosted instance: the reference's array arithmetic (adjoint_step)
+
+# The single-instance adjoint_step of the reference (src/pyshocks/timestepping.py:
+# 155-215) differentiates advance() over the whole ghosted array of n + 2g
+# cells. These functions restate that array arithmetic in torch, so that
+# torch.func.vjp gives the same J^T p as jax.jacfwd (both exact derivatives;
+# max() and |.| share JAX's conventions: an even split at ties, d|x|/dx(0) = 0):
+#   ghost fill        src/pyshocks/scalar.py:419-429 (Dirichlet), 469-495
+#                     (Neumann), 529-540 (periodic: right ghosts, then left)
+#   reconstruction    src/pyshocks/reconstruction.py:153-163 (constant),
+#                     351-377 (WENO-JS5, zero-padded "same" convolutions,
+#                     src/pyshocks/convolve.py:113-114)
+#   Rusanov / LF      src/pyshocks/scalar.py:192-278 (zero-padded face array)
+#   operator, SSPRK33 src/pyshocks/schemes.py:339-346, timestepping.py:312-320
+# They are pinned to the NumPy oracle (oracle/numpy_ref.py, itself pinned to
+# the reference's own runs, ghost entries included) by tests/test_oracle.py.
+
+
+def _conv_same(u: torch.Tensor, taps) -> torch.Tensor:
+    """``numpy.convolve(u, taps, mode="same")`` (zero padding) of a 1D tensor,
+    taps ordered ``(i + h, ..., i - h)``."""
+    k = len(taps)
+    h = k // 2
+    m = u.shape[-1]
+    up = torch.nn.functional.pad(u, (h, h))
+    return sum(float(taps[j]) * up[2 * h - j: 2 * h - j + m] for j in range(k) if taps[j] != 0.0)
+
+
+def _weno53_side_ghosted(f: torch.Tensor, eps: float) -> torch.Tensor:
+    from oracle.numpy_ref import weno_js_53_coefficients
+
+    s = weno_js_53_coefficients()
+    beta = [sum(float(s.a[j]) * _conv_same(f, s.b[i, j]) ** 2 for j in range(s.a.size))
+            for i in range(3)]
+    uhat = [_conv_same(f, s.c[i]) for i in range(3)]
+    alpha = [float(s.d[i, 0]) / (eps + beta[i]) ** 2 for i in range(3)]
+    tot = alpha[0] + alpha[1] + alpha[2]
+    return sum((alpha[i] / tot) * uhat[i] for i in range(3))
+
+
+def ghosted_fill(u: torch.Tensor, g: int, bc: dict, stage: int, x: torch.Tensor) -> torch.Tensor:
+    """The boundary's ghost overwrite of a ghosted array (out of place).
+    ``bc``: ``{"left": kind, "right": kind, "dirichlet": [stage][side][k],
+    "neumann": [stage][side]}``, kind in periodic / dirichlet / neumann; *x*:
+    the cell centres (the Neumann mirror distance, scalar.py:494)."""
+    m = u.shape[0]
+    n = m - 2 * g
+    if bc["left"] == "periodic":
+        return torch.cat([u[n:n + g], u[g:g + n], u[g:2 * g]])
+    parts = []
+    for side in (0, 1):
+        kind = bc["left"] if side == 0 else bc["right"]
+        # ghost cells ordered along the array; k = distance from the interior
+        ks = range(g - 1, -1, -1) if side == 0 else range(g)
+        vals = []
+        for k in ks:
+            ito = g - 1 - k if side == 0 else g + n + k
+            if kind == "dirichlet":
+                vals.append(torch.tensor(float(bc["dirichlet"][stage][side][k]), dtype=u.dtype))
+            else:
+                ifrom = g + k if side == 0 else g + n - 1 - k
+                sgn = -1.0 if side == 0 else 1.0
+                vals.append(u[ifrom] + sgn * float(x[ifrom] - x[ito]) * float(bc["neumann"][stage][side]))
+        parts.append(torch.stack(vals) if vals else u[:0])
+    return torch.cat([parts[0], u[g:g + n], parts[1]])
+
+
+def ghosted_operator(u: torch.Tensor, dx: float, g: int, bc: dict, stage: int, x: torch.Tensor, *,
+                     rec: str = "wenojs53", flux_kind: str = "rusanov", eps: float = 1.0e-6,
+                     nu: float = 1.0, equation: str = "burgers") -> torch.Tensor:
+    """``apply_operator`` on every cell of the ghosted array (ghosts included)."""
+    v = ghosted_fill(u, g, bc, stage, x)
+    if rec == "constant":
+        ul = ur = v
+    else:
+        ur = _weno53_side_ghosted(v, eps)
+        ul = torch.flip(_weno53_side_ghosted(torch.flip(v, (0,)), eps), (0,))
+    fl = physical_flux(equation, ul)
+    fr = physical_flux(equation, ur)
+    a = torch.abs(wavespeed(equation, v))
+    a = torch.amax(a) if flux_kind == "lf" else torch.maximum(a[1:], a[:-1])
+    fnum = 0.5 * (fl[1:] + fr[:-1]) - 0.5 * a * nu * (ul[1:] - ur[:-1])
+    f = torch.nn.functional.pad(fnum, (1, 1))
+    return -(f[1:] - f[:-1]) / dx
+
+
+def ghosted_advance(u: torch.Tensor, dt: float, dx: float, g: int, bc: dict, x: torch.Tensor,
+                    **kw) -> torch.Tensor:
+    """SSPRK33 ``advance`` on the raw ghosted array, the boundary at each stage."""
+    k1 = u + dt * ghosted_operator(u, dx, g, bc, 0, x, **kw)
+    k2 = 3.0 / 4.0 * u + 1.0 / 4.0 * (k1 + dt * ghosted_operator(k1, dx, g, bc, 1, x, **kw))
+    return 1.0 / 3.0 * u + 2.0 / 3.0 * (k2 + dt * ghosted_operator(k2, dx, g, bc, 2, x, **kw))
+
+
+def ghosted_step_vjp(u: torch.Tensor, p: torch.Tensor, dt: float, dx: float, g: int, bc: dict,
+                     x: torch.Tensor, **kw) -> torch.Tensor:
+    """``jac.T @ p`` of one ghosted step (timestepping.py:174, 205-206)."""
+    _, fn = torch.func.vjp(lambda v: ghosted_advance(v, dt, dx, g, bc, x, **kw), u)
+    return fn(p)[0]
+
+
+# }}}

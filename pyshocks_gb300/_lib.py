@@ -127,6 +127,13 @@ SIGNATURES: dict[str, tuple] = {
     "shk_plan_adjoint": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _P]),
     "shk_plan_adjoint_stage_bytes": (ctypes.c_int, [_P, ctypes.POINTER(_I64)]),
     "shk_plan_adjoint_staged": (ctypes.c_int, [_P, _P, _I32, _I32, _P, _P, _P, _P, _P]),
+    "shk_ghosted_workspace_bytes": (ctypes.c_int64, [_I64, _I32]),
+    "shk_apply_operator_ghosted_f64": (ctypes.c_int, [_SCH, ctypes.POINTER(ShkBoundary), _P, _P, _I64,
+                                                      _I32, _D, _P, _I64, _P]),
+    "shk_ssprk33_step_ghosted_f64": (ctypes.c_int, [_SCH, ctypes.POINTER(ShkBoundary), _P, _P, _I64,
+                                                    _I32, _D, _D, _P, _I64, _P]),
+    "shk_ssprk33_vjp_ghosted_f64": (ctypes.c_int, [_SCH, ctypes.POINTER(ShkBoundary), _P, _P, _P, _I64,
+                                                   _I32, _D, _D, _P, _I64, _P]),
     "shk_apply_operator_lf_noalloc_f64": (ctypes.c_int, [_SCH, _P, _P, _I64, _I32, _D, _P]),
     "shk_apply_operator_lf_noalloc_max_cells": (ctypes.c_int64, []),
     "shk_mlp_num_params": (ctypes.c_int, []),

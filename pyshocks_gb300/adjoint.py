@@ -116,26 +116,31 @@ def solve(u0: torch.Tensor, checkpointed: CheckpointedSolve, *, t0=None, tfinal=
 def vjp_step(scheme, grid, dt: float, u: torch.Tensor, p_next: torch.Tensor, *,
              bc=None, t: float = 0.0) -> torch.Tensor:
     """``(d advance / d u)^T p_next`` of one SSPRK33 step of a ghosted single
-    instance (``jac.T @ p`` of ``src/pyshocks/timestepping.py:205-206``). With
-    a Dirichlet / Neumann *bc* the step from time *t* is transposed exactly,
-    the boundary data entering as constants."""
+    instance: the ``jac.T @ p`` of ``src/pyshocks/timestepping.py:174,205-206``
+    with ``jac`` the Jacobian of the whole ghosted step (``shk_ssprk33_vjp_ghosted_f64``):
+    ghost entries of *p_next* reach the interior through the operator's ghost
+    rows, as they do in the reference. With a Dirichlet / Neumann *bc* the step
+    from time *t* is transposed exactly, the boundary data entering as
+    constants. Rusanov (any alpha) or global Lax-Friedrichs with the constant
+    or WENO-JS5 reconstruction."""
     for name, arr in (("u", u), ("p", p_next)):
         if not (arr.is_cuda and arr.dtype == torch.float64 and arr.is_contiguous()
                 and arr.shape[0] == grid.x.shape[0]):
             raise ValueError(f"{name}: expected a contiguous float64 CUDA array of {grid.x.shape[0]}")
+    from pyshocks_gb300.burgers import c_boundary, ghosted_workspace
+
     out = torch.empty_like(u)
     cb = None
     if bc is not None:
-        from pyshocks_gb300.burgers import c_boundary
-
         dt_ = float(dt)
         cb = c_boundary(bc, grid, (float(t), float(t) + dt_, float(t) + 0.5 * dt_))
+    ws = ghosted_workspace(grid, u.device)
     L.check(
-        L.lib().shk_ssprk33_vjp_bc_f64(scheme.c_scheme(grid.dx_min),
-                                       None if cb is None else ctypes.byref(cb), u.data_ptr(),
-                                       p_next.data_ptr(), out.data_ptr(), grid.ncells,
-                                       grid.nghosts, float(grid.dx_min), float(dt),
-                                       L.stream_handle()),
-        "ssprk33_vjp",
+        L.lib().shk_ssprk33_vjp_ghosted_f64(scheme.c_scheme(grid.dx_min),
+                                            None if cb is None else ctypes.byref(cb), u.data_ptr(),
+                                            p_next.data_ptr(), out.data_ptr(), grid.ncells,
+                                            grid.nghosts, float(grid.dx_min), float(dt),
+                                            ws.data_ptr(), ws.numel(), L.stream_handle()),
+        "ssprk33_vjp_ghosted",
     )
     return out

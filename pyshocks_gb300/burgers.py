@@ -231,15 +231,23 @@ def c_boundary(bc: Boundary, grid: Grid, times) -> L.ShkBoundary | None:
         return None
     out = L.ShkBoundary()
     g, n = grid.nghosts, grid.ncells
+    h = float(grid.dx_min)
     for side, b in ((0, bc.left), (1, bc.right)):
         kind = L.SHK_BC_DIRICHLET if isinstance(b, DirichletBoundary) else L.SHK_BC_NEUMANN
         if side == 0:
             out.left = kind
-            idx = [g - 1 - k for k in range(3)]
+            idx = [g - 1 - k for k in range(min(g, 3))]
         else:
             out.right = kind
-            idx = [g + n + k for k in range(3)]
-        x = grid.x[torch.tensor(idx, device=grid.x.device)]
+            idx = [g + n + k for k in range(min(g, 3))]
+        x = grid.x[torch.tensor(idx, device=grid.x.device)].double()
+        if g < 3:
+            # cells beyond a grid with fewer than 3 ghosts (their values reach
+            # only ghost outputs): centres continued outward
+            x0 = float(grid.f[g]) if side == 0 else float(grid.f[g + n])
+            sgn = -1.0 if side == 0 else 1.0
+            extra = [x0 + sgn * (k + 0.5) * h for k in range(g, 3)]
+            x = torch.cat([x, torch.tensor(extra, dtype=x.dtype, device=x.device)])
         for s_, ts in enumerate(times):
             if kind == L.SHK_BC_DIRICHLET:
                 vals = torch.as_tensor(b.g(ts, x), dtype=torch.float64).reshape(-1).cpu()
@@ -250,10 +258,28 @@ def c_boundary(bc: Boundary, grid: Grid, times) -> L.ShkBoundary | None:
     return out
 
 
+def ghosted_workspace(grid: Grid, device) -> torch.Tensor:
+    """Device workspace of the ghosted-array entry points
+    (``shk_ghosted_workspace_bytes``; from torch's caching allocator)."""
+    nb = int(L.lib().shk_ghosted_workspace_bytes(grid.ncells, grid.nghosts))
+    return torch.empty(nb, dtype=torch.uint8, device=device)
+
+
+def _ghosted_ok(scheme) -> bool:
+    """Schemes of the ghosted-array kernels: Rusanov / Lax-Friedrichs with the
+    constant or WENO-JS5 reconstruction."""
+    return scheme.flux_code in (L.SHK_FLUX_RUSANOV, L.SHK_FLUX_LF) and getattr(
+        scheme.rec, "code", -1) in (L.SHK_REC_CONSTANT, L.SHK_REC_WENOJS53)
+
+
 @apply_operator.register(GpuConservationLawScheme)
 def _apply_operator_gpu(scheme, grid: Grid, bc: Boundary, t: Any, u: torch.Tensor):
     """``src/pyshocks/schemes.py:339-346`` in one kernel: periodic ghost fill,
-    reconstruction, numerical flux and flux difference."""
+    reconstruction, numerical flux and flux difference. The global
+    Lax-Friedrichs flux (whose wave speed is the maximum over the whole
+    boundary-filled array, ``scalar.py:258-278``) runs on the ghosted-array
+    kernels (``shk_apply_operator_ghosted_f64``), which also give the
+    reference's ghost outputs."""
     _check_bc(bc)
     _check_state(grid, u)
     lib = L.lib()
@@ -262,23 +288,18 @@ def _apply_operator_gpu(scheme, grid: Grid, bc: Boundary, t: Any, u: torch.Tenso
     n = grid.ncells
     out = torch.empty_like(u)
     stream = L.stream_handle()
-    amax = None
-    cb = c_boundary(bc, grid, (float(t),))
-    if scheme.flux_code == L.SHK_FLUX_LF:
-        if cb is None:
-            amax = torch.empty((), dtype=torch.float64, device=u.device)
-            L.check(lib.shk_max_wavespeed_f64(cs, u.data_ptr(), n, g, amax.data_ptr(), stream),
-                    "max_wavespeed")
-        else:
-            # scalar.py:277: the max over the whole array, ghosts filled by the boundary
-            from pyshocks_gb300.schemes import apply_boundary
-
-            ub = apply_boundary(bc, grid, t, u)
-            speed = torch.abs(ub) if scheme.equation_code == L.SHK_EQ_BURGERS else (
-                torch.abs(1 - 2 * ub) if scheme.equation_code == L.SHK_EQ_LWR
-                else torch.full_like(ub, abs(scheme.speed)))
-            amax = speed.max().reshape(())
+    cb = c_boundary(bc, grid, (float(t),) * 3)
     bptr = None if cb is None else ctypes.byref(cb)
+    if scheme.flux_code == L.SHK_FLUX_LF:
+        if not _ghosted_ok(scheme):
+            raise NotImplementedError("global Lax-Friedrichs runs with the constant or WENO-JS5 "
+                                      "reconstruction on the GB300 path")
+        ws = ghosted_workspace(grid, u.device)
+        L.check(lib.shk_apply_operator_ghosted_f64(cs, bptr, u.data_ptr(), out.data_ptr(), n, g,
+                                                   float(grid.dx_min), ws.data_ptr(), ws.numel(),
+                                                   stream), "apply_operator_ghosted")
+        return out
+    amax = None
     L.check(
         lib.shk_apply_operator_bc_f64(cs, bptr, u.data_ptr(), out.data_ptr(), n, g,
                                       float(grid.dx_min), L.ptr(amax), stream),
@@ -310,11 +331,21 @@ def ssprk33_step(scheme, grid: Grid, bc: Boundary, dt: float, u: torch.Tensor,
     the stage times t, t + dt, t + dt/2."""
     _check_bc(bc)
     _check_state(grid, u)
-    if scheme.flux_code == L.SHK_FLUX_LF:
-        raise NotImplementedError("fused step of the global Lax-Friedrichs flux")
     out = torch.empty_like(u)
     dt = float(dt)
     cb = c_boundary(bc, grid, (float(t), float(t) + dt, float(t) + 0.5 * dt))
+    if scheme.flux_code == L.SHK_FLUX_LF:
+        # the per-stage global maximum: the three stages on the ghosted-array
+        # kernels (shk_ssprk33_step_ghosted_f64), no host round trip
+        if not _ghosted_ok(scheme):
+            raise NotImplementedError("global Lax-Friedrichs runs with the constant or WENO-JS5 "
+                                      "reconstruction on the GB300 path")
+        ws = ghosted_workspace(grid, u.device)
+        L.check(L.lib().shk_ssprk33_step_ghosted_f64(
+            scheme.c_scheme(grid.dx_min), None if cb is None else ctypes.byref(cb), u.data_ptr(),
+            out.data_ptr(), grid.ncells, grid.nghosts, float(grid.dx_min), dt, ws.data_ptr(),
+            ws.numel(), L.stream_handle()), "ssprk33_step_ghosted")
+        return out
     L.check(
         L.lib().shk_ssprk33_step_bc_f64(scheme.c_scheme(grid.dx_min),
                                         None if cb is None else ctypes.byref(cb), u.data_ptr(),

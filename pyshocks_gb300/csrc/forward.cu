@@ -424,6 +424,19 @@ shk_boundary periodic_boundary() {
 }
 
 // both sides periodic, or each Dirichlet / Neumann
+// cells a reconstruction reads on each side of a cell (the reference's
+// stencil_width): the single-instance entry points need that many ghosts
+int rec_reach(int rec) {
+    switch (rec) {
+        case SHK_REC_CONSTANT: return 1;
+        case SHK_REC_WENOJS32:
+        case SHK_REC_ESWENO32:
+        case SHK_REC_MUSCL:
+        case SHK_REC_MUSCLS: return 2;
+        default: return 3;
+    }
+}
+
 bool valid_boundary(const shk_boundary& b) {
     auto ok = [](int k) { return k >= SHK_BC_PERIODIC && k <= SHK_BC_NEUMANN; };
     if (!ok(b.left) || !ok(b.right)) return false;
@@ -697,7 +710,8 @@ int shk_max_wavespeed_f64(const shk_scheme* scheme, const double* u, int64_t n, 
 int shk_apply_operator_bc_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
                               double* out, int64_t n, int32_t nghosts, double dx,
                               const double* amax, void* stream) {
-    if (!valid_scheme(scheme) || !u || !out || n < 3 || nghosts < 3 || !(dx > 0)) return SHK_EINVAL;
+    if (!valid_scheme(scheme) || !u || !out || n < 3 || nghosts < rec_reach(scheme->rec) || !(dx > 0))
+        return SHK_EINVAL;
     if (scheme->flux == SHK_FLUX_LF && !amax) return SHK_EINVAL;
     const shk_boundary b = bc ? *bc : periodic_boundary();
     if (!valid_boundary(b)) return SHK_EINVAL;
@@ -731,7 +745,8 @@ int shk_predict_timestep_f64(const shk_scheme* scheme, const double* u, int64_t 
 int shk_ssprk33_step_bc_f64(const shk_scheme* scheme, const shk_boundary* bc, const double* u,
                             double* u_out, int64_t n, int32_t nghosts, double dx, double dt,
                             void* stream) {
-    if (!valid_scheme(scheme) || !u || !u_out || n < 3 || nghosts < 3 || !(dx > 0)) return SHK_EINVAL;
+    if (!valid_scheme(scheme) || !u || !u_out || n < 3 || nghosts < rec_reach(scheme->rec) || !(dx > 0))
+        return SHK_EINVAL;
     if (!std::isfinite(dt)) return SHK_ENONFINITE;
     if (scheme->flux == SHK_FLUX_LF) return SHK_EUNSUPPORTED;  // global max per stage
     const shk_boundary b = bc ? *bc : periodic_boundary();
@@ -1248,15 +1263,19 @@ extern "C" int64_t shk_apply_operator_lf_noalloc_max_cells(void) {
 // ===========================================================================
 #ifdef SHOCKS_BOUNDS_CHECK
 extern "C" int shk_check_tu_adjoint(shk::BoundsLog* out, int32_t reset);
+extern "C" int shk_check_tu_ghosted(shk::BoundsLog* out, int32_t reset);
 
 extern "C" int shk_check_bounds(int32_t reset, int32_t* flag, int32_t* block, int32_t* thread,
                                 int64_t* offset, int64_t* extent) {
     SHK_CUDA(cudaDeviceSynchronize());
-    shk::BoundsLog logs[2] = {};
+    shk::BoundsLog logs[3] = {};
     SHK_CUDA(shk::bounds_log_read(&logs[0], reset != 0));
-    const int r = shk_check_tu_adjoint(&logs[1], reset);
+    int r = shk_check_tu_adjoint(&logs[1], reset);
+    if (r == SHK_OK) r = shk_check_tu_ghosted(&logs[2], reset);
     if (r != SHK_OK) return r;
-    const shk::BoundsLog* hit = logs[0].flag ? &logs[0] : (logs[1].flag ? &logs[1] : nullptr);
+    const shk::BoundsLog* hit = nullptr;
+    for (const shk::BoundsLog& l : logs)
+        if (!hit && l.flag) hit = &l;
     if (flag) *flag = hit ? 1 : 0;
     if (block) *block = hit ? hit->block : -1;
     if (thread) *thread = hit ? hit->thread : -1;

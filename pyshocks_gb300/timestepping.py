@@ -161,14 +161,16 @@ def _advance_forward_euler(stepper, dt, t, u):
 
 @advance.register(SSPRK33)
 def _advance_ssprk33(stepper, dt, t, u):
-    """``src/pyshocks/timestepping.py:312-320``; one fused kernel when the
-    source is an :class:`OperatorSource` of a scheme on the GB300 path."""
+    """``src/pyshocks/timestepping.py:312-320``; one library call when the
+    source is an :class:`OperatorSource` of a scheme on the GB300 path (one
+    fused kernel, or for the global Lax-Friedrichs flux the three stages on the
+    ghosted-array kernels)."""
     src = stepper.source
     if isinstance(src, OperatorSource):
         from pyshocks_gb300 import burgers
 
         if isinstance(src.scheme, burgers.GpuConservationLawScheme) and (
-            src.scheme.flux_code != burgers.L.SHK_FLUX_LF
+            src.scheme.flux_code != burgers.L.SHK_FLUX_LF or burgers._ghosted_ok(src.scheme)
         ):
             return burgers.ssprk33_step(src.scheme, src.grid, src.bc, dt, u, t=float(t))
     fn = src
@@ -207,10 +209,14 @@ def adjoint_step(
     """``src/pyshocks/timestepping.py:155-215``: the reverse sweep over the
     checkpoints saved by :func:`step`, with dt re-read from them (frozen).
 
-    For a stepper built by :func:`make_time_stepper` each transpose step is one
-    matrix-free CUDA kernel (``shk_ssprk33_vjp_f64``) instead of a dense
-    ``jax.jacfwd`` Jacobian. Cotangents live on interior cells (ghost entries of
-    *p0* are ignored and returned as zero)."""
+    For a stepper built by :func:`make_time_stepper` each transpose step is a
+    matrix-free CUDA transpose of the whole ghosted step
+    (``shk_ssprk33_vjp_ghosted_f64``) instead of a dense ``jax.jacfwd``
+    Jacobian, with the reference's semantics: ghost entries of *p* reach the
+    interior through the operator's ghost rows, and ghost entries pass through.
+    Schemes: Rusanov (any alpha) or global Lax-Friedrichs with the constant or
+    WENO-JS5 reconstruction (the reference adjoint driver's ``lf`` scheme with
+    the default reconstruction, ``drivers/burgers-adjoint.py:380-408``)."""
     if stepper.checkpoint is None:
         raise ValueError("Adjoint time stepping requires a checkpoint.")
     src = stepper.source
@@ -218,11 +224,11 @@ def adjoint_step(
     from pyshocks_gb300 import burgers
 
     gpu = isinstance(src, OperatorSource) and isinstance(src.scheme, burgers.GpuConservationLawScheme)
-    fused = gpu and src.scheme.flux_code == burgers.L.SHK_FLUX_RUSANOV and getattr(
-        src.scheme.rec, "code", -1) == burgers.L.SHK_REC_WENOJS53
+    fused = gpu and burgers._ghosted_ok(src.scheme)
     if gpu and not fused:
-        raise NotImplementedError("the matrix-free adjoint covers Rusanov with WENO-JS5 "
-                                  "(single instance) and the learned scheme (batched plans)")
+        raise NotImplementedError("the single-instance adjoint covers Rusanov and Lax-Friedrichs "
+                                  "with the constant or WENO-JS5 reconstruction (batched plans: "
+                                  "Rusanov with WENO-JS5 or the learned reconstruction)")
 
     def _vjp(dt, t, u, p):
         if fused:
@@ -236,7 +242,8 @@ def adjoint_step(
         chk = dict(load(stepper.checkpoint, m))
         if not isinstance(chk["u"], torch.Tensor):
             chk["u"] = torch.as_tensor(chk["u"], device=p0.device)
-        chk["t"] = _as_float(torch.as_tensor(chk["t"]))
+        # float64 either way: a stored float, a 0-d array or a 0-d tensor
+        chk["t"] = _as_float(chk["t"]) if isinstance(chk["t"], torch.Tensor) else float(chk["t"])
         chk["m"] = int(chk["m"])
         return chk
 
@@ -244,11 +251,6 @@ def adjoint_step(
     assert chk["m"] == maxit
     t = tfinal = chk["t"]
     p = p0
-    if fused:
-        g = src.grid.nghosts
-        p = p.clone()
-        p[:g] = 0
-        p[p.shape[0] - g:] = 0
     if apply_boundary is not None:
         p = apply_boundary(chk["t"], chk["u"], p)
     yield AdjointStepCompleted(t=t, tfinal=tfinal, dt=0.0, iteration=maxit, u=chk["u"], p=p)

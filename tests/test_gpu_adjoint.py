@@ -27,6 +27,19 @@ def _scheme(eq="burgers"):
             "advection": burgers.AdvectionRusanov(rec=rec)}[eq]
 
 
+def _interior_vjp(scheme, grid, dt, u, p):
+    """``shk_ssprk33_vjp_f64``: the transpose of one step with cotangents on
+    the interior cells only (the packed-layout convention of the batched
+    adjoint); ghost entries of p are ignored and those of the result are 0."""
+    from pyshocks_gb300 import _lib as L
+
+    out = torch.empty_like(u)
+    L.check(L.lib().shk_ssprk33_vjp_f64(scheme.c_scheme(grid.dx_min), u.data_ptr(), p.data_ptr(),
+                                        out.data_ptr(), grid.ncells, grid.nghosts,
+                                        float(grid.dx_min), float(dt), L.stream_handle()))
+    return out
+
+
 def _state(n, seed, eq):
     og = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
     rng = np.random.default_rng(seed)
@@ -37,7 +50,6 @@ def _state(n, seed, eq):
                                         (3001, "burgers"), (512, "lwr"), (256, "advection")])
 def test_single_step_vjp_matches_autograd(n, eq):
     import pyshocks_gb300 as gb
-    from pyshocks_gb300 import adjoint
 
     u0 = _state(n, n, eq)
     rng = np.random.default_rng(n + 1)
@@ -48,8 +60,8 @@ def test_single_step_vjp_matches_autograd(n, eq):
     ref = T.step_vjp(ut, torch.tensor(p[3:-3])[None], dt, dx, equation=eq)[0].numpy()
 
     grid = gb.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
-    out = adjoint.vjp_step(_scheme(eq), grid, dt, torch.tensor(u0, device="cuda"),
-                           torch.tensor(p, device="cuda")).cpu().numpy()
+    out = _interior_vjp(_scheme(eq), grid, dt, torch.tensor(u0, device="cuda"),
+                        torch.tensor(p, device="cuda")).cpu().numpy()
     err = np.max(np.abs(out[3:-3] - ref)) / np.max(np.abs(ref))
     assert err < 1.0e-11, err
     np.testing.assert_array_equal(out[:3], 0.0)
@@ -63,7 +75,6 @@ def test_vjp_at_ties_splits_the_max_evenly():
     (ties created only in exact arithmetic, e.g. a symmetric +a/-a jump, break
     differently under different roundings and are not a meaningful check)."""
     import pyshocks_gb300 as gb
-    from pyshocks_gb300 import adjoint
 
     n = 128
     u = np.full(n, 0.3)
@@ -75,8 +86,8 @@ def test_vjp_at_ties_splits_the_max_evenly():
     dt = 0.5 * dx / 0.95
     ref = T.step_vjp(torch.tensor(u)[None], torch.tensor(p[3:-3])[None], dt, dx)[0].numpy()
     grid = gb.make_uniform_cell_grid(-1.0, 1.0, n, nghosts=3)
-    out = adjoint.vjp_step(_scheme(), grid, dt, torch.tensor(ug, device="cuda"),
-                           torch.tensor(p, device="cuda")).cpu().numpy()[3:-3]
+    out = _interior_vjp(_scheme(), grid, dt, torch.tensor(ug, device="cuda"),
+                        torch.tensor(p, device="cuda")).cpu().numpy()[3:-3]
     assert np.max(np.abs(out - ref)) / np.max(np.abs(ref)) < 1.0e-11
 
 
@@ -98,7 +109,9 @@ def test_adjoint_step_generator_matches_autograd():
     for ev in gb.timestepping.step(stepper, torch.tensor(u0, device="cuda"), maxit=maxit):
         pass
     uT = ev.u
-    p0 = uT.clone()  # J = 1/2 |u(T)|^2 over the interior
+    p0 = uT.clone()  # J = 1/2 |u(T)|^2 over the interior: no ghost cotangent
+    p0[:3] = 0.0
+    p0[-3:] = 0.0
     dts = []
     for ev in gb.timestepping.adjoint_step(stepper, p0, maxit=maxit):
         if ev.iteration < maxit:

@@ -88,6 +88,8 @@ RERUN = [
     ("test_gpu_learned", "test_learned_adjoint_matches_autograd"),
     ("test_gpu_learned", "test_stored_stage_states_give_the_same_gradient"),
     ("test_gpu_learned", "test_tensor_core_faces_match_oracle"),
+    ("test_gpu_ghosted", "test_ghosted_operator_and_step_match_oracle"),
+    ("test_gpu_ghosted", "test_ghosted_vjp_matches_autograd"),
     ("test_zz_no_alloc", "test_noalloc_matches_regular_path_twice"),
 ]
 

@@ -87,11 +87,13 @@ def test_numpy_oracle_runs_golden(name, flux_kind, equation, kw):
         eps, delta = R.es_weno_parameters(grid, np.ones_like(grid.x))
         assert eps == float(g["eps"]) and delta == float(g["delta"])
     rhs0 = R.apply_operator(spec, grid, g["u0"])
-    np.testing.assert_array_equal(rhs0[3:-3], g["rhs0"][3:-3])
+    # the whole ghosted arrays: the ghost outputs of the operator (zero-padded
+    # convolutions and end fluxes) and the ghost values the steps pass through
+    np.testing.assert_array_equal(rhs0, g["rhs0"])
     assert R.predict_timestep(spec, grid, g["u0"]) == float(g["dt0"])
     u, dts = R.evolve(spec, grid, g["u0"], theta=1.0, **kw)
     np.testing.assert_array_equal(np.array(dts), g["dts"])
-    np.testing.assert_array_equal(u[3:-3], g["u"][3:-3])
+    np.testing.assert_array_equal(u, g["u"])
 
 
 @pytest.mark.parametrize(("name", "flux_kind", "equation", "kw"), RUNS)
@@ -296,10 +298,10 @@ def test_numpy_oracle_boundary_runs_golden(name, flux_kind, rec, kind):
         def bc(t, u):
             return R.apply_boundary_neumann(u, grid, t, neumann_left, neumann_right)
     rhs0 = R.apply_operator(spec, grid, g["u0"], 0.0, bc)
-    np.testing.assert_array_equal(rhs0[3:-3], g["rhs0"][3:-3])
+    np.testing.assert_array_equal(rhs0, g["rhs0"])  # ghost cells included
     u, dts = R.evolve(spec, grid, g["u0"], theta=1.0, maxit=60, bc=bc)
     np.testing.assert_array_equal(np.array(dts), g["dts"])
-    np.testing.assert_array_equal(u[3:-3], g["u"][3:-3])
+    np.testing.assert_array_equal(u, g["u"])
 
 
 # }}}
@@ -360,5 +362,58 @@ def test_flux_limiters(lim, param, smooth):
     else:
         assert np.max(phi[1:-1]) < 1.0e-12
 
+
+# }}}
+
+
+# {{{ the ghosted torch restatement (adjoint_step's oracle) against the NumPy oracle
+
+GHOSTED = [(rec, fk, alpha, kind, g)
+           for rec, g in (("constant", 1), ("constant", 3), ("wenojs53", 3))
+           for fk, alpha in (("rusanov", 1.0), ("rusanov", 0.98), ("lf", 1.0), ("lf", 0.995))
+           for kind in ("periodic", "dirichlet", "neumann")]
+
+
+def _ghosted_case(rec, fk, alpha, kind, g, n=40, seed=3):
+    rng = np.random.default_rng(seed)
+    grid = R.make_uniform_cell_grid(-1.0, 1.0, n, g)
+    dt = 0.4 * grid.dx_min
+    u = R.random_fourier_ic(rng, grid.f)
+    spec = R.SchemeSpec(flux_kind=fk, rec=rec, eps=1.0e-6, alpha=alpha)
+    data = rng.uniform(-1.0, 1.0, size=(3, 2, 3))
+    neu = rng.uniform(-1.0, 1.0, size=(3, 2))
+    tb = {"left": kind, "right": kind, "dirichlet": data, "neumann": neu}
+    times = (0.0, dt, 0.5 * dt)  # SSPRK33's stage times from t = 0
+
+    def bc(t, v):
+        s_ = times.index(t)
+        if kind == "periodic":
+            return R.apply_boundary_periodic(v, g)
+        if kind == "dirichlet":
+            return R.apply_boundary_dirichlet(
+                v, grid, t, lambda tt, x: data[s_, 0, :g][::-1][: x.size],
+                lambda tt, x: data[s_, 1, :g][: x.size])
+        return R.apply_boundary_neumann(v, grid, t, lambda tt: neu[s_, 0], lambda tt: neu[s_, 1])
+
+    return grid, u, spec, tb, bc, times, dt
+
+
+@pytest.mark.parametrize(("rec", "fk", "alpha", "kind", "g"), GHOSTED)
+def test_torch_ghosted_operator_and_step_match_numpy_oracle(rec, fk, alpha, kind, g):
+    """The ghosted restatement used for the single-instance adjoint oracle
+    equals the NumPy oracle on every cell, ghosts included: the operator at
+    the first stage time, and one SSPRK33 step with the boundary at the three
+    stage times (1e-13 relative)."""
+    grid, u, spec, tb, bc, times, dt = _ghosted_case(rec, fk, alpha, kind, g)
+    nu = 1.0 if alpha == 1.0 else grid.dx_min ** (alpha - 1)
+    kw = dict(rec=rec, flux_kind=fk, eps=1.0e-6, nu=nu)
+    x = torch.tensor(grid.x)
+    ref = R.apply_operator(spec, grid, u, times[0], bc)
+    got = T.ghosted_operator(torch.tensor(u), grid.dx_min, g, tb, 0, x, **kw).numpy()
+    scale = np.max(np.abs(ref))
+    assert np.max(np.abs(got - ref)) <= 1.0e-13 * scale
+    ref = R.ssprk33(lambda t, v: R.apply_operator(spec, grid, v, t, bc), dt, times[0], u)
+    got = T.ghosted_advance(torch.tensor(u), dt, grid.dx_min, g, tb, x, **kw).numpy()
+    assert np.max(np.abs(got - ref)) <= 1.0e-13 * np.max(np.abs(ref))
 
 # }}}
