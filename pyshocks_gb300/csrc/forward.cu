@@ -693,7 +693,11 @@ int shk_version(void) { return 1; }
 
 int shk_max_wavespeed_f64(const shk_scheme* scheme, const double* u, int64_t n, int32_t nghosts,
                           double* amax, void* stream) {
-    if (!valid_scheme(scheme) || !u || !amax || n <= 0 || nghosts < 0) return SHK_EINVAL;
+    // only the wave speed of the equation matters here (any flux and
+    // reconstruction, e.g. Lax-Friedrichs with the constant reconstruction)
+    if (!scheme || scheme->equation < SHK_EQ_BURGERS || scheme->equation > SHK_EQ_LWR || !u || !amax ||
+        n <= 0 || nghosts < 0)
+        return SHK_EINVAL;
     cudaStream_t st = as_stream(stream);
     SHK_CUDA(cudaMemsetAsync(amax, 0, sizeof(double), st));
     const int blocks = static_cast<int>(imin64((n + kThreads - 1) / kThreads, 4 * sm_count()));

@@ -98,9 +98,14 @@ def test_apply_operator_matches_oracle(gb, kind, eq, n):
     scale = np.max(np.abs(ref[3:-3]))
     err = np.max(np.abs(out[3:-3] - ref[3:-3])) / scale
     assert err < 1.0e-12, err
-    # ghost cells hold the periodic image of the interior output
-    np.testing.assert_array_equal(out[:3], out[n : n + 3])
-    np.testing.assert_array_equal(out[-3:], out[3:6])
+    if kind == "lf":
+        # global Lax-Friedrichs runs on the ghosted-array kernels, whose ghost
+        # outputs are the reference's (zero-padded end fluxes and stencils)
+        assert np.max(np.abs(out - ref)) <= 1.0e-12 * np.max(np.abs(ref))
+    else:
+        # ghost cells hold the periodic image of the interior output
+        np.testing.assert_array_equal(out[:3], out[n : n + 3])
+        np.testing.assert_array_equal(out[-3:], out[3:6])
 
     dt = gb.predict_timestep(scheme, grid, bc, 0.0, u)
     assert float(dt) == R.predict_timestep(spec, og, u0)
