@@ -146,8 +146,10 @@ class HostStepper:
 class BatchedSolver:
     """Persistent batched SSPRK33 solver for one scheme on periodic domains.
 
-    :arg scheme: a scheme of :mod:`pyshocks_gb300.burgers` (not the global
-        Lax-Friedrichs flux, whose per-stage global maximum forbids fusing).
+    :arg scheme: a scheme of :mod:`pyshocks_gb300.burgers`. The global
+        Lax-Friedrichs flux (WENO-JS5, float64, periodic instances) steps with
+        one launch per stage instead of the fused kernel: its wave speed is the
+        per-stage maximum over the whole instance.
     :arg sizes: number of interior cells of every instance.
     :arg dx: cell size per instance (or a scalar).
     :arg theta: Courant factor of the driver closure ``theta * predict_timestep``.

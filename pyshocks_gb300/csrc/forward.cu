@@ -147,6 +147,128 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
     }
 }
 
+// ---------------------------------------------------------------------------
+// batched global Lax-Friedrichs: one launch per SSPRK33 stage
+// ---------------------------------------------------------------------------
+// The wave speed of the global Lax-Friedrichs flux is the maximum of |f'| over
+// the whole instance, for each stage state (scalar.py:258-278 under
+// timestepping.py:312-320), so the stages cannot be fused with halo
+// recompute. Stage S reads a window of its input k (u, k1 or k2) and u, writes
+// its output (k1, k2 or u+) and accumulates the instance maximum of |f'| of the
+// output for the next stage (amax_out). Stage 1 uses the step's own maximum
+// (amax[cur], which is also the CFL maximum), and every stage evaluates the
+// instance's dt the same way; the last CTA of stage 3 finalises the step as
+// batched_step_kernel does and clears the stage maxima. float64 states,
+// periodic instances, the reference's stage formulas:
+//   k1 = u + dt L(u),  k2 = 3/4 u + 1/4 (k1 + dt L(k1)),  u+ = 1/3 u + 2/3 (k2 + dt L(k2)).
+template <int EQ, int STAGE>
+__global__ void __launch_bounds__(kThreads) batched_lf_stage_kernel(
+    PlanDev P, const double* __restrict__ u, const double* __restrict__ kin, double* __restrict__ kout,
+    const unsigned long long* __restrict__ amax_in, unsigned long long* amax_out,
+    unsigned long long* amax_clear, OpParams<double> p) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ unsigned long long red[32];
+    __shared__ int is_last;
+    __shared__ DtState item_dt;
+    __shared__ double item_dtdx, item_amax;
+    constexpr int HL = op_halo<double>();
+    Smem<double> sm;
+    sm.carve(smem_raw, P.tile + 2 * HL);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    const int64_t k = *reinterpret_cast<volatile int64_t*>(P.step);
+    const int cur = static_cast<int>(k & 1);
+    const int64_t total = P.offsets[P.B];
+    const Win<const double> gu = make_win(u, total);
+    const Win<double> gout = make_win(kout, total);
+    // stage 1 reads the step's own maximum, stage 3 writes the next step's
+    // (the parity of the device step counter picks the slot)
+    const unsigned long long* ain = STAGE == 1 ? P.amax + size_t(cur) * P.B : amax_in;
+    unsigned long long* aout = STAGE == 3 ? P.amax + size_t(cur ^ 1) * P.B : amax_out;
+    bool ok = true;
+    __shared__ int s_item;
+    for (int item = next_item(P, 6, &s_item); item >= 0 && ok; item = next_item(P, 6, &s_item)) {
+        const int b = P.item_inst[item];
+        const int64_t off = P.offsets[b];
+        const int64_t n = P.offsets[b + 1] - off;
+        const int64_t s0 = int64_t(P.item_tile[item]) * P.tile;
+        const int te = static_cast<int>(imin64(P.tile, n - s0));
+        if (threadIdx.x == 0) {
+            const DtState d = plan_dt(P, k, b, from_bits(P.amax[size_t(cur) * P.B + b]));
+            item_dt = d;
+            item_dtdx = d.dt * P.inv_dx[b];
+            item_amax = from_bits(ain[b]);
+        }
+        __syncthreads();
+        const DtState ds = item_dt;
+        unsigned long long mx = 0;
+        if (!(ds.active && ds.finite)) {
+            // instance finished or frozen: every stage state is u
+            for (int i = threadIdx.x; i < te; i += blockDim.x) {
+                const double v = gu[off + s0 + i];
+                gout[off + s0 + i] = v;
+                const unsigned long long bb = abs_bits(wave_speed<EQ>(v, p.c));
+                mx = bb > mx ? bb : mx;
+            }
+        } else {
+            ok = load_window<double>(sm.U, kin + off, n, s0 - HL, te + 2 * HL, &bar, phase);
+            if (!ok) {
+                if (threadIdx.x == 0) atomicOr(P.status, ERR_TIMEOUT);
+                break;
+            }
+            OpParams<double> pb = p;
+            pb.hnu_amax = p.hnu * item_amax;
+            face_fluxes<double, EQ, SHK_REC_WENOJS53, SHK_FLUX_LF>(sm.U, HL, HL + te, sm, pb);
+            const double dtdx = item_dtdx;
+            for (int i = threadIdx.x; i < te; i += blockDim.x) {
+                const int w = HL + i;
+                const double kk = fma(dtdx, sm.D[w - 1] - sm.D[w], sm.U[w]);  // k + dt L(k)
+                double v;
+                if constexpr (STAGE == 1) v = kk;
+                else if constexpr (STAGE == 2) v = fma(1.0 / 4.0, kk, (3.0 / 4.0) * gu[off + s0 + i]);
+                else v = fma(2.0 / 3.0, kk, (1.0 / 3.0) * gu[off + s0 + i]);
+                gout[off + s0 + i] = v;
+                const unsigned long long bb = abs_bits(wave_speed<EQ>(v, p.c));
+                mx = bb > mx ? bb : mx;
+            }
+        }
+        const unsigned long long bm = block_max<unsigned long long>(mx, red);
+        if (threadIdx.x == 0) atomicMax(aout + b, bm);
+        __syncthreads();
+    }
+    if constexpr (STAGE < 3) {
+        finish_items(P, 6);
+    } else {
+        // the last CTA of the step: time, dt history, step counter, and the
+        // stage maxima cleared for the next step
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            const unsigned prev = atomicAdd(P.done, 1u);
+            is_last = (prev == gridDim.x - 1);
+        }
+        __syncthreads();
+        if (is_last) {
+            __threadfence();
+            finalize_step(P, k);
+            for (int i = threadIdx.x; i < 2 * P.B; i += blockDim.x) amax_clear[i] = 0ull;
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                *reinterpret_cast<volatile unsigned*>(P.done) = 0u;
+                atomicExch(P.sched + 6, 0u);
+                atomicExch(P.sched + 7, 0u);
+                *reinterpret_cast<volatile int64_t*>(P.step) = k + 1;
+                __threadfence();
+            }
+        }
+    }
+}
+
 __global__ void fill_kernel(double* x, int n, double v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) x[i] = v;
@@ -567,13 +689,40 @@ struct BatchedStepLaunch {
     }
 };
 
+// one global Lax-Friedrichs step of a plan: the three stage launches
+struct BatchedLfLaunch {
+    PlanDev D; const double* uin; double* uout; double* k1; double* k2; unsigned long long* amax_lf;
+    OpParams<double> p; size_t smem; int grid; cudaStream_t st;
+    template <int EQ> int run() {
+        auto s1 = batched_lf_stage_kernel<EQ, 1>;
+        auto s2 = batched_lf_stage_kernel<EQ, 2>;
+        auto s3 = batched_lf_stage_kernel<EQ, 3>;
+        for (auto k : {s1, s2, s3})
+            SHK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int B = D.B;
+        s1<<<grid, kThreads, smem, st>>>(D, uin, uin, k1, nullptr, amax_lf, amax_lf, p);
+        SHK_CUDA(cudaGetLastError());
+        s2<<<grid, kThreads, smem, st>>>(D, uin, k1, k2, amax_lf, amax_lf + B, amax_lf, p);
+        SHK_CUDA(cudaGetLastError());
+        s3<<<grid, kThreads, smem, st>>>(D, uin, k2, uout, amax_lf + B, nullptr, amax_lf, p);
+        return cuda_check(cudaGetLastError());
+    }
+};
+
 // resident CTAs per SM of the step kernel a scheme dispatches to, at the
 // given dynamic shared memory (registers and shared memory both counted)
 struct StepOccupancy {
     size_t smem; int* out;
     template <class T, int EQ, int REC, int FLUX> int operator()() {
         if constexpr (FLUX == SHK_FLUX_LF) {
-            return SHK_EUNSUPPORTED;
+            if constexpr (sizeof(T) != 8) {
+                return SHK_EUNSUPPORTED;
+            } else {
+                auto k = batched_lf_stage_kernel<EQ, 2>;
+                SHK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                SHK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, k, kThreads, smem));
+                return SHK_OK;
+            }
         } else {
             auto k = batched_step_kernel<T, EQ, REC, FLUX>;
             SHK_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -617,6 +766,10 @@ struct shk_plan {
     unsigned int* sched = nullptr;  // [8] scheduling counters
     // host mirror of the number of steps launched since reset
     int64_t host_steps = 0;
+    // global Lax-Friedrichs plans: stage states k1, k2 and their maxima [2][B]
+    double* lf_k1 = nullptr;
+    double* lf_k2 = nullptr;
+    unsigned long long* amax_lf = nullptr;
     // captured two-step graph
     cudaGraphExec_t graph = nullptr;
     void* graph_a = nullptr;
@@ -652,6 +805,20 @@ int launch_max(shk_plan* P, const void* u, int slot, cudaStream_t st) {
 template <class T>
 int launch_step(shk_plan* P, const void* uin, void* uout, cudaStream_t st) {
     const PlanDev D = P->dev();
+    if (P->scheme.flux == SHK_FLUX_LF) {
+        if constexpr (sizeof(T) != 8) {
+            return SHK_EUNSUPPORTED;
+        } else {
+            const size_t smem = Smem<double>::host_bytes(P->tile + 2 * op_halo<double>());
+            BatchedLfLaunch f{D, static_cast<const double*>(uin), static_cast<double*>(uout), P->lf_k1,
+                              P->lf_k2, P->amax_lf, make_params<double>(&P->scheme), smem, P->grid, st};
+            switch (P->scheme.equation) {
+                case SHK_EQ_BURGERS: return f.run<SHK_EQ_BURGERS>();
+                case SHK_EQ_ADVECTION: return f.run<SHK_EQ_ADVECTION>();
+                default: return f.run<SHK_EQ_LWR>();
+            }
+        }
+    }
     const size_t smem = Smem<T>::step_bytes(P->tile + 2 * step_halo<T>(), P->scheme.rec);
     OpParams<T> p = make_params<T>(&P->scheme);
     BatchedStepLaunch<T> f{D, static_cast<const T*>(uin), static_cast<T*>(uout), p, smem, P->grid, st};
@@ -783,7 +950,8 @@ int shk_plan_destroy(shk_plan* plan) {
     void* ptrs[] = {plan->item_inst, plan->item_tile, plan->item_first, plan->offsets, plan->cfl,
                     plan->inv_dx, plan->tfinal, plan->amax, plan->t, plan->dt_hist, plan->step,
                     plan->done, plan->status, plan->partial, plan->dt_fixed, plan->bc_dir,
-                    plan->bc_neu, plan->item_order, plan->sched};
+                    plan->bc_neu, plan->item_order, plan->sched, plan->lf_k1, plan->lf_k2,
+                    plan->amax_lf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete plan;
@@ -796,9 +964,11 @@ int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_of
     if (!out) return SHK_EINVAL;
     *out = nullptr;
     if (!valid_scheme(scheme) || batch <= 0 || !h_offsets || !h_dx || !h_cfl) return SHK_EINVAL;
-    if (scheme->flux == SHK_FLUX_LF) return SHK_EUNSUPPORTED;
     const int dtype = opts ? opts->dtype : SHK_F64;
     if (dtype != SHK_F64 && dtype != SHK_F32) return SHK_EINVAL;
+    // global Lax-Friedrichs: float64 stage states kept between the stage launches
+    const bool lf = scheme->flux == SHK_FLUX_LF;
+    if (lf && dtype != SHK_F64) return SHK_EUNSUPPORTED;
     int tile = (opts && opts->tile > 0) ? opts->tile : default_tile(scheme, dtype, opts ? opts->max_steps : 0);
     const int align = dtype == SHK_F64 ? 2 : 4;
     if (tile % align || tile < 16 || tile > 8192) return SHK_EINVAL;
@@ -855,6 +1025,11 @@ int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_of
               alloc((void**)&P->sched, sizeof(unsigned) * 8);
     if (ok && P->max_steps > 0)
         ok = alloc((void**)&P->dt_hist, sizeof(double) * size_t(P->max_steps) * batch);
+    if (ok && lf)
+        ok = alloc((void**)&P->lf_k1, sizeof(double) * size_t(P->total_cells)) &&
+             alloc((void**)&P->lf_k2, sizeof(double) * size_t(P->total_cells)) &&
+             alloc((void**)&P->amax_lf, sizeof(unsigned long long) * 2 * batch) &&
+             cudaMemset(P->amax_lf, 0, sizeof(unsigned long long) * 2 * batch) == cudaSuccess;
     if (!ok) {
         shk_plan_destroy(P);
         return SHK_ENOMEM;
@@ -880,8 +1055,9 @@ int shk_plan_create(const shk_scheme* scheme, int32_t batch, const int64_t* h_of
     // persistent grid: resident CTAs per SM x SMs
     int per_sm = opts && opts->ctas_per_sm > 0 ? opts->ctas_per_sm : 0;
     if (per_sm == 0) {
-        const size_t smem = dtype == SHK_F64 ? Smem<double>::step_bytes(tile + 2 * step_halo<double>(), scheme->rec)
-                                             : Smem<float>::step_bytes(tile + 2 * step_halo<float>(), scheme->rec);
+        const size_t smem = lf ? Smem<double>::host_bytes(tile + 2 * op_halo<double>())
+                               : (dtype == SHK_F64 ? Smem<double>::step_bytes(tile + 2 * step_halo<double>(), scheme->rec)
+                                                   : Smem<float>::step_bytes(tile + 2 * step_halo<float>(), scheme->rec));
         int resident = 0;
         const int r = dtype == SHK_F64 ? dispatch_scheme<double>(scheme, StepOccupancy{smem, &resident})
                                        : dispatch_scheme<float>(scheme, StepOccupancy{smem, &resident});
@@ -939,6 +1115,7 @@ int shk_plan_reset(shk_plan* plan, const void* u, const double* t0, const double
     cudaStream_t st = as_stream(stream);
     const int B = plan->B;
     SHK_CUDA(cudaMemsetAsync(plan->amax, 0, sizeof(unsigned long long) * 2 * B, st));
+    if (plan->amax_lf) SHK_CUDA(cudaMemsetAsync(plan->amax_lf, 0, sizeof(unsigned long long) * 2 * B, st));
     SHK_CUDA(cudaMemsetAsync(plan->step, 0, sizeof(int64_t), st));
     SHK_CUDA(cudaMemsetAsync(plan->done, 0, sizeof(unsigned), st));
     SHK_CUDA(cudaMemsetAsync(plan->sched, 0, sizeof(unsigned) * 8, st));
@@ -1009,6 +1186,8 @@ int set_plan_boundary(shk_plan* plan, int32_t left, int32_t right, const double*
     b.left = left;
     b.right = right;
     if (!valid_boundary(b)) return SHK_EINVAL;
+    // the global Lax-Friedrichs speed would also span the ghost values
+    if (plan->scheme.flux == SHK_FLUX_LF && left != SHK_BC_PERIODIC) return SHK_EUNSUPPORTED;
     const bool need_dir = left == SHK_BC_DIRICHLET || right == SHK_BC_DIRICHLET;
     const bool need_neu = left == SHK_BC_NEUMANN || right == SHK_BC_NEUMANN;
     if ((need_dir && !dirichlet) || (need_neu && !neumann)) return SHK_EINVAL;

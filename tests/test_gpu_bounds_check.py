@@ -76,6 +76,7 @@ RERUN = [
     ("test_gpu_forward", "test_fused_step_matches_oracle"),
     ("test_gpu_forward", "test_batched_uneven_matches_oracle"),
     ("test_gpu_forward", "test_host_stepper_equals_device_plan"),
+    ("test_gpu_forward", "test_batched_lax_friedrichs_matches_oracle"),
     ("test_gpu_boundary", "test_apply_operator_with_boundary_matches_oracle"),
     ("test_gpu_boundary", "test_batched_plan_with_boundary_matches_oracle"),
     ("test_gpu_boundary", "test_batched_adjoint_with_boundary_against_finite_differences"),

@@ -577,3 +577,39 @@ def test_norms_match_oracle(gb, dtype):
                 got = float(solver.norm(p, weighted=w)[b])
                 assert abs(got - ref) <= tol * abs(ref), (n, p, w)
         assert abs(float(solver.reduce(0)[b]) - float(np.sum(ur))) <= tol * float(np.sum(np.abs(ur)))
+
+
+@pytest.mark.parametrize("tile", [0, 64])
+def test_batched_lax_friedrichs_matches_oracle(gb, tile):
+    """Global Lax-Friedrichs in a batched plan (``src/pyshocks/scalar.py:258-278``:
+    the wave speed is each stage state's maximum over the whole instance; one
+    launch per stage): uneven and ragged instances, 25 fixed-count steps,
+    against the oracle's LF runs (1e-11 relative, dt history 1e-12)."""
+    from pyshocks_gb300.batched import BatchedSolver
+
+    sizes = [64, 50, 7, 1024, 333, 2048, 96]
+    nsteps = 25
+    u0s, refs, dts_ref = [], [], []
+    for b, n in enumerate(sizes):
+        og = R.make_uniform_cell_grid(-1.0, 1.0, n, 3)
+        u0 = R.random_fourier_ic(np.random.default_rng(300 + b), og.f)
+        u, dts = R.evolve(R.SchemeSpec(flux_kind="lf"), og, u0, theta=0.8, maxit=nsteps)
+        u0s.append(u0[3:-3])
+        refs.append(u[3:-3])
+        dts_ref.append(dts)
+    solver = BatchedSolver(_scheme(gb, "lf"), sizes, [2.0 / n for n in sizes], theta=0.8,
+                           tile=tile, max_steps=nsteps)
+    solver.reset(torch.tensor(np.concatenate(u0s)))
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        solver.step(nsteps - 5, graph=True)  # the three-launch step in the captured graph too
+        solver.step(5)
+    stream.synchronize()
+    hist = solver.dt_history().cpu().numpy()
+    for b, n in enumerate(sizes):
+        u = solver.instance(b).cpu().numpy()
+        err = np.max(np.abs(u - refs[b])) / max(1.0, np.max(np.abs(refs[b])))
+        assert err < 1.0e-11, (b, n, err)
+        rel = np.max(np.abs(hist[:, b] - dts_ref[b]) / np.array(dts_ref[b]))
+        assert rel < 1.0e-12, (b, rel)
+    assert solver.status() == 0

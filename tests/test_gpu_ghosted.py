@@ -138,15 +138,30 @@ def _tophat(grid_a, grid_b, t, x):
     return us * h_l + (x - xa) / (t + 1.0e-15) * h_e + uc * h_c + us * h_r
 
 
-def test_reference_adjoint_driver_end_to_end():
+@pytest.mark.parametrize("ic", ["tophat", "smooth"])
+def test_reference_adjoint_driver_end_to_end(ic):
     """``drivers/burgers-adjoint.py`` (its defaults: n = 256 on [-1.5, 1.5],
     t_final = 0.75, theta = 1, ``lf`` with alpha = 0.995 and the default
-    constant reconstruction, so one ghost cell): cell averages of the top hat by
-    2-point Gauss-Legendre, Dirichlet data from the exact solution, ``step`` to
-    t_final with in-memory checkpoints, then ``adjoint_step`` from p0 = u(T)
-    with the homogeneous Neumann adjoint boundary applied to p after each
-    step. Compared with the same loop on the ghosted torch restatement
-    (torch.func.vjp per step, the GPU's dt sequence)."""
+    constant reconstruction, so one ghost cell; Dirichlet forward boundary),
+    ``step`` to t_final with in-memory checkpoints, then ``adjoint_step`` from
+    p0 = u(T) with the homogeneous Neumann adjoint boundary applied to p after
+    each step. Compared with the same loop on the ghosted torch restatement
+    (torch.func.vjp per step, at the GPU's checkpointed states and dt).
+
+    ``tophat``: the driver's own initial state (cell averages of the top hat by
+    2-point Gauss-Legendre, Dirichlet data from the exact solution). Its
+    maximum |u| = 1 is attained on a whole plateau, so the Lax-Friedrichs
+    speed's cotangent is split among the tied cells, and whether a cell at the
+    plateau's edge rounds to exactly 1 in the recomputed stage states depends
+    on the arithmetic's rounding (the reference's XLA order has its own).
+    The tie count then differs by a cell here and there: a few entries move by
+    up to ~1e-4, the rest agree to round-off. Bar: 1e-3 of the range in
+    max-abs, 1e-6 in the mean.
+
+    ``smooth``: the same pipeline from a smooth state with a single maximum
+    (constant Dirichlet data): 1e-9 relative. There the ghost rows matter: the
+    interior-only transpose (ghost cotangents dropped before each step) is off
+    by O(1), and the GPU result must be far from it."""
     import pyshocks_gb300 as gb
     from pyshocks_gb300 import burgers, reconstruction, scalar
     from pyshocks_gb300.checkpointing import InMemoryCheckpoint
@@ -157,9 +172,24 @@ def test_reference_adjoint_driver_end_to_end():
     scheme = burgers.make_scheme_from_name("lf", rec=rec, alpha=0.995)
     assert rec.stencil_width == 1
     grid = gb.make_uniform_cell_grid(a=a, b=b, n=n, nghosts=scheme.stencil_width)
-    quad = make_leggauss_quadrature(grid, order=int(max(scheme.order, 1)) + 1)
-    u0 = cell_average(quad, lambda x: _tophat(a, b, 0.0, x), like=grid.x)
-    bc = scalar.make_dirichlet_boundary(ga=lambda t, x: _tophat(a, b, t, x))
+    g = grid.nghosts
+    x = grid.x.double().cpu()
+    if ic == "tophat":
+        quad = make_leggauss_quadrature(grid, order=int(max(scheme.order, 1)) + 1)
+        u0 = cell_average(quad, lambda xx: _tophat(a, b, 0.0, xx), like=grid.x)
+
+        def gfun(t, xx):
+            return _tophat(a, b, t, xx)
+    else:
+        u0 = (0.5 + 0.4 * torch.sin(np.pi * grid.x / 1.5)
+              + 0.1 * torch.cos(2 * np.pi * grid.x / 1.5)).double().contiguous()
+        vl, vr = float(u0[0]), float(u0[-1])
+
+        def gfun(t, xx):
+            out = torch.full_like(torch.as_tensor(xx, dtype=torch.float64), vl)
+            out[torch.as_tensor(xx) > 0] = vr
+            return out
+    bc = scalar.make_dirichlet_boundary(ga=gfun)
     scheme = gb.bind(scheme, grid, bc)
     stepper = gb.timestepping.make_time_stepper(scheme, grid, bc, theta=1.0,
                                                 checkpoint=InMemoryCheckpoint("Iteration"))
@@ -180,8 +210,6 @@ def test_reference_adjoint_driver_end_to_end():
     got = ev.p.cpu().numpy()
 
     # the same loop on the ghosted restatement (CPU, float64)
-    g = grid.nghosts
-    x = grid.x.double().cpu()
     xg = x[torch.tensor([0, g + n])]
     nu = grid.dx_min ** (0.995 - 1)
     # checkpoint times as step() accumulates them; the adjoint's dt is their
@@ -195,7 +223,7 @@ def test_reference_adjoint_driver_end_to_end():
     def table(t0, dt):
         d = np.zeros((3, 2, 3))
         for s_, ts in enumerate((t0, t0 + dt, t0 + 0.5 * dt)):
-            v = _tophat(a, b, ts, xg)
+            v = gfun(ts, xg)
             d[s_, 0, 0], d[s_, 1, 0] = float(v[0]), float(v[1])
         return {"left": "dirichlet", "right": "dirichlet", "dirichlet": d,
                 "neumann": np.zeros((3, 2))}
@@ -206,12 +234,26 @@ def test_reference_adjoint_driver_end_to_end():
         p[p.shape[0] - g:] = p[p.shape[0] - 2 * g:p.shape[0] - g].flip(0)
         return p
 
-    p = neumann0(uf.double().cpu())
-    for m in range(maxit - 1, -1, -1):
-        dt = times[m + 1] - times[m]
-        p = T.ghosted_step_vjp(states[m].double().cpu(), p, dt, grid.dx_min, g,
-                               table(times[m], dt), x, rec="constant", flux_kind="lf", nu=nu)
-        p = neumann0(p)
-    ref = p.numpy()
-    assert np.max(np.abs(got - ref)) <= 1.0e-9 * np.max(np.abs(ref)), np.max(np.abs(got - ref))
-    assert np.max(np.abs(ref)) > 0.1
+    def sweep(interior_only):
+        p = neumann0(uf.double().cpu())
+        for m in range(maxit - 1, -1, -1):
+            dt = times[m + 1] - times[m]
+            if interior_only:
+                p = p.clone()
+                p[:g] = 0.0
+                p[p.shape[0] - g:] = 0.0
+            p = T.ghosted_step_vjp(states[m].double().cpu(), p, dt, grid.dx_min, g,
+                                   table(times[m], dt), x, rec="constant", flux_kind="lf", nu=nu)
+            p = neumann0(p)
+        return p.numpy()
+
+    ref = sweep(False)
+    scale = np.max(np.abs(ref))
+    assert scale > 0.1
+    d = np.abs(got - ref)
+    if ic == "tophat":
+        assert np.max(d) <= 1.0e-3 * scale, np.max(d)
+        assert np.mean(d) <= 1.0e-6 * scale, np.mean(d)
+    else:
+        assert np.max(d) <= 1.0e-9 * scale, np.max(d)
+        assert np.max(np.abs(got - sweep(True))) > 0.1 * scale
