@@ -570,6 +570,72 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, Win<double
     return mx;
 }
 
+// Float state, WENO-JS5 + Rusanov: each stage in one pass over the window. A
+// warp takes 30 consecutive output cells cb .. cb+29; its 32 lanes
+// reconstruct cells cb-1 .. cb+30 (weno53_cell_f from the five window values),
+// the left face value and the cell value of the right neighbour come from the
+// lane above by shuffle, each lane forms the flux of its right face, and the
+// flux of its left face comes from the lane below. Lanes 1 .. 30 update their
+// cell. One barrier per stage (the staged face-value and flux arrays of the
+// three-pass stage took three), the same operations in the same order, so the
+// same results bit for bit; 32 reconstructions serve 30 cells. The stages
+// ping-pong between S (k1) and UL (k2), since a warp's output cells are other
+// warps' stencil inputs.
+template <int EQ>
+__device__ unsigned int step_tile_f32_weno(const Smem<float>& sm, Win<float> gout, int te, float dtdx,
+                                           const OpParams<float>& p, const BcView& bc, int64_t g0,
+                                           int64_t n, const StageOut<float>& so) {
+    constexpr int HL = step_halo<float>();
+    constexpr unsigned kFull = 0xffffffffu;
+    const bool np = !bc.periodic();
+    if (np) apply_bc(sm.U, g0, n, 0, te + 2 * HL, bc, 0);
+    dtdx *= p.fscale;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const float eps4 = 4.0f * p.eps;
+    const Win<float> K2 = sm.UL;
+    unsigned int mx = 0;
+    // stage s reads v on [lo-3, hi+3) and updates [lo, hi)
+    auto stage = [&](const Win<float>& v, int lo, int hi, int s) {
+        for (int cb = lo + 30 * warp; cb < hi; cb += 30 * nw) {
+            const int c = cb - 1 + lane;
+            const int cc = c < hi ? c : hi;  // cells past hi only feed unused faces
+            const float vm2 = v[cc - 2], vm1 = v[cc - 1], v0 = v[cc], vp1 = v[cc + 1], vp2 = v[cc + 2];
+            float ul, ur;
+            weno53_cell_f(v0, vm1 - vm2, v0 - vm1, vp1 - v0, vp2 - vp1, eps4, ul, ur);
+            const float uln = __shfl_down_sync(kFull, ul, 1);
+            const float vn = __shfl_down_sync(kFull, v0, 1);
+            const float f = rusanov_face<EQ, float>(ur, uln, v0, vn, p.hnu, p.c);  // face c + 1/2
+            const float fl = __shfl_up_sync(kFull, f, 1);                        // face c - 1/2
+            if (lane >= 1 && lane <= 30 && c < hi) {
+                if (s == 1) {
+                    const float d = dtdx * (fl - f);
+                    sm.I[c] = d;
+                    sm.S[c] = sm.U[c] + d;
+                } else if (s == 2) {
+                    const float d = 0.25f * (sm.I[c] + dtdx * (fl - f));
+                    sm.I[c] = d;
+                    K2[c] = sm.U[c] + d;
+                } else {
+                    const float un = sm.U[c] + (2.0f / 3.0f) * (sm.I[c] + dtdx * (fl - f));
+                    gout[c - HL] = un;
+                    const unsigned int b = abs_bits(wave_speed<EQ>(un, p.c));
+                    mx = b > mx ? b : mx;
+                }
+            }
+        }
+        __syncthreads();
+    };
+    stage(sm.U, HL - 6, HL + te + 6, 1);
+    if (np) apply_bc(sm.S, g0, n, HL - 6, HL + te + 6, bc, 1);
+    store_interior(so.k1, sm.S, HL, te);
+    stage(sm.S, HL - 3, HL + te + 3, 2);
+    if (np) apply_bc(K2, g0, n, HL - 3, HL + te + 3, bc, 2);
+    store_interior(so.k2, K2, HL, te);
+    if (!gout) return mx;
+    stage(K2, HL, HL + te, 3);
+    return mx;
+}
+
 // g0: global cell of window position 0 (s - HL); n: cells of the instance;
 // bc: its boundary (periodic: nothing to overwrite)
 // so: what the reverse sweep keeps of this step (StageOut); gout may then be
@@ -581,6 +647,8 @@ __device__ typename Bits<T>::type step_tile(const Smem<T>& sm, Win<T> gout, int 
                                             const StageOut<stage_t<T, REC>>& so = StageOut<stage_t<T, REC>>()) {
     if constexpr (sizeof(T) == 8 && REC == SHK_REC_LEARNED)
         return step_tile_mixed<EQ, FLUX>(sm, gout, te, dtdx, p, bc, g0, n, so);
+    if constexpr (sizeof(T) == 4 && REC == SHK_REC_WENOJS53 && FLUX == SHK_FLUX_RUSANOV)
+        return step_tile_f32_weno<EQ>(sm, gout, te, dtdx, p, bc, g0, n, so);
     constexpr int HL = step_halo<T>();
     const int tid = threadIdx.x, nt = blockDim.x;
     const bool np = !bc.periodic();
