@@ -203,15 +203,19 @@ def test_autograd_function_backward():
     assert float(err) < 1.0e-9
 
 
-def test_n4096_gradient_16_directions():
+@pytest.mark.parametrize(("nsteps", "tol"), [(400, 1.0e-5), (4000, 1.0e-4)])
+def test_n4096_gradient_16_directions(nsteps, tol):
     """The adjoint benchmark's check at its instance size (N = 4096): dJ/du0
     along 16 random directions against central differences (h = 1e-6) of the
     GPU forward itself, replaying the recorded dt sequence (frozen dt, as
-    adjoint_step), with J = 1/2 |u(T) - u_target|^2 and sqrt(n) checkpoints."""
+    adjoint_step), with J = 1/2 |u(T) - u_target|^2 and sqrt(n) checkpoints;
+    400 steps (before the shock forms) and the configuration's 4000 (t ~ 0.65,
+    past it, where a perturbation of h can cross a kink of the Rusanov speed
+    max(|u_j|, |u_j+1|) and the central difference sees it)."""
     from pyshocks_gb300.adjoint import CheckpointedSolve
     from pyshocks_gb300.batched import BatchedSolver
 
-    n, nsteps, B = 4096, 400, 2
+    n, B = 4096, 2
     rng = np.random.default_rng(31)
     u1 = R.exact_cell_average_sine(R.make_uniform_cell_grid(-1, 1, n, 3))[3:-3]
     u0 = np.tile(u1, B)
@@ -233,11 +237,14 @@ def test_n4096_gradient_16_directions():
         return 0.5 * float(torch.sum((replay.u - target) ** 2))
 
     h = 1.0e-6
+    worst = 0.0
     for k in range(16):
         v = rng.standard_normal(u0.size)
         fd = (J(u0 + h * v) - J(u0 - h * v)) / (2 * h)
         ad = float(np.dot(grad, v))
-        assert abs(fd - ad) <= 1.0e-5 * max(1.0, abs(ad)), (k, fd, ad)
+        worst = max(worst, abs(fd - ad) / max(1.0, abs(ad)))
+        assert abs(fd - ad) <= tol * max(1.0, abs(ad)), (k, fd, ad)
+    print(f"N=4096, {nsteps} steps: worst |fd - ad| / max(1, |ad|) over 16 directions {worst:.2e}")
 
 
 @pytest.mark.parametrize("boundary", ["periodic", "neumann"])
