@@ -265,7 +265,7 @@ def ghosted_workspace(grid: Grid, device) -> torch.Tensor:
     return torch.empty(nb, dtype=torch.uint8, device=device)
 
 
-def _ghosted_ok(scheme) -> bool:
+def ghosted_supported(scheme) -> bool:
     """Schemes of the ghosted-array kernels: Rusanov / Lax-Friedrichs with the
     constant or WENO-JS5 reconstruction."""
     return scheme.flux_code in (L.SHK_FLUX_RUSANOV, L.SHK_FLUX_LF) and getattr(
@@ -291,7 +291,7 @@ def _apply_operator_gpu(scheme, grid: Grid, bc: Boundary, t: Any, u: torch.Tenso
     cb = c_boundary(bc, grid, (float(t),) * 3)
     bptr = None if cb is None else ctypes.byref(cb)
     if scheme.flux_code == L.SHK_FLUX_LF:
-        if not _ghosted_ok(scheme):
+        if not ghosted_supported(scheme):
             raise NotImplementedError("global Lax-Friedrichs runs with the constant or WENO-JS5 "
                                       "reconstruction on the GB300 path")
         ws = ghosted_workspace(grid, u.device)
@@ -337,7 +337,7 @@ def ssprk33_step(scheme, grid: Grid, bc: Boundary, dt: float, u: torch.Tensor,
     if scheme.flux_code == L.SHK_FLUX_LF:
         # the per-stage global maximum: the three stages on the ghosted-array
         # kernels (shk_ssprk33_step_ghosted_f64), no host round trip
-        if not _ghosted_ok(scheme):
+        if not ghosted_supported(scheme):
             raise NotImplementedError("global Lax-Friedrichs runs with the constant or WENO-JS5 "
                                       "reconstruction on the GB300 path")
         ws = ghosted_workspace(grid, u.device)

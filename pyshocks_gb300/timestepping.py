@@ -170,7 +170,7 @@ def _advance_ssprk33(stepper, dt, t, u):
         from pyshocks_gb300 import burgers
 
         if isinstance(src.scheme, burgers.GpuConservationLawScheme) and (
-            src.scheme.flux_code != burgers.L.SHK_FLUX_LF or burgers._ghosted_ok(src.scheme)
+            src.scheme.flux_code != burgers.L.SHK_FLUX_LF or burgers.ghosted_supported(src.scheme)
         ):
             return burgers.ssprk33_step(src.scheme, src.grid, src.bc, dt, u, t=float(t))
     fn = src
@@ -224,7 +224,7 @@ def adjoint_step(
     from pyshocks_gb300 import burgers
 
     gpu = isinstance(src, OperatorSource) and isinstance(src.scheme, burgers.GpuConservationLawScheme)
-    fused = gpu and burgers._ghosted_ok(src.scheme)
+    fused = gpu and burgers.ghosted_supported(src.scheme)
     if gpu and not fused:
         raise NotImplementedError("the single-instance adjoint covers Rusanov and Lax-Friedrichs "
                                   "with the constant or WENO-JS5 reconstruction (batched plans: "

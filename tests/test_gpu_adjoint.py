@@ -203,7 +203,7 @@ def test_autograd_function_backward():
     assert float(err) < 1.0e-9
 
 
-@pytest.mark.parametrize(("nsteps", "tol"), [(400, 1.0e-5), (4000, 1.0e-4)])
+@pytest.mark.parametrize(("nsteps", "tol"), [(400, 1.0e-5), (4000, 2.0e-5)])
 def test_n4096_gradient_16_directions(nsteps, tol):
     """The adjoint benchmark's check at its instance size (N = 4096): dJ/du0
     along 16 random directions against central differences (h = 1e-6) of the
@@ -211,7 +211,8 @@ def test_n4096_gradient_16_directions(nsteps, tol):
     adjoint_step), with J = 1/2 |u(T) - u_target|^2 and sqrt(n) checkpoints;
     400 steps (before the shock forms) and the configuration's 4000 (t ~ 0.65,
     past it, where a perturbation of h can cross a kink of the Rusanov speed
-    max(|u_j|, |u_j+1|) and the central difference sees it)."""
+    max(|u_j|, |u_j+1|) and the central difference sees it; measured worst
+    relative mismatch 4e-8 at 400 steps, 3.4e-6 at 4000)."""
     from pyshocks_gb300.adjoint import CheckpointedSolve
     from pyshocks_gb300.batched import BatchedSolver
 
