@@ -64,6 +64,9 @@ struct AdjSmem {
         Smem<T> s;
         s.U = U; s.S = state_out; s.H = H; s.D = D; s.Q = Q;
         s.UL = ul ? ul : UL; s.UR = ur ? ur : UR;
+        // the learned phase's scratch: H and D (contiguous in both layouts)
+        const int hd = 2 * W * int(sizeof(T) / sizeof(float));
+        s.scr = learned_scratch(make_win(reinterpret_cast<float*>(win_raw(H)), hd), hd);
         s.W = W;
         return s;
     }
@@ -86,10 +89,8 @@ __device__ void vjp_stage(PV v, PW w, PZ z, int lo, int hi, const AdjSmem<T>& a,
         //   gR_j = fb_j (f'(R)/2 + a_j), and cell j+1 with gL = fb_j (f'(L)/2 - a_j),
         // fb_j = dt/dx (w_{j+1} - w_j), a_j = nu/2 max(|f'(v_j)|, |f'(v_{j+1})|).
         // The face values are kept for the wave-speed terms below.
-        MlpFrags f;
-        mlp_load_frags(p.lp.mlp, f);
-        MlpBackFrags bk;
-        mlp_load_back_frags(p.lp.mlp, bk);
+        const MlpShared& ms = mlp_shared();
+        const MlpBackShared& bk = mlp_back_shared();
         // warp scratch: GL, GR, GA (3W floats, unused by this branch)
         float* scr = win_span(learned_scratch(a.GL, 3 * a.W), (tid >> 5) * kWarpScratchVjp,
                               kWarpScratchVjp);
@@ -114,7 +115,7 @@ __device__ void vjp_stage(PV v, PW w, PZ z, int lo, int hi, const AdjSmem<T>& a,
                 gL = ((wc - wm) * dtdx) * fmaf(0.5f, flux_prime<EQ>(ul, p.c), -hm);
             };
             float dd[5];
-            learned_cell_vjp32(f, bk, sc, seed, p.lp, scr, dd);
+            learned_cell_vjp32(ms, bk, sc, seed, p.lp, scr, dd);
             if (r < ncell) {
                 a.T0[c] = dd[0]; a.T1[c] = dd[1]; a.T2[c] = dd[2]; a.T3[c] = dd[3]; a.T4[c] = dd[4];
                 a.UL[c] = ul;
@@ -512,6 +513,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 2 : 1) batc
         fence_mbar_init();
     }
     __syncthreads();
+    learned_stage<REC, true>(p.lp);
     uint32_t phase = 0;
     const Win<const T> gpnext = make_win(pnext, total);
     const Win<T> gpout = make_win(pout, total);
@@ -565,6 +567,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : 1) repl
         fence_mbar_init();
     }
     __syncthreads();
+    learned_stage<REC>(p.lp);
     uint32_t phase = 0;
     const Win<const T> guin = make_win(uin, total);
     const Win<T> guout = make_win(uout, total);

@@ -73,6 +73,7 @@ __global__ void __launch_bounds__(kThreads, REC == SHK_REC_LEARNED ? 3 : (REC ==
         fence_mbar_init();
     }
     __syncthreads();
+    learned_stage<REC>(p.lp);
     uint32_t phase = 0;
     const int64_t k = *reinterpret_cast<volatile int64_t*>(P.step);
     const int cur = static_cast<int>(k & 1), nxt = cur ^ 1;
@@ -395,6 +396,7 @@ __global__ void __launch_bounds__(kThreads) apply_operator_kernel(const T* __res
         fence_mbar_init();
     }
     __syncthreads();
+    learned_stage<REC>(p.lp);
     uint32_t phase = 0;
     if constexpr (FLUX == SHK_FLUX_LF) p.hnu_amax = p.hnu * static_cast<T>(*amax);
     const int64_t s0 = int64_t(blockIdx.x) * tile;
@@ -457,6 +459,7 @@ __global__ void __launch_bounds__(kThreads) single_step_kernel(const T* __restri
         fence_mbar_init();
     }
     __syncthreads();
+    learned_stage<REC>(p.lp);
     uint32_t phase = 0;
     const int64_t s0 = int64_t(blockIdx.x) * tile;
     const int te = static_cast<int>(imin64(tile, n - s0));

@@ -224,8 +224,8 @@ __global__ void __launch_bounds__(256) learned_faces_kernel(LearnedParams lp, co
                                                             float* __restrict__ out, int64_t n) {
     __shared__ __align__(16) float scratch[(256 / 32) * kWarpScratch];
     float* scr = scratch + (threadIdx.x >> 5) * kWarpScratch;
-    MlpFrags f;
-    mlp_load_frags(lp.mlp, f);
+    mlp_stage_forward(lp.mlp, mlp_shared());
+    const MlpShared& ms = mlp_shared();
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int myrow = 16 * (t >> 1) + 8 * (t & 1) + g;
     const int64_t warps = int64_t(gridDim.x) * (blockDim.x >> 5);
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(256) learned_faces_kernel(LearnedParams lp, co
         for (int k = 0; k < 5; ++k) ds[k] = s[k] - s[2];
         ds[2] = 0.0f;
         float cr, cl;
-        learned_cell32(f, ds, lp, scr, cr, cl);
+        learned_cell32(ms, ds, lp, scr, cr, cl);
         if (r < n) {
             out[2 * r] = s[2] + cr;
             out[2 * r + 1] = s[2] + cl;

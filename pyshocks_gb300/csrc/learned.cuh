@@ -144,50 +144,84 @@ __device__ __forceinline__ void mma_bf16(float& d0, float& d1, float& d2, float&
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-// B fragments of the three layers for this lane (g = lane/4, t = lane%4):
-// layer l: out = act . W^T, B[k][n] = W[n][k]; b0 = (k=2t,2t+1), b1 = (k=2t+8,2t+9), n = g
-struct MlpFrags {
-    uint32_t w1[4][2];     // 4 n-tiles, K = 16 (5 inputs, bias column 5, zeros)
-    uint32_t w2[4][2][2];  // 4 n-tiles x 2 k-tiles
-    uint32_t w3[2][2];     // 1 n-tile (3 outputs + 5 zero rows) x 2 k-tiles
-    float b2[4][2];        // bias of layer 2 for columns nt*8 + 2t, +1
-    float b3[2];           // bias of layer 3 for columns 2t, 2t+1
+// The network's B fragments in shared memory, staged once per launch by the
+// whole block (mlp_stage) and read at each use: register-resident fragments
+// held 38 registers per thread for the whole kernel and made the step spill.
+// Lane L's words sit at [.][L] as one 16-byte vector, so the warp's load of a
+// vector is 512 contiguous bytes (no bank conflicts). Fragments of lane
+// (g = lane/4, t = lane%4), layer l: out = act . W^T, B[k][n] = W[n][k],
+// b0 = (k = 2t, 2t+1), b1 = (k = 2t+8, 2t+9), n = g.
+struct MlpShared {
+    uint4 w1[32];     // b0 of layer-1 n-tiles 0..3 (b1 is zero: 5 inputs + bias column)
+    uint4 w2[4][32];  // layer-2 n-tile nt: (k-tile 0 b0, b1, k-tile 1 b0, b1)
+    uint4 w3[32];     // layer 3 (n = 3 outputs + 5 zero rows): (k-tile 0 b0, b1, k-tile 1 b0, b1)
+    float b2[32];
+    float b3[8];      // 3 outputs, zero padded (columns 2t, 2t+1 for every t)
 };
 
-__device__ __forceinline__ void mlp_load_frags(const float* __restrict__ P, MlpFrags& f) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    auto w1e = [&](int n, int k) -> float {
-        if (k < kMlpIn) return P[kOffW1 + n * kMlpIn + k];
-        if (k == kMlpIn) return P[kOffB1 + n];
-        return 0.0f;
-    };
+// the fp16 B fragments of the network backward (see mlp_stage_back)
+struct MlpBackShared {
+    uint4 w3[32];     // dz W3: n-tiles 0..3
+    uint4 w2[4][32];  // da2 W2, n-tile nt: (k-tile 0 b0, b1, k-tile 1 b0, b1)
+    uint4 w1[32];     // da1 W1: (k-tile 0 b0, b1, k-tile 1 b0, b1)
+};
+
+// The block's staged network: one of each per kernel that runs the learned
+// reconstruction (a kernel that never calls these allocates neither).
+__device__ __forceinline__ MlpShared& mlp_shared() {
+    __shared__ MlpShared s;
+    return s;
+}
+__device__ __forceinline__ MlpBackShared& mlp_back_shared() {
+    __shared__ MlpBackShared s;
+    return s;
+}
+
+// layer-1 weight of unit n for input k: inputs 0..4, the bias as input 5
+__device__ __forceinline__ float mlp_w1(const float* __restrict__ P, int n, int k) {
+    if (k < kMlpIn) return P[kOffW1 + n * kMlpIn + k];
+    if (k == kMlpIn) return P[kOffB1 + n];
+    return 0.0f;
+}
+
+// stage the inference fragments of parameters P (whole block; ends with a barrier)
+__device__ inline void mlp_stage_forward(const float* __restrict__ P, MlpShared& s) {
+    for (int i = threadIdx.x; i < 6 * 32; i += blockDim.x) {
+        const int j = i >> 5, lane = i & 31, g = lane >> 2, t = lane & 3;
+        uint32_t w[4];
+        if (j == 0) {
 #pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        const int n = nt * 8 + g;
-        f.w1[nt][0] = pack_bf16(w1e(n, 2 * t), w1e(n, 2 * t + 1));
-        f.w1[nt][1] = pack_bf16(w1e(n, 2 * t + 8), w1e(n, 2 * t + 9));
+            for (int nt = 0; nt < 4; ++nt)
+                w[nt] = pack_bf16(mlp_w1(P, nt * 8 + g, 2 * t), mlp_w1(P, nt * 8 + g, 2 * t + 1));
+            s.w1[lane] = make_uint4(w[0], w[1], w[2], w[3]);
+        } else if (j <= 4) {
+            const int n = (j - 1) * 8 + g;
 #pragma unroll
-        for (int kt = 0; kt < 2; ++kt) {
-            const float* row = P + kOffW2 + n * kMlpH + kt * 16;
-            f.w2[nt][kt][0] = pack_bf16(row[2 * t], row[2 * t + 1]);
-            f.w2[nt][kt][1] = pack_bf16(row[2 * t + 8], row[2 * t + 9]);
-        }
-        f.b2[nt][0] = P[kOffB2 + nt * 8 + 2 * t];
-        f.b2[nt][1] = P[kOffB2 + nt * 8 + 2 * t + 1];
-    }
-#pragma unroll
-    for (int kt = 0; kt < 2; ++kt) {
-        if (g < kMlpOut) {
-            const float* row = P + kOffW3 + g * kMlpH + kt * 16;
-            f.w3[kt][0] = pack_bf16(row[2 * t], row[2 * t + 1]);
-            f.w3[kt][1] = pack_bf16(row[2 * t + 8], row[2 * t + 9]);
+            for (int kt = 0; kt < 2; ++kt) {
+                const float* row = P + kOffW2 + n * kMlpH + kt * 16;
+                w[2 * kt] = pack_bf16(row[2 * t], row[2 * t + 1]);
+                w[2 * kt + 1] = pack_bf16(row[2 * t + 8], row[2 * t + 9]);
+            }
+            s.w2[j - 1][lane] = make_uint4(w[0], w[1], w[2], w[3]);
         } else {
-            f.w3[kt][0] = 0u;
-            f.w3[kt][1] = 0u;
+#pragma unroll
+            for (int kt = 0; kt < 2; ++kt) {
+                if (g < kMlpOut) {
+                    const float* row = P + kOffW3 + g * kMlpH + kt * 16;
+                    w[2 * kt] = pack_bf16(row[2 * t], row[2 * t + 1]);
+                    w[2 * kt + 1] = pack_bf16(row[2 * t + 8], row[2 * t + 9]);
+                } else {
+                    w[2 * kt] = w[2 * kt + 1] = 0u;
+                }
+            }
+            s.w3[lane] = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
-    f.b3[0] = (2 * t < kMlpOut) ? P[kOffB3 + 2 * t] : 0.0f;
-    f.b3[1] = (2 * t + 1 < kMlpOut) ? P[kOffB3 + 2 * t + 1] : 0.0f;
+    for (int i = threadIdx.x; i < 40; i += blockDim.x) {
+        if (i < 32) s.b2[i] = P[kOffB2 + i];
+        else s.b3[i - 32] = i - 32 < kMlpOut ? P[kOffB3 + i - 32] : 0.0f;
+    }
+    __syncthreads();
 }
 
 // ---- 32 cells per warp iteration ----------------------------------------------
@@ -250,32 +284,54 @@ __device__ __forceinline__ float4 accum_row4(float* scr, int myrow, const float 
     return *reinterpret_cast<const float4*>(scr + 4 * myrow);
 }
 
-// hidden layers + output of one m16 tile; a0/a1: layer-1 A registers (rows g, g+8)
-__device__ __forceinline__ void mlp_tile(const MlpFrags& f, uint32_t a0, uint32_t a1, float& z0,
-                                         float& z1, float& z2, float& z3) {
-    uint32_t A2[2][4];
+// hidden layers + output of both m16 tiles of a 32-cell block: layer-1 A
+// registers a[0], a[1] (tile A, rows g and g+8) and a[2], a[3] (tile B). Each
+// fragment loaded from shared memory serves both tiles, and the two tiles'
+// mma chains interleave. A2x / A3x: the bf16 hidden activations
+// tanh(layer-1 / layer-2 pre-activation) of tile x in A-fragment layout (the
+// backward keeps them); zA, zB: the logit accumulators.
+__device__ __forceinline__ void mlp_tiles(const MlpShared& s, const uint32_t a[4], uint32_t A2a[2][4],
+                                          uint32_t A2b[2][4], uint32_t A3a[2][4], uint32_t A3b[2][4],
+                                          float zA[4], float zB[4]) {
+    const int lane = threadIdx.x & 31, t = lane & 3;
+    {
+        const uint4 w = s.w1[lane];
+        const uint32_t w1[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
+            float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f, d3 = 0.0f;
+            mma_bf16(c0, c1, c2, c3, a[0], a[1], 0u, 0u, w1[nt], 0u);
+            mma_bf16(d0, d1, d2, d3, a[2], a[3], 0u, 0u, w1[nt], 0u);
+            A2a[nt >> 1][(nt & 1) * 2 + 0] = tanh_bf16x2(pack_bf16(c0, c1));
+            A2a[nt >> 1][(nt & 1) * 2 + 1] = tanh_bf16x2(pack_bf16(c2, c3));
+            A2b[nt >> 1][(nt & 1) * 2 + 0] = tanh_bf16x2(pack_bf16(d0, d1));
+            A2b[nt >> 1][(nt & 1) * 2 + 1] = tanh_bf16x2(pack_bf16(d2, d3));
+        }
+    }
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt) {
-        float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
-        mma_bf16(c0, c1, c2, c3, a0, a1, 0u, 0u, f.w1[nt][0], f.w1[nt][1]);
-        A2[nt >> 1][(nt & 1) * 2 + 0] = tanh_bf16x2(pack_bf16(c0, c1));
-        A2[nt >> 1][(nt & 1) * 2 + 1] = tanh_bf16x2(pack_bf16(c2, c3));
+        const uint4 w = s.w2[nt][lane];
+        const float2 bb = *reinterpret_cast<const float2*>(&s.b2[nt * 8 + 2 * t]);
+        float c0 = bb.x, c1 = bb.y, c2 = bb.x, c3 = bb.y;
+        float d0 = bb.x, d1 = bb.y, d2 = bb.x, d3 = bb.y;
+        mma_bf16(c0, c1, c2, c3, A2a[0][0], A2a[0][1], A2a[0][2], A2a[0][3], w.x, w.y);
+        mma_bf16(d0, d1, d2, d3, A2b[0][0], A2b[0][1], A2b[0][2], A2b[0][3], w.x, w.y);
+        mma_bf16(c0, c1, c2, c3, A2a[1][0], A2a[1][1], A2a[1][2], A2a[1][3], w.z, w.w);
+        mma_bf16(d0, d1, d2, d3, A2b[1][0], A2b[1][1], A2b[1][2], A2b[1][3], w.z, w.w);
+        A3a[nt >> 1][(nt & 1) * 2 + 0] = tanh_bf16x2(pack_bf16(c0, c1));
+        A3a[nt >> 1][(nt & 1) * 2 + 1] = tanh_bf16x2(pack_bf16(c2, c3));
+        A3b[nt >> 1][(nt & 1) * 2 + 0] = tanh_bf16x2(pack_bf16(d0, d1));
+        A3b[nt >> 1][(nt & 1) * 2 + 1] = tanh_bf16x2(pack_bf16(d2, d3));
     }
-    uint32_t A3[2][4];
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        float c0 = f.b2[nt][0], c1 = f.b2[nt][1], c2 = f.b2[nt][0], c3 = f.b2[nt][1];
-#pragma unroll
-        for (int kt = 0; kt < 2; ++kt)
-            mma_bf16(c0, c1, c2, c3, A2[kt][0], A2[kt][1], A2[kt][2], A2[kt][3], f.w2[nt][kt][0],
-                     f.w2[nt][kt][1]);
-        A3[nt >> 1][(nt & 1) * 2 + 0] = tanh_bf16x2(pack_bf16(c0, c1));
-        A3[nt >> 1][(nt & 1) * 2 + 1] = tanh_bf16x2(pack_bf16(c2, c3));
-    }
-    z0 = f.b3[0]; z1 = f.b3[1]; z2 = f.b3[0]; z3 = f.b3[1];
-#pragma unroll
-    for (int kt = 0; kt < 2; ++kt)
-        mma_bf16(z0, z1, z2, z3, A3[kt][0], A3[kt][1], A3[kt][2], A3[kt][3], f.w3[kt][0], f.w3[kt][1]);
+    const uint4 w = s.w3[lane];
+    const float2 bb = *reinterpret_cast<const float2*>(&s.b3[2 * t]);
+    zA[0] = bb.x; zA[1] = bb.y; zA[2] = bb.x; zA[3] = bb.y;
+    zB[0] = bb.x; zB[1] = bb.y; zB[2] = bb.x; zB[3] = bb.y;
+    mma_bf16(zA[0], zA[1], zA[2], zA[3], A3a[0][0], A3a[0][1], A3a[0][2], A3a[0][3], w.x, w.y);
+    mma_bf16(zB[0], zB[1], zB[2], zB[3], A3b[0][0], A3b[0][1], A3b[0][2], A3b[0][3], w.x, w.y);
+    mma_bf16(zA[0], zA[1], zA[2], zA[3], A3a[1][0], A3a[1][1], A3a[1][2], A3a[1][3], w.z, w.w);
+    mma_bf16(zB[0], zB[1], zB[2], zB[3], A3b[1][0], A3b[1][1], A3b[1][2], A3b[1][3], w.z, w.w);
 }
 
 // The face corrections sum_k omega_k (uhat_k - s_2) of this lane's cell (right
@@ -283,7 +339,7 @@ __device__ __forceinline__ void mlp_tile(const MlpFrags& f, uint32_t a0, uint32_
 // WENO-JS trust band per face. All 32 lanes must call it (shuffles) with
 // finite stencils.
 // scr: the warp's kWarpScratch floats of shared memory (16-byte aligned).
-__device__ __forceinline__ void learned_cell32(const MlpFrags& f, const float ds[5],
+__device__ __forceinline__ void learned_cell32(const MlpShared& ms, const float ds[5],
                                                const LearnedParams& lp, float* scr, float& cr,
                                                float& cl) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -296,8 +352,10 @@ __device__ __forceinline__ void learned_cell32(const MlpFrags& f, const float ds
     rows_to_afrags(scr, myrow, pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], 1.0f),
                    0u, a);
     float zA[4], zB[4];
-    mlp_tile(f, a[0], a[1], zA[0], zA[1], zA[2], zA[3]);
-    mlp_tile(f, a[2], a[3], zB[0], zB[1], zB[2], zB[3]);
+    {
+        uint32_t A2a[2][4], A2b[2][4], A3a[2][4], A3b[2][4];
+        mlp_tiles(ms, a, A2a, A2b, A3a, A3b, zA, zB);
+    }
     // logits of the owned row (columns 0..2 of the output tiles)
     const float4 zr = accum_row4(scr, myrow, zA, zB);
     const float z0 = zr.x, z1 = zr.y, z2 = zr.z;
@@ -351,66 +409,48 @@ __device__ __forceinline__ float round_bf16(float x) {
     return __bfloat162float(__float2bfloat16_rn(x));
 }
 
-// fp16 B fragments of the backward products for this lane (g = lane/4, t = lane%4):
-// B[k][n] with k the contracted index (rows 2t, 2t+1 and 2t+8, 2t+9), n = g
-struct MlpBackFrags {
-    uint32_t w3[4];        // dz W3: k = output (3 of 16), n = hidden (4 n-tiles)
-    uint32_t w2[4][2][2];  // da2 W2: k = layer-2 unit (2 k-tiles), n = layer-1 unit (4 n-tiles)
-    uint32_t w1[2][2];     // da1 W1: k = layer-1 unit (2 k-tiles), n = input (5 of 8)
-};
-
-__device__ __forceinline__ void mlp_load_back_frags(const float* __restrict__ P, MlpBackFrags& b) {
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    auto h = [](float w) { return round_bf16(w); };
+// stage the fp16 B fragments of the backward products for parameters P
+// (whole block; ends with a barrier). Lane (g = lane/4, t = lane%4): B[k][n]
+// with k the contracted index (rows 2t, 2t+1 and 2t+8, 2t+9), n = g; dz W3
+// (k = output, 3 of 16; n = hidden, 4 n-tiles), da2 W2 (k = layer-2 unit,
+// 2 k-tiles; n = layer-1 unit, 4 n-tiles), da1 W1 (k = layer-1 unit, 2
+// k-tiles; n = input, 5 of 8). The weights are the forward's bf16 roundings.
+__device__ inline void mlp_stage_back(const float* __restrict__ P, MlpBackShared& s) {
+    for (int i = threadIdx.x; i < 6 * 32; i += blockDim.x) {
+        const int j = i >> 5, lane = i & 31, g = lane >> 2, t = lane & 3;
+        uint32_t w[4];
+        if (j == 0) {
 #pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        const int n = nt * 8 + g;
-        // rows k = 2t, 2t+1 of W3 (k < 3), column n
-        const float w30 = 2 * t < kMlpOut ? h(P[kOffW3 + (2 * t) * kMlpH + n]) : 0.0f;
-        const float w31 = 2 * t + 1 < kMlpOut ? h(P[kOffW3 + (2 * t + 1) * kMlpH + n]) : 0.0f;
-        b.w3[nt] = pack_f16(w30, w31);
+            for (int nt = 0; nt < 4; ++nt) {
+                const int n = nt * 8 + g;
+                const float w30 = 2 * t < kMlpOut ? round_bf16(P[kOffW3 + (2 * t) * kMlpH + n]) : 0.0f;
+                const float w31 = 2 * t + 1 < kMlpOut ? round_bf16(P[kOffW3 + (2 * t + 1) * kMlpH + n]) : 0.0f;
+                w[nt] = pack_f16(w30, w31);
+            }
+            s.w3[lane] = make_uint4(w[0], w[1], w[2], w[3]);
+        } else if (j <= 4) {
+            const int n = (j - 1) * 8 + g;
 #pragma unroll
-        for (int kt = 0; kt < 2; ++kt) {
-            const int k = kt * 16 + 2 * t;
-            b.w2[nt][kt][0] = pack_f16(h(P[kOffW2 + k * kMlpH + n]), h(P[kOffW2 + (k + 1) * kMlpH + n]));
-            b.w2[nt][kt][1] = pack_f16(h(P[kOffW2 + (k + 8) * kMlpH + n]), h(P[kOffW2 + (k + 9) * kMlpH + n]));
+            for (int kt = 0; kt < 2; ++kt) {
+                const int k = kt * 16 + 2 * t;
+                w[2 * kt] = pack_f16(round_bf16(P[kOffW2 + k * kMlpH + n]),
+                                     round_bf16(P[kOffW2 + (k + 1) * kMlpH + n]));
+                w[2 * kt + 1] = pack_f16(round_bf16(P[kOffW2 + (k + 8) * kMlpH + n]),
+                                         round_bf16(P[kOffW2 + (k + 9) * kMlpH + n]));
+            }
+            s.w2[j - 1][lane] = make_uint4(w[0], w[1], w[2], w[3]);
+        } else {
+            auto w1 = [&](int kk) { return g < kMlpIn ? round_bf16(P[kOffW1 + kk * kMlpIn + g]) : 0.0f; };
+#pragma unroll
+            for (int kt = 0; kt < 2; ++kt) {
+                const int k = kt * 16 + 2 * t;
+                w[2 * kt] = pack_f16(w1(k), w1(k + 1));
+                w[2 * kt + 1] = pack_f16(w1(k + 8), w1(k + 9));
+            }
+            s.w1[lane] = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
-#pragma unroll
-    for (int kt = 0; kt < 2; ++kt) {
-        const int k = kt * 16 + 2 * t;
-        auto w1 = [&](int kk) { return g < kMlpIn ? h(P[kOffW1 + kk * kMlpIn + g]) : 0.0f; };
-        b.w1[kt][0] = pack_f16(w1(k), w1(k + 1));
-        b.w1[kt][1] = pack_f16(w1(k + 8), w1(k + 9));
-    }
-}
-
-// hidden layers + output of one m16 tile, keeping the bf16 activations
-// (A2 = tanh(h1 pre-activation), A3 = tanh(h2 pre-activation)) in A-fragment layout
-__device__ __forceinline__ void mlp_tile_keep(const MlpFrags& f, uint32_t a0, uint32_t a1,
-                                              uint32_t A2[2][4], uint32_t A3[2][4], float& z0,
-                                              float& z1, float& z2, float& z3) {
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
-        mma_bf16(c0, c1, c2, c3, a0, a1, 0u, 0u, f.w1[nt][0], f.w1[nt][1]);
-        A2[nt >> 1][(nt & 1) * 2 + 0] = tanh_bf16x2(pack_bf16(c0, c1));
-        A2[nt >> 1][(nt & 1) * 2 + 1] = tanh_bf16x2(pack_bf16(c2, c3));
-    }
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        float c0 = f.b2[nt][0], c1 = f.b2[nt][1], c2 = f.b2[nt][0], c3 = f.b2[nt][1];
-#pragma unroll
-        for (int kt = 0; kt < 2; ++kt)
-            mma_bf16(c0, c1, c2, c3, A2[kt][0], A2[kt][1], A2[kt][2], A2[kt][3], f.w2[nt][kt][0],
-                     f.w2[nt][kt][1]);
-        A3[nt >> 1][(nt & 1) * 2 + 0] = tanh_bf16x2(pack_bf16(c0, c1));
-        A3[nt >> 1][(nt & 1) * 2 + 1] = tanh_bf16x2(pack_bf16(c2, c3));
-    }
-    z0 = f.b3[0]; z1 = f.b3[1]; z2 = f.b3[0]; z3 = f.b3[1];
-#pragma unroll
-    for (int kt = 0; kt < 2; ++kt)
-        mma_bf16(z0, z1, z2, z3, A3[kt][0], A3[kt][1], A3[kt][2], A3[kt][3], f.w3[kt][0], f.w3[kt][1]);
+    __syncthreads();
 }
 
 // (x0, x1) * (1 - h^2) for a bf16 pair h, packed to fp16
@@ -419,36 +459,56 @@ __device__ __forceinline__ uint32_t tanh_back_f16(float x0, float x1, uint32_t h
     return pack_f16(x0 * fmaf(-h0, h0, 1.0f), x1 * fmaf(-h1, h1, 1.0f));
 }
 
-// network backward of one m16 tile: d0 / d1 the fp16 A registers of the
-// (scaled) logit cotangents of rows g / g+8 (columns 2t, 2t+1); returns the
-// input cotangents dx (row g: columns 2t, 2t+1 in x[0], x[1]; row g+8 in x[2], x[3])
-__device__ __forceinline__ void mlp_tile_back(const MlpBackFrags& b, uint32_t d0, uint32_t d1,
-                                              const uint32_t A2[2][4], const uint32_t A3[2][4],
-                                              float x[4]) {
-    uint32_t D2[2][4];
+// network backward of both m16 tiles of a block: d[0], d[1] / d[2], d[3] the
+// fp16 A registers of the (scaled) logit cotangents of tile A / B (rows g,
+// g+8; columns 2t, 2t+1), A2x / A3x the tiles' kept activations; returns the
+// input cotangents (row g: columns 2t, 2t+1 in x[0], x[1]; row g+8 in x[2],
+// x[3]) of tile A in xa and of tile B in xb. Each fragment load serves both tiles.
+__device__ __forceinline__ void mlp_tiles_back(const MlpBackShared& s, const uint32_t d[4],
+                                               const uint32_t A2a[2][4], const uint32_t A2b[2][4],
+                                               const uint32_t A3a[2][4], const uint32_t A3b[2][4],
+                                               float xa[4], float xb[4]) {
+    const int lane = threadIdx.x & 31;
+    uint32_t D2a[2][4], D2b[2][4];
+    {
+        const uint4 w = s.w3[lane];
+        const uint32_t w3[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt) {
+            float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
+            float e0 = 0.0f, e1 = 0.0f, e2 = 0.0f, e3 = 0.0f;
+            mma_f16(c0, c1, c2, c3, d[0], d[1], 0u, 0u, w3[nt], 0u);
+            mma_f16(e0, e1, e2, e3, d[2], d[3], 0u, 0u, w3[nt], 0u);
+            const int j = nt >> 1, q = (nt & 1) * 2;
+            D2a[j][q] = tanh_back_f16(c0, c1, A3a[j][q]);
+            D2a[j][q + 1] = tanh_back_f16(c2, c3, A3a[j][q + 1]);
+            D2b[j][q] = tanh_back_f16(e0, e1, A3b[j][q]);
+            D2b[j][q + 1] = tanh_back_f16(e2, e3, A3b[j][q + 1]);
+        }
+    }
+    uint32_t D1a[2][4], D1b[2][4];
 #pragma unroll
     for (int nt = 0; nt < 4; ++nt) {
+        const uint4 w = s.w2[nt][lane];
         float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
-        mma_f16(c0, c1, c2, c3, d0, d1, 0u, 0u, b.w3[nt], 0u);
-        D2[nt >> 1][(nt & 1) * 2 + 0] = tanh_back_f16(c0, c1, A3[nt >> 1][(nt & 1) * 2 + 0]);
-        D2[nt >> 1][(nt & 1) * 2 + 1] = tanh_back_f16(c2, c3, A3[nt >> 1][(nt & 1) * 2 + 1]);
+        float e0 = 0.0f, e1 = 0.0f, e2 = 0.0f, e3 = 0.0f;
+        mma_f16(c0, c1, c2, c3, D2a[0][0], D2a[0][1], D2a[0][2], D2a[0][3], w.x, w.y);
+        mma_f16(e0, e1, e2, e3, D2b[0][0], D2b[0][1], D2b[0][2], D2b[0][3], w.x, w.y);
+        mma_f16(c0, c1, c2, c3, D2a[1][0], D2a[1][1], D2a[1][2], D2a[1][3], w.z, w.w);
+        mma_f16(e0, e1, e2, e3, D2b[1][0], D2b[1][1], D2b[1][2], D2b[1][3], w.z, w.w);
+        const int j = nt >> 1, q = (nt & 1) * 2;
+        D1a[j][q] = tanh_back_f16(c0, c1, A2a[j][q]);
+        D1a[j][q + 1] = tanh_back_f16(c2, c3, A2a[j][q + 1]);
+        D1b[j][q] = tanh_back_f16(e0, e1, A2b[j][q]);
+        D1b[j][q + 1] = tanh_back_f16(e2, e3, A2b[j][q + 1]);
     }
-    uint32_t D1[2][4];
-#pragma unroll
-    for (int nt = 0; nt < 4; ++nt) {
-        float c0 = 0.0f, c1 = 0.0f, c2 = 0.0f, c3 = 0.0f;
-#pragma unroll
-        for (int kt = 0; kt < 2; ++kt)
-            mma_f16(c0, c1, c2, c3, D2[kt][0], D2[kt][1], D2[kt][2], D2[kt][3], b.w2[nt][kt][0],
-                    b.w2[nt][kt][1]);
-        D1[nt >> 1][(nt & 1) * 2 + 0] = tanh_back_f16(c0, c1, A2[nt >> 1][(nt & 1) * 2 + 0]);
-        D1[nt >> 1][(nt & 1) * 2 + 1] = tanh_back_f16(c2, c3, A2[nt >> 1][(nt & 1) * 2 + 1]);
-    }
-    x[0] = x[1] = x[2] = x[3] = 0.0f;
-#pragma unroll
-    for (int kt = 0; kt < 2; ++kt)
-        mma_f16(x[0], x[1], x[2], x[3], D1[kt][0], D1[kt][1], D1[kt][2], D1[kt][3], b.w1[kt][0],
-                b.w1[kt][1]);
+    const uint4 w = s.w1[lane];
+    xa[0] = xa[1] = xa[2] = xa[3] = 0.0f;
+    xb[0] = xb[1] = xb[2] = xb[3] = 0.0f;
+    mma_f16(xa[0], xa[1], xa[2], xa[3], D1a[0][0], D1a[0][1], D1a[0][2], D1a[0][3], w.x, w.y);
+    mma_f16(xb[0], xb[1], xb[2], xb[3], D1b[0][0], D1b[0][1], D1b[0][2], D1b[0][3], w.x, w.y);
+    mma_f16(xa[0], xa[1], xa[2], xa[3], D1a[1][0], D1a[1][1], D1a[1][2], D1a[1][3], w.z, w.w);
+    mma_f16(xb[0], xb[1], xb[2], xb[3], D1b[1][0], D1b[1][1], D1b[1][2], D1b[1][3], w.z, w.w);
 }
 
 // gR d(u_R)/ds + gL d(u_L)/ds of this lane's cell (right and left face values)
@@ -460,7 +520,7 @@ __device__ __forceinline__ void mlp_tile_back(const MlpBackFrags& b, uint32_t d0
 // depend on the face values). All 32 lanes must call it (shuffles, mma) with
 // finite stencils; returns dsum[5].
 template <class Seed>
-__device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpBackFrags& bk,
+__device__ __forceinline__ void learned_cell_vjp32(const MlpShared& ms, const MlpBackShared& bk,
                                                    const float s[5], Seed&& seed,
                                                    const LearnedParams& lp, float* scr,
                                                    float dsum[5]) {
@@ -474,8 +534,7 @@ __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpB
                    0u, a);
     uint32_t A2a[2][4], A3a[2][4], A2b[2][4], A3b[2][4];
     float zA[4], zB[4];
-    mlp_tile_keep(f, a[0], a[1], A2a, A3a, zA[0], zA[1], zA[2], zA[3]);
-    mlp_tile_keep(f, a[2], a[3], A2b, A3b, zB[0], zB[1], zB[2], zB[3]);
+    mlp_tiles(ms, a, A2a, A2b, A3a, A3b, zA, zB);
     const float4 zr = accum_row4(scr, myrow, zA, zB);
     const float z0 = zr.x, z1 = zr.y, z2 = zr.z;
     // ---- per-cell part: weights, fallback, direct terms, logit cotangents
@@ -547,8 +606,7 @@ __device__ __forceinline__ void learned_cell_vjp32(const MlpFrags& f, const MlpB
     rows_to_afrags(scr, myrow, pack_f16(dz[0] * up, dz[1] * up), pack_f16(dz[2] * up, 0.0f), 0u,
                    0u, d);
     float xa[4], xb[4];
-    mlp_tile_back(bk, d[0], d[1], A2a, A3a, xa);
-    mlp_tile_back(bk, d[2], d[3], A2b, A3b, xb);
+    mlp_tiles_back(bk, d, A2a, A2b, A3a, A3b, xa, xb);
     // the owned row's dx[0..5] (columns 0..5 of the input-gradient tiles, held
     // by lanes t = 0, 1, 2), through rows of 6 floats
     float dx[6];

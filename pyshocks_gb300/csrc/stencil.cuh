@@ -19,9 +19,15 @@ constexpr int kThreads = 256;
 constexpr int kDefaultTile = 1024;
 // shortest tile of a plan with the learned reconstruction: its warp scratch
 // (8 warps x 128 floats forward, x 192 in the reverse step) lives in window
-// arrays that the learned phase leaves free (2W floats in the mixed step,
-// 3W in the float step and the reverse step)
+// arrays that the learned phase leaves free (the face-flux array D, at least
+// kLearnedScratch floats, in the mixed step; 2W floats in the float step, 3W
+// in the reverse step)
 constexpr int kLearnedMinTile = 512;
+// floats of the forward learned phase's scratch (8 warps, 16-byte alignment slack)
+constexpr int kLearnedScratch = (kThreads / 32) * kWarpScratch + 4;
+// length of the face-flux array D of the mixed step's layout (the learned
+// phase's scratch before it takes the fluxes)
+__host__ __device__ constexpr int mixed_d_len(int W) { return W > kLearnedScratch ? W : kLearnedScratch; }
 
 // halo of a window: 9 cells are needed for three fused stages, rounded up so
 // that the window start stays 16-byte aligned for cp.async.bulk
@@ -33,6 +39,17 @@ __host__ __device__ inline int64_t imin64(int64_t a, int64_t b) { return a < b ?
 __host__ __device__ inline int64_t imod(int64_t a, int64_t n) {
     int64_t r = a % n;
     return r < 0 ? r + n : r;
+}
+
+// the scratch of the learned phase: the nfloats floats of shared memory from
+// `region` that the layout leaves free in that phase, from a 16-byte aligned
+// start
+template <class PR>
+__device__ __forceinline__ Win<float> learned_scratch(PR region, int nfloats) {
+    float* r = reinterpret_cast<float*>(win_raw(region));
+    const uintptr_t a = reinterpret_cast<uintptr_t>(r);
+    float* s = reinterpret_cast<float*>((a + 15) & ~uintptr_t(15));
+    return make_win(s, nfloats - static_cast<int>(s - r));
 }
 
 // ---------------------------------------------------------------------------
@@ -48,15 +65,17 @@ struct Smem {
     Win<T> UL;  // ul (value at the left face of the cell)
     Win<T> UR;  // ur (value at the right face of the cell)
     Win<T> I;   // float states: stage increments (see step_tile); null for double
+    Win<float> scr;  // the learned phase's warp scratch (free in that phase)
     int W;      // window length (cells) of every array
 
     // float states carry one more array (the stage increments)
     static constexpr int kArrays = sizeof(T) == 4 ? 8 : 7;
     __host__ static size_t host_bytes(int W) { return size_t(kArrays) * W * sizeof(T); }
     // the step tile of a double state with the learned reconstruction runs in
-    // mixed precision (step_tile_mixed) on the double window and 7 float arrays
+    // mixed precision (step_tile_mixed) on the double window and 6 float arrays
     __host__ static size_t step_bytes(int W, int rec) {
-        if (sizeof(T) == 8 && rec == SHK_REC_LEARNED) return size_t(W) * (sizeof(double) + 7 * sizeof(float));
+        if (sizeof(T) == 8 && rec == SHK_REC_LEARNED)
+            return size_t(W) * sizeof(double) + size_t(5 * W + mixed_d_len(W)) * sizeof(float);
         if (sizeof(T) == 4 && rec == SHK_REC_WENOJS53) return size_t(6) * W * sizeof(T);
         return host_bytes(W);
     }
@@ -67,21 +86,23 @@ struct Smem {
         U = make_win(p, W); S = make_win(p + W, W); D = make_win(p + 2 * W, W);
         UL = make_win(p + 3 * W, W); UR = make_win(p + 4 * W, W); I = make_win(p + 5 * W, W);
         H = Q = Win<T>();
+        scr = Win<float>();
         this->W = W;
     }
     // compact layout of that mixed step: U (double window), then as float
-    // arrays S (2W: uf, k), I (increments), H, D, UL, UR; H and D are
-    // contiguous (the learned phase's warp scratch, before D takes the face
-    // fluxes); Q aliases D (the learned reconstruction does not use it)
+    // arrays S (2W: uf, k), I (increments), UL, UR and D (mixed_d_len(W)
+    // floats: the learned phase's warp scratch before it takes the face
+    // fluxes); no H, and Q aliases D (the learned reconstruction uses neither)
     __device__ void carve_mixed(unsigned char* base, int W) {
         U = make_win(reinterpret_cast<T*>(base), W);
         float* f = reinterpret_cast<float*>(base + size_t(W) * sizeof(double));
         S = win_cast<T>(make_win(f, 2 * W));
         I = win_cast<T>(make_win(f + 2 * W, W));
-        H = win_cast<T>(make_win(f + 3 * W, W));
-        D = win_cast<T>(make_win(f + 4 * W, W));
-        UL = win_cast<T>(make_win(f + 5 * W, W));
-        UR = win_cast<T>(make_win(f + 6 * W, W));
+        UL = win_cast<T>(make_win(f + 3 * W, W));
+        UR = win_cast<T>(make_win(f + 4 * W, W));
+        D = win_cast<T>(make_win(f + 5 * W, W));
+        scr = learned_scratch(make_win(f + 5 * W, mixed_d_len(W)), mixed_d_len(W));
+        H = Win<T>();
         Q = D;
         this->W = W;
     }
@@ -91,6 +112,8 @@ struct Smem {
         D = make_win(p + 3 * W, W); Q = make_win(p + 4 * W, W);
         UL = make_win(p + 5 * W, W); UR = make_win(p + 6 * W, W);
         I = kArrays > 7 ? make_win(p + 7 * W, W) : Win<T>();
+        const int hd = 2 * W * int(sizeof(T) / sizeof(float));  // H and D as floats
+        scr = learned_scratch(make_win(reinterpret_cast<float*>(p + 2 * W), hd), hd);
         this->W = W;
     }
 };
@@ -212,19 +235,21 @@ __host__ __device__ inline OpParams<float> float_params(const OpParams<T>& p) {
     return f;
 }
 
-// the scratch of the learned phase: the nfloats floats of shared memory from
-// `region` that the layout leaves free in that phase, from a 16-byte aligned
-// start
-template <class PR>
-__device__ __forceinline__ Win<float> learned_scratch(PR region, int nfloats) {
-    float* r = reinterpret_cast<float*>(win_raw(region));
-    const uintptr_t a = reinterpret_cast<uintptr_t>(r);
-    float* s = reinterpret_cast<float*>((a + 15) & ~uintptr_t(15));
-    return make_win(s, nfloats - static_cast<int>(s - r));
+// Stage the network of a learned scheme in the block's shared memory (every
+// kernel that may run the learned reconstruction, before its first use; the
+// whole block; ends with a barrier). BACK: also the backward's fragments.
+template <int REC, bool BACK = false>
+__device__ __forceinline__ void learned_stage(const LearnedParams& lp) {
+    if constexpr (REC == SHK_REC_LEARNED) {
+        mlp_stage_forward(lp.mlp, mlp_shared());
+        if constexpr (BACK) mlp_stage_back(lp.mlp, mlp_back_shared());
+    }
 }
 
+
 // learned reconstruction of cells [clo, chi): one cell per lane, 32 cells per
-// warp iteration, both faces of a cell from one network evaluation. A cell's
+// warp iteration, both faces of a cell from one network evaluation (the
+// network staged by learned_stage). A cell's
 // stencil relative to v_c is formed in the state precision straight from the
 // window (v_{c+o} - v_c, o = -2..2) and rounded to float; the face values are
 // v_c + correction in the state precision.
@@ -232,8 +257,7 @@ __device__ __forceinline__ Win<float> learned_scratch(PR region, int nfloats) {
 template <class T, class PV, class PO>
 __device__ __forceinline__ void learned_phase(PV v, int clo, int chi, PO UL, PO UR,
                                               const LearnedParams& lp, const Win<float>& scratch) {
-    MlpFrags f;
-    mlp_load_frags(lp.mlp, f);
+    const MlpShared& ms = mlp_shared();
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     float* scr = win_span(scratch, warp * kWarpScratch, kWarpScratch);
@@ -247,7 +271,7 @@ __device__ __forceinline__ void learned_phase(PV v, int clo, int chi, PO UL, PO 
                              0.0f, static_cast<float>(v[c + 1] - vc),
                              static_cast<float>(v[c + 2] - vc)};
         float cr, cl;
-        learned_cell32(f, ds, lp, scr, cr, cl);
+        learned_cell32(ms, ds, lp, scr, cr, cl);
         if (r < ncell) {
             UR[c] = vc + static_cast<T>(cr);
             UL[c] = vc + static_cast<T>(cl);
@@ -301,10 +325,10 @@ __device__ __forceinline__ void face_fluxes(PV v, int lo, int hi, const Smem<T>&
         }
         __syncthreads();
     } else if constexpr (REC == SHK_REC_LEARNED) {
-        // warp scratch: H onward (free in this phase: H and D, 2W floats, in
-        // every learned layout; with tiles of at least kLearnedMinTile that is
-        // more than the 8 x kWarpScratch + 3 floats needed)
-        learned_phase<T>(v, lo - 1, hi + 1, sm.UL, sm.UR, p.lp, learned_scratch(sm.H, 2 * sm.W));
+        // warp scratch: sm.scr (free in this phase; with tiles of at least
+        // kLearnedMinTile every learned layout gives it kLearnedScratch floats
+        // or more)
+        learned_phase<T>(v, lo - 1, hi + 1, sm.UL, sm.UR, p.lp, sm.scr);
         __syncthreads();
     } else if constexpr (REC == SHK_REC_CONSTANT) {
         // reconstruction.py:153-163: ul = ur = u
@@ -524,6 +548,7 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, Win<double
     fs.UL = win_cast<float>(sm.UL);
     fs.UR = win_cast<float>(sm.UR);
     fs.I = win_cast<float>(sm.I);
+    fs.scr = sm.scr;
     fs.W = W;
     const Win<float> inc = fs.I;
     const float dtf = static_cast<float>(dtdx);
