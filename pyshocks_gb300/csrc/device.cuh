@@ -226,6 +226,19 @@ __device__ __forceinline__ T phys_flux(T u, T c) {
     else if constexpr (EQ == SHK_EQ_ADVECTION) return c * u;
     else return u * (T(1) - u);
 }
+// f(L) + f(R) with every product and the sum rounded separately, as the
+// reference evaluates it: left to the compiler, one product could be fused
+// into an FMA with the sum, and which one depends on the surrounding code
+template <int EQ, class T>
+__device__ __forceinline__ T phys_flux_sum(T L, T R, T c) {
+    if constexpr (sizeof(T) == 8) {
+        if constexpr (EQ == SHK_EQ_ADVECTION) return __dadd_rn(__dmul_rn(c, L), __dmul_rn(c, R));
+        else return __dadd_rn(__dmul_rn(L, 1.0 - L), __dmul_rn(R, 1.0 - R));
+    } else {
+        if constexpr (EQ == SHK_EQ_ADVECTION) return __fadd_rn(__fmul_rn(c, L), __fmul_rn(c, R));
+        else return __fadd_rn(__fmul_rn(L, 1.0f - L), __fmul_rn(R, 1.0f - R));
+    }
+}
 template <int EQ, class T>
 __device__ __forceinline__ T wave_speed(T u, T c) {
     if constexpr (EQ == SHK_EQ_BURGERS) return u;
@@ -293,19 +306,24 @@ __device__ __forceinline__ void weno53_cell_d(double v, double dm1, double d0, d
 }
 
 // Float variant of weno53_cell_d for the one-pass float reconstruction: the
-// same unscaled differences (d_{c-2} .. d_{c+1} from the window, E and G formed
-// here) and folded corrections, with the weights P_k = 1/s_k and the two
-// normalisations as one-instruction approximate reciprocals (a product form
-// could underflow in float).
-__device__ __forceinline__ void weno53_cell_f(float v, float dm2, float dm1, float d0, float dp1,
-                                              float eps4, float& ul, float& ur) {
-    const float Em1 = dm1 - dm2, E0 = d0 - dm1, Ep1 = dp1 - d0;
+// same unscaled differences (d_{c-1}, d_c, E_{c-1..c+1} and the terms
+// G_j = 13/3 E_j^2 + 4 eps, which neighbouring cells share) and folded
+// corrections, with the weights P_k = 1/s_k and the two normalisations as
+// one-instruction approximate reciprocals (a product form could underflow in
+// float).
+__device__ __forceinline__ float weno53_g_f(float E, float eps4) {
+    return fmaf((13.0f / 3.0f) * E, E, eps4);
+}
+
+__device__ __forceinline__ void weno53_cell_fg(float v, float dm1, float d0, float Em1, float E0,
+                                               float Ep1, float Gm1, float G0, float Gp1,
+                                               float& ul, float& ur) {
     const float h0 = fmaf(2.0f, dm1, Em1);
     const float h1 = d0 + dm1;
     const float h2 = fmaf(-2.0f, d0, Ep1);
-    float s0 = fmaf(h0, h0, fmaf((13.0f / 3.0f) * Em1, Em1, eps4)); s0 = s0 * s0;
-    float s1 = fmaf(h1, h1, fmaf((13.0f / 3.0f) * E0, E0, eps4)); s1 = s1 * s1;
-    float s2 = fmaf(h2, h2, fmaf((13.0f / 3.0f) * Ep1, Ep1, eps4)); s2 = s2 * s2;
+    float s0 = fmaf(h0, h0, Gm1); s0 = s0 * s0;
+    float s1 = fmaf(h1, h1, G0); s1 = s1 * s1;
+    float s2 = fmaf(h2, h2, Gp1); s2 = s2 * s2;
     const float P0 = rcp_approx_f32(s0), P1 = rcp_approx_f32(s1), P2 = rcp_approx_f32(s2);
     const float cr0 = fmaf(2.0f, h0, -dm1);
     const float cr1 = fmaf(12.0f, d0, 6.0f * dm1);
@@ -320,6 +338,14 @@ __device__ __forceinline__ void weno53_cell_f(float v, float dm2, float dm1, flo
     const float dl = fmaf(6.0f, P2, fmaf(18.0f, P0, m));
     ur = fmaf(nr, rcp_approx_f32(dr), v);
     ul = fmaf(nl, rcp_approx_f32(dl), v);
+}
+
+// the same from the four differences d_{c-2} .. d_{c+1} of the cell's stencil
+__device__ __forceinline__ void weno53_cell_f(float v, float dm2, float dm1, float d0, float dp1,
+                                              float eps4, float& ul, float& ur) {
+    const float Em1 = dm1 - dm2, E0 = d0 - dm1, Ep1 = dp1 - d0;
+    weno53_cell_fg(v, dm1, d0, Em1, E0, Ep1, weno53_g_f(Em1, eps4), weno53_g_f(E0, eps4),
+                   weno53_g_f(Ep1, eps4), ul, ur);
 }
 
 // 2|x| from the bit pattern of |x| (integer exponent increment, exact for
@@ -457,7 +483,7 @@ __device__ __forceinline__ T rusanov_face(T R, T L, T vj, T vj1, T hnu, T c) {
     if constexpr (EQ == SHK_EQ_BURGERS) {
         return fma(T(0.25), fma(L, L, R * R), -diss);
     } else {
-        return fma(T(0.5), phys_flux<EQ>(L, c) + phys_flux<EQ>(R, c), -diss);
+        return fma(T(0.5), phys_flux_sum<EQ>(L, R, c), -diss);
     }
 }
 
@@ -468,7 +494,7 @@ __device__ __forceinline__ T lf_face(T R, T L, T hnu_amax, T c) {
     if constexpr (EQ == SHK_EQ_BURGERS) {
         return fma(T(0.25), fma(L, L, R * R), -diss);
     } else {
-        return fma(T(0.5), phys_flux<EQ>(L, c) + phys_flux<EQ>(R, c), -diss);
+        return fma(T(0.5), phys_flux_sum<EQ>(L, R, c), -diss);
     }
 }
 

@@ -595,17 +595,18 @@ __device__ unsigned long long step_tile_mixed(const Smem<double>& sm, Win<double
     return mx;
 }
 
-// Float state, WENO-JS5 + Rusanov: each stage in one pass over the window. A
-// warp takes 30 consecutive output cells cb .. cb+29; its 32 lanes
-// reconstruct cells cb-1 .. cb+30 (weno53_cell_f from the five window values),
-// the left face value and the cell value of the right neighbour come from the
-// lane above by shuffle, each lane forms the flux of its right face, and the
-// flux of its left face comes from the lane below. Lanes 1 .. 30 update their
-// cell. One barrier per stage (the staged face-value and flux arrays of the
-// three-pass stage took three), the same operations in the same order, so the
-// same results bit for bit; 32 reconstructions serve 30 cells. The stages
-// ping-pong between S (k1) and UL (k2), since a warp's output cells are other
-// warps' stencil inputs.
+// Float state, WENO-JS5 + Rusanov: each stage in one pass over the window,
+// two adjacent cells per lane. A warp reconstructs the 64 cells r0 .. r0+63
+// (r0 even), lane L the pair c0 = r0 + 2L, c0 + 1: its six window values come
+// in three aligned 8-byte loads, and the pair shares its differences d,
+// second differences E and the terms G = 13/3 E^2 + 4 eps (weno53_cell_fg).
+// Each lane forms the fluxes of both its cells' right faces (the left face
+// value of the next pair comes from the lane above by shuffle) and takes the
+// flux of its first cell's left face from the lane below. The warp updates
+// the 62 cells r0+1 .. r0+62. One barrier per stage, the same operations in
+// the same order per cell as the one-cell-per-lane stage, so the same results
+// bit for bit. The stages ping-pong between S (k1) and UL (k2), since a warp's
+// output cells are other warps' stencil inputs.
 template <int EQ>
 __device__ unsigned int step_tile_f32_weno(const Smem<float>& sm, Win<float> gout, int te, float dtdx,
                                            const OpParams<float>& p, const BcView& bc, int64_t g0,
@@ -619,33 +620,70 @@ __device__ unsigned int step_tile_f32_weno(const Smem<float>& sm, Win<float> gou
     const float eps4 = 4.0f * p.eps;
     const Win<float> K2 = sm.UL;
     unsigned int mx = 0;
-    // stage s reads v on [lo-3, hi+3) and updates [lo, hi)
+    auto ld2 = [](const Win<float>& a, int i) {  // a[i], a[i+1]; i even
+        return *reinterpret_cast<const float2*>(win_span(a, i, 2));
+    };
+    // stage s reads v on [lo-3, hi+3) and updates [lo, hi); pairs past hi
+    // are clamped to the last even start at or below hi (their values only
+    // feed unused faces), which keeps every load inside [lo-4, hi+4)
     auto stage = [&](const Win<float>& v, int lo, int hi, int s) {
-        for (int cb = lo + 30 * warp; cb < hi; cb += 30 * nw) {
-            const int c = cb - 1 + lane;
-            const int cc = c < hi ? c : hi;  // cells past hi only feed unused faces
-            const float vm2 = v[cc - 2], vm1 = v[cc - 1], v0 = v[cc], vp1 = v[cc + 1], vp2 = v[cc + 2];
-            float ul, ur;
-            weno53_cell_f(v0, vm1 - vm2, v0 - vm1, vp1 - v0, vp2 - vp1, eps4, ul, ur);
-            const float uln = __shfl_down_sync(kFull, ul, 1);
-            const float vn = __shfl_down_sync(kFull, v0, 1);
-            const float f = rusanov_face<EQ, float>(ur, uln, v0, vn, p.hnu, p.c);  // face c + 1/2
-            const float fl = __shfl_up_sync(kFull, f, 1);                        // face c - 1/2
-            if (lane >= 1 && lane <= 30 && c < hi) {
-                if (s == 1) {
-                    const float d = dtdx * (fl - f);
-                    sm.I[c] = d;
-                    sm.S[c] = sm.U[c] + d;
-                } else if (s == 2) {
-                    const float d = 0.25f * (sm.I[c] + dtdx * (fl - f));
-                    sm.I[c] = d;
-                    K2[c] = sm.U[c] + d;
-                } else {
-                    const float un = sm.U[c] + (2.0f / 3.0f) * (sm.I[c] + dtdx * (fl - f));
-                    gout[c - HL] = un;
-                    const unsigned int b = abs_bits(wave_speed<EQ>(un, p.c));
-                    mx = b > mx ? b : mx;
+        const int cmax = hi & ~1;
+        for (int r0 = ((lo - 1) & ~1) + 62 * warp; r0 + 1 < hi; r0 += 62 * nw) {
+            const int c0 = r0 + 2 * lane;
+            const int cc = c0 < cmax ? c0 : cmax;
+            const float2 wa = ld2(v, cc - 2), wb = ld2(v, cc), wc = ld2(v, cc + 2);
+            const float dA = wa.y - wa.x, dB = wb.x - wa.y, dC = wb.y - wb.x, dD = wc.x - wb.y,
+                        dE = wc.y - wc.x;
+            const float EB = dB - dA, EC = dC - dB, ED = dD - dC, EE = dE - dD;
+            const float GB = weno53_g_f(EB, eps4), GC = weno53_g_f(EC, eps4), GD = weno53_g_f(ED, eps4),
+                        GE = weno53_g_f(EE, eps4);
+            float ula, ura, ulb, urb;
+            weno53_cell_fg(wb.x, dB, dC, EB, EC, ED, GB, GC, GD, ula, ura);
+            weno53_cell_fg(wb.y, dC, dD, EC, ED, EE, GC, GD, GE, ulb, urb);
+            const float uln = __shfl_down_sync(kFull, ula, 1);  // left face value of cell c0 + 2
+            const float fa = rusanov_face<EQ, float>(ura, ulb, wb.x, wb.y, p.hnu, p.c);  // c0 + 1/2
+            const float fb = rusanov_face<EQ, float>(urb, uln, wb.y, wc.x, p.hnu, p.c);  // c0 + 3/2
+            const float fl = __shfl_up_sync(kFull, fb, 1);                               // c0 - 1/2
+            const bool va = lane >= 1 && c0 >= lo && c0 < hi;
+            const bool vb = lane <= 30 && c0 + 1 >= lo && c0 + 1 < hi;
+            if (!(va || vb)) continue;
+            const float2 u = ld2(sm.U, cc);
+            const float ra = dtdx * (fl - fa), rb = dtdx * (fa - fb);
+            if (s == 3) {
+                const float2 inc = ld2(sm.I, cc);
+                const float una = u.x + (2.0f / 3.0f) * (inc.x + ra);
+                const float unb = u.y + (2.0f / 3.0f) * (inc.y + rb);
+                if (va) {
+                    gout[c0 - HL] = una;
+                    const unsigned int bb = abs_bits(wave_speed<EQ>(una, p.c));
+                    mx = bb > mx ? bb : mx;
                 }
+                if (vb) {
+                    gout[c0 + 1 - HL] = unb;
+                    const unsigned int bb = abs_bits(wave_speed<EQ>(unb, p.c));
+                    mx = bb > mx ? bb : mx;
+                }
+                continue;
+            }
+            float da, db;
+            if (s == 1) {
+                da = ra;
+                db = rb;
+            } else {
+                const float2 inc = ld2(sm.I, cc);
+                da = 0.25f * (inc.x + ra);
+                db = 0.25f * (inc.y + rb);
+            }
+            const Win<float>& out = s == 1 ? sm.S : K2;
+            if (va && vb) {
+                *reinterpret_cast<float2*>(win_span(sm.I, c0, 2)) = make_float2(da, db);
+                *reinterpret_cast<float2*>(win_span(out, c0, 2)) = make_float2(u.x + da, u.y + db);
+            } else if (va) {
+                sm.I[c0] = da;
+                out[c0] = u.x + da;
+            } else {
+                sm.I[c0 + 1] = db;
+                out[c0 + 1] = u.y + db;
             }
         }
         __syncthreads();
