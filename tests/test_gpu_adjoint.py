@@ -275,21 +275,27 @@ def test_stored_stages_and_faces_give_the_same_gradient(boundary):
     assert torch.equal(grads[0], grads[1])
 
 
-def test_plain_results_do_not_depend_on_the_tile():
-    """Plain WENO-JS5 in double: forward steps and reverse sweeps give the same
-    values, bit for bit, at tiles of 64, 512 and 1024 cells (more halo than
-    interior, the reverse sweep's default, the forward's default)."""
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_plain_results_do_not_depend_on_the_tile(dtype):
+    """Plain WENO-JS5: forward steps and reverse sweeps give the same values,
+    bit for bit, at tiles of 64, 512 and 1024 cells (more halo than interior,
+    the reverse sweep's default, the float64 forward's default) and in float32
+    also 2048 (its forward default; a float64 reverse step of 2048 cells does
+    not fit in shared memory). In float32 the forward stage takes two cells
+    per lane, so odd instance and stage lengths end a warp's pairs at every
+    parity."""
     from pyshocks_gb300.adjoint import CheckpointedSolve
     from pyshocks_gb300.batched import BatchedSolver
 
-    sizes = [4096, 1500, 600, 96]
+    sizes = [4096, 1500, 601, 96, 33]
     nsteps = 9
     rng = np.random.default_rng(47)
     u0 = np.concatenate([R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)) for n in sizes])
-    p_T = torch.tensor(rng.standard_normal(u0.size), device="cuda")
+    p_T = torch.tensor(rng.standard_normal(u0.size), device="cuda", dtype=dtype)
     outs, grads = [], []
-    for tile in (64, 512, 1024):
-        s = BatchedSolver(_scheme(), sizes, [2.0 / n for n in sizes], tile=tile, max_steps=nsteps)
+    for tile in (64, 512, 1024) + ((2048,) if dtype == torch.float32 else ()):
+        s = BatchedSolver(_scheme(), sizes, [2.0 / n for n in sizes], tile=tile, max_steps=nsteps,
+                          dtype=dtype)
         cs = CheckpointedSolve(s, nsteps, stride=4)
         outs.append(cs.forward(torch.tensor(u0)).clone())
         grads.append(cs.backward(p_T))
@@ -297,6 +303,31 @@ def test_plain_results_do_not_depend_on_the_tile():
     for o, g in zip(outs[1:], grads[1:]):
         assert torch.equal(o, outs[0])
         assert torch.equal(g, grads[0])
+
+
+@pytest.mark.parametrize("boundary", ["periodic", "neumann"])
+def test_float32_lwr_steps_do_not_depend_on_the_tile(boundary):
+    """The float32 forward step with the LWR flux (the flux sum f(L) + f(R)
+    rounded term by term) gives the same states, bit for bit, at every tile,
+    periodic or with homogeneous Neumann ghosts."""
+    from pyshocks_gb300.batched import BatchedSolver
+
+    sizes = [2048, 1500, 601, 96, 33, 7]
+    rng = np.random.default_rng(53)
+    u0 = np.concatenate([np.clip(0.5 + 0.3 * R.random_fourier_ic(rng, np.linspace(-1, 1, n + 1)), 0, 1)
+                         for n in sizes])
+    outs = []
+    for tile in (64, 512, 2048):
+        s = BatchedSolver(_scheme("lwr"), sizes, [2.0 / n for n in sizes], tile=tile,
+                          dtype=torch.float32)
+        if boundary == "neumann":
+            s.set_boundary("neumann", neumann=(0.0, 0.0))
+        s.reset(torch.tensor(u0, dtype=torch.float32))
+        outs.append(s.step(40).clone())
+        assert s.status() == 0
+    assert torch.isfinite(outs[0]).all()
+    for o in outs[1:]:
+        assert torch.equal(o, outs[0])
 
 
 def test_step_and_adjoint_step_through_npz_checkpoints(tmp_path):
