@@ -570,7 +570,11 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
     """Learned-weight WENO against the plain float64 kernel: forward rate on
     B=4096 x N=4096, adjoint rate on the adjoint configuration, and L1 error
     at t=0.4 against the plain float64 solution on a 4x finer grid (restricted
-    by averaging) for B=64 instances of the same initial-condition family."""
+    by averaging) for ``--accuracy-batch`` instances (512 by default) of the
+    same initial-condition family. The fine solution stays in float64: a
+    float32 one raised every scheme's L1 by about 1.3e-5 (6 %), alike for all,
+    which shifts the equal-error comparison; in float64 the configuration's
+    4096 instances would take the fine grid about 190 s."""
     import torch
 
     from pyshocks_gb300 import burgers, learned
@@ -595,11 +599,11 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
         rates[name] = B * n / (_timed_steps(s, u0, k, stream) * 1e-3)
         del s
     # accuracy
-    Bl, r, T = 64, 4, 0.4
+    Bl, r, T = args.accuracy_batch, 4, 0.4
     prm = workload_params(SEED + 5, batch=Bl)[1]
 
     def run(sch, nn, dt):
-        """The B=64 accuracy set on nn cells to t=T: (state, steps taken)."""
+        """The accuracy set on nn cells to t=T: (state, mean steps taken)."""
         s = BatchedSolver(sch, [nn] * Bl, 2.0 / nn, dtype=dt, max_steps=2 * nn)
         with torch.cuda.stream(stream):
             s.reset(initial_state(np.full(Bl, nn), prm, dev), tfinal=T)
@@ -617,10 +621,12 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
     nf = n * r
     cum = torch.cat([torch.zeros(Bl, 1, dtype=torch.float64, device=dev),
                      torch.cumsum(fine, -1) * (2.0 / nf)], -1)
+    del fine
 
     def l1(u):
         """L1 distance to the fine solution averaged onto u's cells (exact
-        cell averages of the piecewise-constant fine solution, any N)."""
+        cell averages of the piecewise-constant fine solution, any N), mean
+        over the instances."""
         nn = u.shape[-1]
         xf = torch.arange(nn + 1, dtype=torch.float64, device=dev) * (nf / nn)
         i0 = torch.clamp(xf.floor().long(), max=nf - 1)
@@ -651,7 +657,8 @@ def bench_learned(plain, dev, stream, args, adjoint_plain) -> dict:
                     "learned_f32": adj["learned_f32"]["value"],
                     "speedup_learned_f64": adj["learned_f64"]["value"] / adjoint_plain["value"],
                     "speedup_learned_f32": adj["learned_f32"]["value"] / adjoint_plain["value"]},
-        "l1_vs_fine_plain": {"config": {"batch": Bl, "n": n, "t_final": T, "fine": n * r},
+        "l1_vs_fine_plain": {"config": {"batch": Bl, "n": n, "t_final": T, "fine": n * r,
+                                        "fine_state": "float64"},
                              **err, "steps": {k_: v[1] for k_, v in runs.items()}},
         "iso_l1": iso,
         "note": ("learned_f64 keeps the state and its accumulation in float64 and runs the "
@@ -688,7 +695,7 @@ def bench_iso_l1(plain, lscheme, run, l1, err, runs, rates, stream, dev, args, B
         return r
 
     out = {"target_l1": target, "learned_n": n,
-           "config": {"batch": B, "t_final": T, "accuracy_batch": 64}}
+           "config": {"batch": B, "t_final": T, "accuracy_batch": args.accuracy_batch}}
     lsteps = runs["learned_f64"][1]
     t_learned = B * n * lsteps / rates["learned_f64"]
     out["learned_f64"] = {"n": n, "l1": target, "steps": lsteps, "rate": rates["learned_f64"],
@@ -805,6 +812,9 @@ def main() -> None:
     ap.add_argument("--e2e-chunks", type=int, default=0,
                     help="chunks of the pipelined host-buffer e2e leg (0: the library default)")
     ap.add_argument("--adjoint-steps", type=int, default=4000)
+    ap.add_argument("--accuracy-batch", type=int, default=512,
+                    help="instances of the learned-vs-plain L1 comparison (their float64 "
+                         "solution on the 4x finer grid costs about 24 s per 512)")
     ap.add_argument("--accuracy-steps", type=int, default=2000,
                     help="steps of the float32-vs-float64 comparison of the batch (full: 2000)")
     ap.add_argument("--inverse-steps", type=int, default=3000,
