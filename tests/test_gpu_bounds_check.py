@@ -8,9 +8,10 @@ instead of touching memory (``include/shocks_check.h``). With no memory checker
 available on the target machines, this build is the memory-safety evidence:
 
 * the oracle-parity tests of the forward, boundary, adjoint, learned and
-  no-allocation paths run again, with every parameter set they declare, with
-  the checked library in place of the product one, and must leave the log
-  empty (their own oracle tolerances still apply);
+  no-allocation paths and the tile-independence tests of the plain steps run
+  again, with every parameter set they declare and the checked library in
+  place of the product one, and must leave the log empty (their own oracle
+  tolerances still apply);
 * ragged and odd-sized batches (7, 50, 333 and 3001 cells; tiles 64 and 1024;
   float64 and float32) match the oracle with plan status 0;
 * the forced-timeout hook makes the loader's bounded wait expire on a tiny plan
@@ -85,6 +86,8 @@ RERUN = [
     ("test_gpu_adjoint", "test_single_step_vjp_matches_autograd"),
     ("test_gpu_adjoint", "test_batched_checkpointed_gradient_matches_autograd"),
     ("test_gpu_adjoint", "test_stored_stages_and_faces_give_the_same_gradient"),
+    ("test_gpu_adjoint", "test_plain_results_do_not_depend_on_the_tile"),
+    ("test_gpu_adjoint", "test_float32_lwr_steps_do_not_depend_on_the_tile"),
     ("test_gpu_learned", "test_learned_batched_step_matches_oracle"),
     ("test_gpu_learned", "test_learned_adjoint_matches_autograd"),
     ("test_gpu_learned", "test_stored_stage_states_give_the_same_gradient"),
