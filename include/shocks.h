@@ -291,7 +291,7 @@ int shk_plan_forward_checkpointed(shk_plan* plan, void* u_a, void* u_b, int32_t 
  * backwards (sqrt(nsteps) checkpointing when stride ~ sqrt(nsteps)). Rusanov +
  * WENO-JS53 only. */
 /* SHK_EUNSUPPORTED when the plan's tile is too long for the reverse step's
- * shared memory (about 1140 cells in float64, 2600 with the learned
+ * shared memory (about 1140 cells in float64, 2500 in float64 with the learned
  * reconstruction, 2300 in float32). */
 int shk_plan_adjoint(shk_plan* plan, const void* ckpt, int32_t stride, int32_t nsteps,
                      void* seg, void* p_a, void* p_b, void* stream);

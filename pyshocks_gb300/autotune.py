@@ -61,22 +61,33 @@ def shape_key(scheme, sizes: Sequence[int], dtype: torch.dtype, device) -> str:
                        str(dtype), int(sizes.size), hist], sort_keys=True)
 
 
+#: static shared memory of the kernels with the learned reconstruction: the
+#: staged network fragments (forward; forward and backward in the reverse step)
+LEARNED_STATIC = 3584
+LEARNED_STATIC_ADJOINT = 6400
+
+
 def _smem_bytes(tile: int, dtype: torch.dtype, learned: bool = False, weno5: bool = False) -> int:
     # the step tile's shared memory: 7 double arrays of the window (halo 10),
-    # or for the learned reconstruction the double window plus 7 float arrays;
-    # for float32 states (halo 12) 6 float arrays with WENO-JS5, else 8
+    # or for the learned reconstruction the double window plus 6 float arrays
+    # (the face-flux array at least 1028 floats); for float32 states (halo 12)
+    # 6 float arrays with WENO-JS5, else 8
     if dtype == torch.float64:
-        return (tile + 20) * (8 + 7 * 4 if learned else 7 * 8)
-    return (6 if weno5 else 8) * (tile + 24) * 4
+        w = tile + 20
+        if learned:
+            return w * 8 + (5 * w + max(w, 1028)) * 4 + LEARNED_STATIC
+        return w * 7 * 8
+    return (6 if weno5 else 8) * (tile + 24) * 4 + (LEARNED_STATIC if learned else 0)
 
 
 def _adjoint_smem_bytes(tile: int, dtype: torch.dtype, learned: bool = False) -> int:
     # the reverse step: 24 windows (halo 20) of the state type, or for float64
     # with the learned reconstruction 22 float windows
     w = tile + 40
+    extra = LEARNED_STATIC_ADJOINT if learned else 0
     if dtype == torch.float64:
-        return w * (22 * 4 if learned else 24 * 8)
-    return w * 24 * 4
+        return w * (22 * 4 if learned else 24 * 8) + extra
+    return w * 24 * 4 + extra
 
 
 def candidates(dtype: torch.dtype, max_cells: int, learned: bool = False,
