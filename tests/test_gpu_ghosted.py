@@ -6,7 +6,9 @@ the NumPy oracle by ``tests/test_oracle.py``); and the reference adjoint
 driver (``drivers/burgers-adjoint.py``: global Lax-Friedrichs, alpha 0.995,
 constant reconstruction on a one-ghost grid, Dirichlet forward boundary,
 homogeneous Neumann adjoint boundary, p0 = u(T)) end to end through ``step``
-and ``adjoint_step``.
+and ``adjoint_step``; and, for a linear scheme, the transpose against the
+whole finite-difference Jacobian of the forward step (the reference's
+``tests/test_finite_difference.py`` check).
 
 Tolerances: operator and step 1e-12 relative to the data scale (different
 summation order, and (2k+1) dx for the Neumann mirror distance where the
@@ -257,3 +259,59 @@ def test_reference_adjoint_driver_end_to_end(ic):
     else:
         assert np.max(d) <= 1.0e-9 * scale, np.max(d)
         assert np.max(np.abs(got - sweep(True))) > 0.1 * scale
+
+
+@pytest.mark.parametrize("kind", ["periodic", "dirichlet"])
+def test_linear_step_transpose_matches_finite_difference_jacobian(kind):
+    """The reference's finite-difference check of a linear scheme's Jacobian
+    (``tests/test_finite_difference.py:110-171``: constant reconstruction,
+    periodic or zero Dirichlet data, n = 32, central differences of every
+    component) on the ghosted GPU step: linear advection (c = 1) with the
+    Rusanov flux and the constant reconstruction is linear in u, so central
+    differences of the forward step give its whole Jacobian, ghost rows and
+    columns included, up to rounding, and the matrix-free transpose applied to
+    every unit cotangent must give its transpose. Bars: at the reference's
+    eps = 1e-3 the float64 rounding of the two steps divided by 2 eps is the
+    floor (the torch restatement itself lands at 1.0e-13 there), so 5e-13; at
+    eps = 1 (exact for a linear map) 1e-14 (the restatement: 1.3e-16)."""
+    from pyshocks_gb300 import _lib as L
+
+    n, g = 32, 1
+    dx = 2.0 / n
+    dt = 0.5 * dx
+    m = n + 2 * g
+    s = L.ShkScheme(flux=L.SHK_FLUX_RUSANOV, rec=L.SHK_REC_CONSTANT, equation=L.SHK_EQ_ADVECTION,
+                    eps=1.0e-6, delta=0.0, nu=1.0, speed=1.0)
+    b = L.ShkBoundary()
+    b.left = b.right = L.SHK_BC_PERIODIC if kind == "periodic" else L.SHK_BC_DIRICHLET
+    ws = _ws(L, n, g)
+    u = np.random.default_rng(42).standard_normal(m)
+
+    def step(v):
+        vd = torch.tensor(v, device="cuda")
+        out = torch.empty_like(vd)
+        st = L.lib().shk_ssprk33_step_ghosted_f64(s, ctypes.byref(b), vd.data_ptr(), out.data_ptr(),
+                                                  n, g, dx, dt, ws.data_ptr(), ws.numel(),
+                                                  L.stream_handle())
+        assert st == 0, L.errstr(st)
+        return out.cpu().numpy()
+
+    ud = torch.tensor(u, device="cuda")
+    jt = np.empty((m, m))
+    for i in range(m):
+        pd = torch.zeros(m, dtype=torch.float64, device="cuda")
+        pd[i] = 1.0
+        out = torch.empty_like(ud)
+        st = L.lib().shk_ssprk33_vjp_ghosted_f64(s, ctypes.byref(b), ud.data_ptr(), pd.data_ptr(),
+                                                 out.data_ptr(), n, g, dx, dt, ws.data_ptr(),
+                                                 ws.numel(), L.stream_handle())
+        assert st == 0, L.errstr(st)
+        jt[:, i] = out.cpu().numpy()  # column i of J^T = row i of J
+    for eps, bar in ((1.0e-3, 5.0e-13), (1.0, 1.0e-14)):
+        fd = np.empty((m, m))
+        for i in range(m):
+            e = np.zeros(m)
+            e[i] = eps
+            fd[:, i] = (step(u + e) - step(u - e)) / (2.0 * eps)
+        err = np.linalg.norm(jt.T - fd) / np.linalg.norm(fd)
+        assert err < bar, (eps, err)
