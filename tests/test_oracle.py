@@ -117,6 +117,24 @@ def test_torch_oracle_runs_golden(name, flux_kind, equation, kw):
 # {{{ ports of the reference's property tests
 
 
+def test_convolve_same_vs_scipy():
+    """``tests/test_utils.py:21-86`` compares the reference's ``convolve1d``
+    with ``scipy.ndimage.convolve1d`` for its padded modes; the path uses the
+    "same" mode (zero padding, ``src/pyshocks/convolve.py:113-114``), which for
+    the odd stencil lengths of the reconstructions is scipy's ``constant``
+    mode. Random sizes as in the reference test, relative error below 1e-12."""
+    snd = pytest.importorskip("scipy.ndimage")
+    rng = np.random.default_rng(seed=42)
+    for _ in range(16):
+        n = int(rng.integers(126, 384))
+        m = 2 * int(rng.integers(1, 14)) + 1
+        a = rng.random(n)
+        w = rng.random(m)
+        ref = snd.convolve1d(a, w, mode="constant", cval=0.0)
+        got = R.convolve1d(a, w)
+        assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1.0e-12, (n, m)
+
+
 @pytest.mark.parametrize("rec_name", ["wenojs32", "wenojs53"])
 def test_weno_smoothness_indicator_vectorization(rec_name):
     """``tests/test_weno.py:34-108``: loop vs convolution, rtol 2e-15."""
