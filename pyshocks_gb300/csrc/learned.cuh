@@ -11,7 +11,8 @@
 // conservative. The trust band, per face: where the network puts more than
 // `band` of its weight on sub-stencils that WENO-JS marks as crossing a
 // discontinuity (JS weight below `tau`), or moves any weight more than `dev`
-// away from the WENO-JS weight, that face uses the plain WENO-JS weights.
+// away from the WENO-JS weight (dev = 1 never triggers), that face uses the
+// plain WENO-JS weights.
 //
 // Inference runs on the tensor cores: each warp evaluates 32 cells at a time
 // with mma.sync m16n8k16 (bf16 inputs, fp32 accumulate); the layer outputs stay

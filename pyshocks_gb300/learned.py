@@ -7,7 +7,9 @@ conservative. It plugs into the reference's reconstruction slot
 (``src/pyshocks/reconstruction.py:79-119``) as :class:`LearnedWENO`. Plain
 WENO-JS is the per-face fallback wherever the network leaves the trust band:
 more than ``band`` of its weight on sub-stencils whose JS weight is below
-``tau``, or any weight more than ``dev`` away from the JS weight.
+``tau`` (sub-stencils across a discontinuity), or, when ``dev`` < 1, any weight
+more than ``dev`` away from the JS weight (off by default: a weight-deviation
+cap of 0.5 raised the L1 error of the trained network by 25 %).
 
 Training pairs come from the plain solver itself: fine-grid runs (N = 4096)
 restricted to the coarse grid (N = 256, 16-cell averages) give coarse stencils,
@@ -75,7 +77,7 @@ class LearnedWENO(Reconstruction):
     eps: float = 1.0e-6
     tau: float = 1.0e-2
     band: float = 0.1
-    dev: float = 0.5
+    dev: float = 1.0
     #: floor of the stencil range in the input normalisation
     #: ``(s - mean) / (range + norm_eps)`` (the network's counterpart of eps)
     norm_eps: float = NORM_EPS
@@ -289,14 +291,14 @@ class Trainer:
 # }}}
 
 
-def train_default(*, n_ics: int = 640, epochs: int = 64, reg: float = 0.1, seed: int = 0,
+def train_default(*, n_ics: int = 640, epochs: int = 64, reg: float = 0.02, seed: int = 0,
                   lr: float = 1.0e-2, batch: int = 32768):
     """Train the default network: 5.2e6 cells (1.05e7 face targets; N = 256
     restricted from N = 4096, Burgers and linear advection, 0.5 + sin(pi x)-like and
     random-Fourier initial conditions), Adam with cosine decay to 1e-4.
     Returns ``(params, loss history)``. The committed default was made with
-    these arguments and ``NORM_EPS`` (the face loss falls from 6.3e-4 to
-    4.7e-4)."""
+    these arguments and ``NORM_EPS`` (the loss, face error plus the pull
+    toward the ideal weights, falls from 5.8e-4 to 3.6e-4)."""
     s, t, w = generate_pairs(n_coarse=256, ratio=16, n_ics=n_ics, snapshots=16,
                              steps_between=256, seed=seed)
     params = init_params(seed=seed)
