@@ -183,10 +183,12 @@ def test_stored_stage_states_give_the_same_gradient(dtype, boundary):
 def test_trained_network_gains_over_plain_wenojs_and_untrained():
     """What training buys. (1) Solver level: the committed network (learned
     weights in the flux kernel, float64 state) against plain WENO-JS5 (eps
-    1e-6) at N=1024, t=0.4, both measured by L1 against the plain float64
-    solution on a 4x finer grid restricted by averaging. (2) Data level: the
-    face loss on held-out training-style pairs, trained vs the network at
-    initialisation."""
+    1e-6) and against the network at initialisation (softmax at the ideal
+    weights) with the same trust band, at N=1024, t=0.4, all measured by L1
+    against the plain float64 solution on a 4x finer grid restricted by
+    averaging (the benchmark's 512-instance set at N=4096 measures 32 % and
+    14 %). (2) Data level: the face loss on held-out training-style pairs,
+    trained vs the network at initialisation."""
     from pyshocks_gb300 import burgers, learned, reconstruction
     from pyshocks_gb300.batched import BatchedSolver
 
@@ -216,7 +218,10 @@ def test_trained_network_gains_over_plain_wenojs_and_untrained():
 
     e_plain = l1(run(plain, n))
     e_learned = l1(run(burgers.Rusanov(rec=learned.LearnedWENO(params=trained)), n))
-    assert e_learned < 0.95 * e_plain, (e_learned, e_plain)
+    e_untrained = l1(run(burgers.Rusanov(rec=learned.LearnedWENO(params=learned.init_params(seed=0))), n))
+    print(f"L1 at N={n}: plain {e_plain:.4e}, trained {e_learned:.4e}, untrained {e_untrained:.4e}")
+    assert e_learned < 0.85 * e_plain, (e_learned, e_plain)
+    assert e_learned < 0.95 * e_untrained, (e_learned, e_untrained)
     # held-out pairs (seed not used for the committed network)
     s, t, w = learned.generate_pairs(n_coarse=128, ratio=8, n_ics=8, snapshots=4,
                                      steps_between=64, seed=12345)
@@ -279,8 +284,8 @@ def test_trained_network_steps_match_oracle(n, nsteps, kind, dtype):
     bfloat16 roundings differ. Flipping 1 % of the oracle's bfloat16 roundings
     moves these trajectories by at most 1.2e-5 of the initial range (L1 4e-7,
     a thousandth of the method's L1 error against the fine solution,
-    1.9e-4 at N=4096). The bar is 2e-3 of the range in max-abs and 2e-5 in
-    L1 (a tenth of the method error). The fraction of faces in the WENO-JS
+    1.6e-4 at N=4096). The bar is 2e-3 of the range in max-abs and 2e-5 in
+    L1 (an eighth of the method error). The fraction of faces in the WENO-JS
     fallback at the final state is reported (and must be below 5 %)."""
     from pyshocks_gb300 import learned
     from pyshocks_gb300.batched import BatchedSolver
