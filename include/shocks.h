@@ -70,7 +70,7 @@ typedef struct {
     float tau;         /* SHK_REC_LEARNED: JS weight marking a non-smooth sub-stencil */
     float band;        /* SHK_REC_LEARNED: max network weight on such sub-stencils */
     float dev;         /* SHK_REC_LEARNED: max |omega - omega_JS| per sub-stencil
-                        * (1: no cap)                                           */
+                        * (>= 1: no cap)                                        */
     float norm_eps;    /* SHK_REC_LEARNED: floor of the stencil range in the network's
                         * input normalisation (s - mean) / (range + norm_eps); <= 0
                         * means 1e-12 */

@@ -13,9 +13,8 @@ its smoothness indicators): ``omega_L = softmax(z2 - ln 3, z1, z0 + ln 3)``.
 Each face value is the convex combination ``sum_k omega_k uhat_k`` of its
 sub-stencil values, so the flux stays conservative. Where the network puts
 more than ``band`` of a face's weight on sub-stencils that WENO-JS marks as
-crossing a discontinuity (JS weight below ``tau``), or (with ``dev`` < 1)
-moves any weight more than ``dev`` from the JS weight, that face uses the
-plain WENO-JS weights.
+crossing a discontinuity (JS weight below ``tau``), or moves any weight more
+than ``dev`` from the JS weight, that face uses the plain WENO-JS weights.
 
 Parameter vector (1347 float32): W1[32,5], b1[32], W2[32,32], b2[32],
 W3[3,32], b3[3], row-major.
@@ -106,7 +105,7 @@ def _band(w, wjs, tau, band, dev):
     return (excess > band) | (torch.amax(torch.abs(w - wjs), dim=-1) > dev)
 
 
-def cell_face_values(params, s, *, eps: float, tau: float, band: float, dev: float = 1.0,
+def cell_face_values(params, s, *, eps: float, tau: float, band: float, dev: float = 0.8,
                      bf16: bool = False, return_fallback: bool = False,
                      norm_eps: float = NORM_EPS):
     """Learned ``(right, left)`` face values of cell stencils ``s[..., 5]``
@@ -131,7 +130,7 @@ def stencils_periodic(u: torch.Tensor):
 
 def learned_recon(u: torch.Tensor, weights: dict, eps: float):
     """``(ul, ur)`` of every cell for the torch oracle's ``face_flux``."""
-    kw = dict(eps=eps, tau=weights["tau"], band=weights["band"], dev=weights.get("dev", 1.0),
+    kw = dict(eps=eps, tau=weights["tau"], band=weights["band"], dev=weights.get("dev", 0.8),
               bf16=weights.get("bf16", False), norm_eps=weights.get("norm_eps", NORM_EPS))
     vr, vl = cell_face_values(weights["params"], stencils_periodic(u), **kw)
     return vl, vr

@@ -11,7 +11,7 @@
 // conservative. The trust band, per face: where the network puts more than
 // `band` of its weight on sub-stencils that WENO-JS marks as crossing a
 // discontinuity (JS weight below `tau`), or moves any weight more than `dev`
-// away from the WENO-JS weight (dev = 1 never triggers), that face uses the
+// away from the WENO-JS weight (dev >= 1 never triggers), that face uses the
 // plain WENO-JS weights.
 //
 // Inference runs on the tensor cores: each warp evaluates 32 cells at a time
