@@ -186,8 +186,8 @@ def test_trained_network_gains_over_plain_wenojs_and_untrained():
     1e-6) and against the network at initialisation (softmax at the ideal
     weights) with the same trust band, at N=1024, t=0.4, all measured by L1
     against the plain float64 solution on a 4x finer grid restricted by
-    averaging (the benchmark's 512-instance set at N=4096 measures 32 % and
-    14 %). (2) Data level: the face loss on held-out training-style pairs,
+    averaging (measured at N=1024: 23 % and 10 %; the benchmark's
+    512-instance set at N=4096: 32 % and 15 %). (2) Data level: the face loss on held-out training-style pairs,
     trained vs the network at initialisation."""
     from pyshocks_gb300 import burgers, learned, reconstruction
     from pyshocks_gb300.batched import BatchedSolver
