@@ -146,7 +146,8 @@ __device__ __forceinline__ void mma_bf16(float& d0, float& d1, float& d2, float&
 }
 
 // The network's B fragments in shared memory, staged once per launch by the
-// whole block (mlp_stage) and read at each use: register-resident fragments
+// whole block (mlp_stage_forward / mlp_stage_back, called by learned_stage in
+// stencil.cuh) and read at each use: register-resident fragments
 // held 38 registers per thread for the whole kernel and made the step spill.
 // Lane L's words sit at [.][L] as one 16-byte vector, so the warp's load of a
 // vector is 512 contiguous bytes (no bank conflicts). Fragments of lane
