@@ -70,3 +70,20 @@ def test_training_loss_gradient_is_finite_and_pulls_to_ideal():
     loss = LR.training_loss(pp, s, t, torch.ones(64, dtype=torch.float64), reg=0.5)
     (g,) = torch.autograd.grad(loss, pp)
     assert float(loss.detach()) < 1e-28 and float(g.abs().max()) < 1e-12
+
+
+def test_library_and_oracle_share_the_trust_band_defaults():
+    """The library's LearnedWENO trust-band defaults (tau, band, dev) and
+    normalisation floor are the oracle's, so tests that leave them out compare
+    the same scheme."""
+    import dataclasses
+    import inspect
+
+    from pyshocks_gb300 import learned
+
+    lib = {f.name: f.default for f in dataclasses.fields(learned.LearnedWENO)
+           if f.name in ("tau", "band", "dev", "norm_eps")}
+    sig = inspect.signature(LR.cell_face_values).parameters
+    assert lib["dev"] == sig["dev"].default == 0.8
+    assert lib["norm_eps"] == sig["norm_eps"].default == LR.NORM_EPS == learned.NORM_EPS
+    assert (lib["tau"], lib["band"]) == (1.0e-2, 0.1)
